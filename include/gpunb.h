@@ -1,0 +1,128 @@
+/*
+ * gpunb.h -- C ABI of libgpunb.so, the GB300 (sm_103a) regular-force library.
+ *
+ * Drop-in replacement for the reference's regular-force back-ends.  The first
+ * block of entry points keeps the exact Fortran-mangled names, argument
+ * meaning and in-band conventions that NBODY6++'s Fortran host code calls
+ * (src/Main/fpoly0.F:31,76,125; intgrt.F:168,918,1497; util_gpu.F:60;
+ * adjust.F:315,424; energy.F:38), so the Fortran side links against this
+ * library unchanged.  All array arguments are caller-owned HOST memory:
+ *   xj/vj/xi/vi/acc/jrk are C double[n][3] (Fortran X(3,N) column-major),
+ *   list is Fortran LISTGP(LMAX,NI): row i at list + i*lmax,
+ *   list[i*lmax] = count, list[i*lmax+1 .. count] = 0-based j indices into the
+ *   array given to gpunb_send_, ascending, the i-particle itself included;
+ *   count > nnbmax is reported as -count (entries undefined).
+ * Errors: the reference aborts through assert(); this library prints the
+ * reason and calls abort() by default too, or, after
+ * gpunb_set_abort_on_error(0), records the code for gpunb_last_error().
+ */
+#ifndef GPUNB_GB300_H
+#define GPUNB_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- reference ABI ----------------------------------------------------- */
+
+/* Select and initialise the device (reference: GPUNB_devinit,
+ * src/Main/gpunb.velocity.cu:574-626, export :905-907).  GPU_LIST picks the
+ * device (its first entry; one GPU per process). */
+void gpunb_devinit_(int *irank);
+
+/* Open the library for up to *nbmax j-particles (reference: GPUNB_open,
+ * gpunb.velocity.cu:628-666, export :908-910). */
+void gpunb_open_(int *nbmax, int *irank);
+
+/* Release device buffers (reference: GPUNB_close, gpunb.velocity.cu:668-701,
+ * export :911-913). */
+void gpunb_close_(void);
+
+/* Upload the j-set: nj bodies, masses mj[nj], positions xj[nj][3], velocities
+ * vj[nj][3] (FP64, already predicted to the current time) (reference:
+ * GPUNB_send, gpunb.velocity.cu:703-729, export :914-920). */
+void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]);
+
+/* Regular force, jerk, potential and neighbour lists of *ni i-particles
+ * against the whole j-set (reference: GPUNB_regf, gpunb.velocity.cu:731-880,
+ * export :921-935; CPU variant src/Main/reg.avx.cpp:185-331).
+ *   h2[i]  neighbour radius squared (RS**2, or RS**2/BODYM when *m_flag)
+ *   dtr[i] regular step for the predicted-distance criterion
+ *   neighbour iff min(r2, |dx + dtr dv|^2) < h2 (< m_j h2 when *m_flag);
+ *   neighbours are excluded from acc, jrk and pot; pot is +sum m/r.
+ * Differences from the reference, all in the direction of fewer limits:
+ * no NIMAX cap on ni, no 2^21 cap on the total list length, no per-j-block
+ * 256 cap; overflow is count > nnbmax only. */
+void gpunb_regf_(int *ni, double h2[], double dtr[], double xi[][3], double vi[][3],
+                 double acc[][3], double jrk[][3], double pot[], int *lmax, int *nnbmax,
+                 int *list, int *m_flag);
+
+/* Print and reset the call counters in the reference's format
+ * (reference: GPUNB_profile, gpunb.velocity.cu:882-902, export :936-938). */
+void gpunb_profile_(int *irank);
+
+/* Potential for the energy check: pot[k] = sum_{j: r2 > 0} m_j / r_ij for
+ * i = istart-1+k, k < ni, over n bodies (reference: gpupot_,
+ * src/Main/gpupot.gpu.cu:61-127; CPU src/Main/pot.avx.cpp:72-159). */
+void gpupot_(int *irank, int *istart, int *ni, int *n, double m[], double x[][3],
+             double pot[]);
+
+/* ---- additions of this library (no reference counterpart) -------------- */
+
+/* Error codes (0 = none). */
+enum {
+  GPUNB_OK = 0, GPUNB_E_NOT_OPEN = 1, GPUNB_E_ARG = 2, GPUNB_E_NAN = 3,
+  GPUNB_E_CUDA = 4, GPUNB_E_CAPACITY = 5, GPUNB_E_TIMEOUT = 6,
+  GPUNB_E_NO_DEVICE = 7, GPUNB_E_ALLOC = 8
+};
+int gpunb_last_error(void);                 /* code of the first error since clear */
+const char *gpunb_last_error_message(void); /* text of that error */
+void gpunb_clear_error(void);
+void gpunb_set_abort_on_error(int flag);    /* 1 (default): print + abort() */
+
+/* Pair kernel selection: 0 = split precision (FP32 arithmetic on double-single
+ * positions, FP64 merges and neighbour re-tests; default), 1 = plain FP64. */
+void gpunb_set_precision(int mode);
+
+/* Force a launch shape (variant index, j-splits); -1/0 restores the
+ * autotuned or heuristic choice.  gpunb_num_variants() lists the shapes. */
+void gpunb_set_launch(int variant, int splits);
+int gpunb_num_variants(void);
+int gpunb_variant_info(int variant, int *ipt, int *warps_i, int *warps_j);
+
+/* Autotuner: time every shape for (nj, ni) on the current j-set with
+ * synthetic i-particles drawn from it, keep the fastest, and cache it per
+ * (nj bucket, ni bucket).  Returns the chosen variant; *splits, *ms out. */
+int gpunb_autotune(int ni, int m_flag, int *splits, float *ms);
+/* Load / save the tuning cache (text file); return the number of entries. */
+int gpunb_tune_load(const char *path);
+int gpunb_tune_save(const char *path);
+
+/* Time the pair kernel of each subsequent regf call with a pair of CUDA events
+ * recorded on the stream it is launched on.  gpunb_kernel_times() waits for
+ * the recorded launches, writes up to max durations (ms) in launch order,
+ * returns their number and starts a new record; gpunb_last_kernel_ms()
+ * returns the last duration read. */
+void gpunb_set_timing(int flag);
+int gpunb_kernel_times(float *ms, int max);
+float gpunb_last_kernel_ms(void);
+/* Launch shape used by the last regf call. */
+void gpunb_last_launch(int *variant, int *splits, int *grid_x);
+
+/* Device-resident variants: all pointers are device memory, work is queued
+ * on `stream` (a cudaStream_t; NULL = the library's stream) and nothing is
+ * copied to the host.  regf writes acc[ni][3], jrk[ni][3], pot[ni], nnb[ni]
+ * (count or -count), list_off[ni+1] (offsets of accepted rows in list) and
+ * list[...] (capacity list_cap ints; ni*nnbmax always suffices). */
+int gpunb_send_device(int nj, const double *m, const double *x, const double *v, void *stream);
+int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double *xi,
+                      const double *vi, double *acc, double *jrk, double *pot, int *nnb,
+                      int *list_off, int *list, size_t list_cap, int nnbmax, int m_flag,
+                      void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUNB_GB300_H */

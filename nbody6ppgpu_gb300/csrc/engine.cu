@@ -1,0 +1,889 @@
+// Host runtime of libgpunb.so: device state, buffers, launch planning,
+// autotuning, CUDA-graph replay, and the C ABI of include/gpunb.h.
+//
+// Reference host code replaced: src/Main/gpunb.velocity.cu:555-939 (static
+// state, GPUNB_devinit/open/close/send/regf/profile, extern "C" exports),
+// include/cuda_pointer.h (synchronous pinned/device pairs) and
+// src/Main/gpupot.gpu.cu:59-127.  Differences by design: one GPU per process,
+// j-set resident in HBM in a split-precision tiled layout built on the device,
+// one stream, asynchronous copies from pinned staging, device-side reductions
+// and list compaction (no host prefix sum and no second upload of offsets).
+#include <cerrno>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <algorithm>
+#include <map>
+#include <vector>
+#include <mutex>
+#include <string>
+#include <sys/time.h>
+#include <unistd.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "gpunb.h"
+#include "launch.h"
+
+namespace gpunb {
+
+// ---------------------------------------------------------------------------
+// errors
+static int g_err_code = 0;
+static std::string g_err_msg;
+static int g_abort_on_error = 1;
+
+static void fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (g_err_code == 0) {
+    g_err_code = code;
+    g_err_msg = buf;
+  }
+  fprintf(stderr, "gpunb: error %d: %s\n", code, buf);
+  if (g_abort_on_error) abort();
+}
+
+#define CUDA_OR(call, ret)                                                          \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      fail(GPUNB_E_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));            \
+      return ret;                                                                   \
+    }                                                                               \
+  } while (0)
+
+static double wtime() {
+  struct timeval tv;
+  gettimeofday(&tv, nullptr);
+  return tv.tv_sec + 1.e-6 * tv.tv_usec;
+}
+
+// ---------------------------------------------------------------------------
+// grow-only buffers
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  bool ensure(size_t n) {
+    if (n <= bytes) return true;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    size_t want = n + n / 4 + 256;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      fail(GPUNB_E_ALLOC, "cudaMalloc of %zu bytes failed", want);
+      return false;
+    }
+    bytes = want;
+    return true;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T> T *as() const { return (T *)p; }
+};
+
+struct PinBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  bool ensure(size_t n) {
+    if (n <= bytes) return true;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    size_t want = n + n / 4 + 256;
+    if (cudaMallocHost(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      fail(GPUNB_E_ALLOC, "cudaMallocHost of %zu bytes failed", want);
+      return false;
+    }
+    bytes = want;
+    return true;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T> T *as() const { return (T *)p; }
+};
+
+// parallel host copy for large staging transfers
+static void hcopy(void *dst, const void *src, size_t bytes) {
+#ifdef _OPENMP
+  if (bytes >= (4u << 20)) {
+    const int nt = omp_get_max_threads();
+    const size_t chunk = (bytes + nt - 1) / nt;
+#pragma omp parallel for schedule(static)
+    for (int t = 0; t < nt; ++t) {
+      const size_t b = (size_t)t * chunk;
+      if (b < bytes) memcpy((char *)dst + b, (const char *)src + b, std::min(chunk, bytes - b));
+    }
+    return;
+  }
+#endif
+  memcpy(dst, src, bytes);
+}
+
+// ---------------------------------------------------------------------------
+struct TuneEntry {
+  int variant, splits;
+  float ms;
+};
+
+struct Engine {
+  bool devinit = false, is_open = false;
+  int device = 0, n_sm = 0;
+  char devname[256] = {0};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ek0 = nullptr, ek1 = nullptr;   // autotuner timing
+  std::vector<cudaEvent_t> evpool;            // per-launch timing pairs
+  int evused = 0;
+  int nbodymax = 0;
+  // j-set
+  int nj = 0;
+  DevBuf jraw;     // m[nj] | x[nj][3] | v[nj][3]  (FP64 as sent)
+  DevBuf jtiles;   // split-precision tiles
+  PinBuf hj;
+  // i-set and work buffers
+  DevBuf iraw;     // h2[ni] | dtr[ni] | x[ni][3] | v[ni][3]
+  DevBuf part, cnt, rows, rowlen, off, btot, dense, outblk, err;
+  PinBuf hin, hout, hlist;
+  // configuration
+  int precision = 0;
+  int force_variant = -1, force_splits = 0;
+  int timing = 0;
+  float last_kernel_ms = 0.f;
+  int last_variant = -1, last_splits = 0, last_gx = 0;
+  std::map<long long, TuneEntry> tune;
+  int autotune_on = 0;
+  // profile counters (GPUNB_profile)
+  double time_send = 0, time_grav = 0, time_reduce = 0, time_out = 0;
+  long long num_inter = 0;
+  long long icall = 0, ini = 0, isend = 0;
+  // potential
+  DevBuf praw, ptiles, ppart, pout;
+  PinBuf hp;
+};
+
+static Engine g;
+static std::mutex g_mutex;
+
+// largest active block per call: the two-level list scan covers
+// SCAN_ITEMS * SCAN_ITEMS rows (4096 * 4096)
+constexpr int kMaxNi = 4096 * 4096;
+
+static bool devinit(int irank) {
+  if (g.devinit) return true;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    cudaGetLastError();
+    fail(GPUNB_E_NO_DEVICE, "no CUDA device visible");
+    return false;
+  }
+  int dev = 0;
+  if (const char *gl = getenv("GPU_LIST")) dev = atoi(gl);
+  if (dev < 0 || dev >= ndev) dev = 0;
+  CUDA_OR(cudaSetDevice(dev), false);
+  cudaDeviceProp prop;
+  CUDA_OR(cudaGetDeviceProperties(&prop, dev), false);
+  g.device = dev;
+  g.n_sm = prop.multiProcessorCount;
+  snprintf(g.devname, sizeof(g.devname), "%s", prop.name);
+  CUDA_OR(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking), false);
+  CUDA_OR(cudaEventCreate(&g.ek0), false);
+  CUDA_OR(cudaEventCreate(&g.ek1), false);
+  if (!g.err.ensure(sizeof(int))) return false;
+  char host[150] = {0};
+  gethostname(host, sizeof(host) - 1);
+  fprintf(stderr, "# GPU initialization - rank: %d; HOST %s; NGPU 1; device: %d %s\n", irank,
+          host, dev, prop.name);
+  g.devinit = true;
+  if (const char *p = getenv("GPUNB_TUNE_CACHE")) gpunb_tune_load(p);
+  if (const char *p = getenv("GPUNB_AUTOTUNE")) g.autotune_on = atoi(p);
+  return true;
+}
+
+// device error word -> host error
+static bool check_device_error(int code_from_device) {
+  if (code_from_device == 0) return true;
+  const char *what = code_from_device == GPUNB_E_NAN       ? "NaN in an input array"
+                     : code_from_device == GPUNB_E_TIMEOUT ? "a device wait timed out"
+                                                           : "device error";
+  fail(code_from_device, "%s", what);
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// j-set upload: FP64 arrays on the device + split-precision tiles
+static int send_common(int nj, cudaStream_t st) {
+  const int ntile = (nj + JT - 1) / JT;
+  if (!g.jtiles.ensure((size_t)std::max(ntile, 1) * TILE_BYTES)) return GPUNB_E_ALLOC;
+  double *m = g.jraw.as<double>();
+  CUDA_OR(launch_pack_jtiles(m, m + nj, m + 4 * (size_t)nj, nj, g.jtiles.as<float>(), ntile,
+                             g.err.as<int>(), st),
+          GPUNB_E_CUDA);
+  g.nj = nj;
+  return GPUNB_OK;
+}
+
+static JSet jset() {
+  JSet js;
+  const double *m = g.jraw.as<double>();
+  js.tiles = g.jtiles.as<float>();
+  js.m64 = m;
+  js.x64 = m + g.nj;
+  js.v64 = m + 4 * (size_t)g.nj;
+  js.nj = g.nj;
+  js.ntile = (g.nj + JT - 1) / JT;
+  js.ntile64 = (g.nj + JT64 - 1) / JT64;
+  return js;
+}
+
+// ---------------------------------------------------------------------------
+// launch planning
+static long long tune_key(int nj, int ni, int mflag, int prec) {
+  auto bucket = [](int n) {
+    if (n <= 1) return 0;
+    int b = 0;
+    while ((2ll << b) <= n) ++b;                      // floor(log2 n)
+    const int half = (n >= (3ll << b) / 2) ? 1 : 0;  // half-octave
+    return 2 * b + half;
+  };
+  return ((long long)bucket(nj) << 24) | ((long long)bucket(ni) << 8) | (mflag << 1) | prec;
+}
+
+static void heuristic_plan(int ni, int ntile, bool mflag, int &variant, int &splits) {
+  if (ni >= 16384) variant = 0;
+  else if (ni >= 2048) variant = 1;
+  else if (ni >= 256) variant = 3;
+  else variant = 2;
+  const VariantDesc d = regf_variant(variant);
+  const int gx = (ni + d.itile() - 1) / d.itile();
+  const int bps = regf_ds_blocks_per_sm(variant, mflag);
+  const long long want = 2ll * g.n_sm * bps;  // two waves of resident blocks
+  long long s = (want + gx - 1) / gx;
+  const int smax = std::max(1, ntile);
+  if (s > smax) s = smax;
+  if (s < 1) s = 1;
+  splits = (int)s;
+}
+
+static void fp64_plan(int ni, int ntile64, int &gx, int &splits) {
+  gx = (ni + FP64_THREADS - 1) / FP64_THREADS;
+  const long long want = 8ll * g.n_sm;
+  long long s = (want + gx - 1) / gx;
+  if (s > std::max(1, ntile64)) s = std::max(1, ntile64);
+  splits = (int)std::max(1ll, s);
+}
+
+// ---------------------------------------------------------------------------
+// the pair pass + merge + list compaction, all queued on `st`.
+// Inputs: device ISet; outputs: device acc/jrk/pot/nnb/dense list.
+struct RegfDev {
+  double *acc, *jrk, *pot;
+  int *nnb, *rowlen, *off, *btot, *dense;
+};
+
+static bool ensure_work(int ni, int nnbmax, int S, int ni_pad) {
+  return g.part.ensure((size_t)S * NQ * ni_pad * sizeof(double)) &&
+         g.cnt.ensure((size_t)ni * sizeof(int)) &&
+         g.rows.ensure((size_t)ni * std::max(nnbmax, 1) * sizeof(int));
+}
+
+static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, int S,
+                         cudaStream_t st, bool timed) {
+  const JSet js = jset();
+  const int ni = is.ni;
+  RegfOut out;
+  int gx;
+  if (g.precision == 1) {
+    gx = (ni + FP64_THREADS - 1) / FP64_THREADS;
+    out.ni_pad = gx * FP64_THREADS;
+  } else {
+    const VariantDesc d = regf_variant(variant);
+    gx = (ni + d.itile() - 1) / d.itile();
+    out.ni_pad = gx * d.itile();
+  }
+  if (!ensure_work(ni, nnbmax, S, out.ni_pad)) return GPUNB_E_ALLOC;
+  out.part = g.part.as<double>();
+  out.cnt = g.cnt.as<int>();
+  out.rows = g.rows.as<int>();
+  out.cap = std::max(nnbmax, 0);
+  out.err = g.err.as<int>();
+  CUDA_OR(cudaMemsetAsync(out.cnt, 0, (size_t)ni * sizeof(int), st), GPUNB_E_CUDA);
+  // events: the autotuner uses ek0/ek1; timing mode takes a fresh pair from
+  // the pool so that every launch of a timed region can be read afterwards
+  cudaEvent_t e0 = g.ek0, e1 = g.ek1;
+  const bool pooled = !timed && g.timing;
+  if (pooled) {
+    if ((int)g.evpool.size() < 2 * (g.evused + 1)) {
+      cudaEvent_t a, b;
+      CUDA_OR(cudaEventCreate(&a), GPUNB_E_CUDA);
+      CUDA_OR(cudaEventCreate(&b), GPUNB_E_CUDA);
+      g.evpool.push_back(a);
+      g.evpool.push_back(b);
+    }
+    e0 = g.evpool[2 * g.evused];
+    e1 = g.evpool[2 * g.evused + 1];
+    g.evused++;
+  }
+  if (timed || pooled) CUDA_OR(cudaEventRecord(e0, st), GPUNB_E_CUDA);
+  if (g.precision == 1) {
+    CUDA_OR(launch_regf_fp64(mflag, gx, S, js, is, out, st), GPUNB_E_CUDA);
+  } else {
+    CUDA_OR(launch_regf_ds(variant, mflag, gx, S, js, is, out, st), GPUNB_E_CUDA);
+  }
+  if (timed || pooled) CUDA_OR(cudaEventRecord(e1, st), GPUNB_E_CUDA);
+  g.last_variant = g.precision == 1 ? -1 : variant;
+  g.last_splits = S;
+  g.last_gx = gx;
+  return GPUNB_OK;
+}
+
+static int finish_lists(int ni, int nnbmax, int S, int ni_pad, const RegfDev &o, size_t list_cap,
+                        cudaStream_t st) {
+  CUDA_OR(launch_regf_merge(g.part.as<double>(), S, ni, ni_pad, g.cnt.as<int>(), nnbmax, o.acc,
+                            o.jrk, o.pot, o.nnb, o.rowlen, st),
+          GPUNB_E_CUDA);
+  CUDA_OR(launch_list_scan(o.rowlen, ni, o.off, o.btot, st), GPUNB_E_CUDA);
+  (void)list_cap;
+  CUDA_OR(launch_list_gather(g.rows.as<int>(), std::max(nnbmax, 0), o.rowlen, o.off, o.btot, ni,
+                             o.dense, st),
+          GPUNB_E_CUDA);
+  return GPUNB_OK;
+}
+
+static void choose_plan(int ni, bool mflag, int &variant, int &S) {
+  const JSet js = jset();
+  if (g.precision == 1) {
+    int gx;
+    fp64_plan(ni, js.ntile64, gx, S);
+    variant = -1;
+    return;
+  }
+  heuristic_plan(ni, js.ntile, mflag, variant, S);
+  auto it = g.tune.find(tune_key(g.nj, ni, mflag, 0));
+  if (it != g.tune.end()) {
+    variant = it->second.variant;
+    S = std::min(it->second.splits, std::max(1, js.ntile));
+  }
+  if (g.force_variant >= 0 && g.force_variant < regf_num_variants()) variant = g.force_variant;
+  if (g.force_splits > 0) S = std::min(g.force_splits, std::max(1, js.ntile));
+}
+
+// time every launch shape for (nj, ni) with the given device i-set; keeps
+// the fastest in the cache.
+static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out,
+                         float *ms_out) {
+  const JSet js = jset();
+  const int ni = is.ni;
+  int best_v = -1, best_s = 1;
+  float best = 1e30f;
+  cudaStream_t st = g.stream;
+  for (int v = 0; v < regf_num_variants(); ++v) {
+    int hv, hs;
+    const int saved = g.force_variant;
+    g.force_variant = -1;
+    heuristic_plan(ni, js.ntile, mflag, hv, hs);
+    g.force_variant = saved;
+    const VariantDesc d = regf_variant(v);
+    const int gx = (ni + d.itile() - 1) / d.itile();
+    const int bps = regf_ds_blocks_per_sm(v, mflag);
+    const long long base = std::max(1ll, (2ll * g.n_sm * bps + gx - 1) / gx);
+    const long long cands[5] = {base / 4, base / 2, base, base * 2, base * 4};
+    for (long long sc : cands) {
+      int s = (int)std::max(1ll, std::min<long long>(sc, std::max(1, js.ntile)));
+      float tot = 0.f;
+      const int reps = 3;
+      bool ok = true;
+      for (int r = 0; r < reps + 1 && ok; ++r) {
+        if (run_pair_pass(is, nnbmax, mflag, v, s, st, true) != GPUNB_OK) ok = false;
+        if (cudaStreamSynchronize(st) != cudaSuccess) ok = false;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, g.ek0, g.ek1);
+        if (r > 0) tot += ms;
+      }
+      if (!ok) continue;
+      const float ms = tot / reps;
+      if (ms < best) {
+        best = ms;
+        best_v = v;
+        best_s = s;
+      }
+    }
+  }
+  if (best_v >= 0) g.tune[tune_key(g.nj, ni, mflag, 0)] = TuneEntry{best_v, best_s, best};
+  if (splits_out) *splits_out = best_s;
+  if (ms_out) *ms_out = best;
+  return best_v;
+}
+
+// ---------------------------------------------------------------------------
+// host-buffer regf: the gpunb_regf_ contract
+static void regf_host(int ni, const double *h2, const double *dtr, const double (*xi)[3],
+                      const double (*vi)[3], double (*acc)[3], double (*jrk)[3], double *pot,
+                      int lmax, int nnbmax, int *list, int m_flag) {
+  if (!g.is_open) { fail(GPUNB_E_NOT_OPEN, "gpunb_regf_ called before gpunb_open_"); return; }
+  if (ni <= 0 || ni > kMaxNi) {
+    fail(GPUNB_E_ARG, "gpunb_regf_: ni = %d outside [1, %d]", ni, kMaxNi);
+    return;
+  }
+  if (nnbmax < 0 || lmax < 1 || nnbmax > lmax - 1) {
+    fail(GPUNB_E_ARG, "gpunb_regf_: need 0 <= nnbmax (%d) <= lmax-1 (%d)", nnbmax, lmax - 1);
+    return;
+  }
+  const double t_begin = wtime();
+  g.num_inter += (long long)ni * g.nj;
+  g.ini += ni;
+  g.icall++;
+  cudaStream_t st = g.stream;
+  const bool mflag = m_flag != 0;
+
+  // stage inputs: h2 | dtr | x | v
+  const size_t in_doubles = (size_t)8 * ni;
+  if (!g.hin.ensure(in_doubles * sizeof(double)) || !g.iraw.ensure(in_doubles * sizeof(double)))
+    return;
+  double *hin = g.hin.as<double>();
+  hcopy(hin, h2, (size_t)ni * sizeof(double));
+  hcopy(hin + ni, dtr, (size_t)ni * sizeof(double));
+  hcopy(hin + 2 * (size_t)ni, xi, (size_t)ni * 3 * sizeof(double));
+  hcopy(hin + 5 * (size_t)ni, vi, (size_t)ni * 3 * sizeof(double));
+  double *din = g.iraw.as<double>();
+  CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
+  CUDA_OR(cudaMemcpyAsync(din, hin, in_doubles * sizeof(double), cudaMemcpyHostToDevice, st), );
+  ISet is;
+  is.h2 = din;
+  is.dtr = din + ni;
+  is.x = din + 2 * (size_t)ni;
+  is.v = din + 5 * (size_t)ni;
+  is.ni = ni;
+
+  int variant, S;
+  if (g.autotune_on && g.precision == 0 && g.force_variant < 0 &&
+      g.tune.find(tune_key(g.nj, ni, mflag, 0)) == g.tune.end())
+    autotune_with(is, nnbmax, mflag, nullptr, nullptr);
+  choose_plan(ni, mflag, variant, S);
+  if (run_pair_pass(is, nnbmax, mflag, variant, S, st, false) != GPUNB_OK) return;
+
+  // outputs: acc | jrk | pot (doubles), then nnb (ints)
+  const int nb = list_scan_blocks(ni);
+  if (!g.outblk.ensure((size_t)7 * ni * sizeof(double) + (size_t)(ni + 2) * sizeof(int)) ||
+      !g.rowlen.ensure((size_t)ni * sizeof(int)) || !g.off.ensure((size_t)(ni + 1) * sizeof(int)) ||
+      !g.btot.ensure((size_t)(nb + 1) * sizeof(int)) ||
+      !g.dense.ensure((size_t)ni * std::max(nnbmax, 1) * sizeof(int)))
+    return;
+  double *ob = g.outblk.as<double>();
+  RegfDev o;
+  o.acc = ob;
+  o.jrk = ob + 3 * (size_t)ni;
+  o.pot = ob + 6 * (size_t)ni;
+  o.nnb = (int *)(ob + 7 * (size_t)ni);
+  o.rowlen = g.rowlen.as<int>();
+  o.off = g.off.as<int>();
+  o.btot = g.btot.as<int>();
+  o.dense = g.dense.as<int>();
+  const int ni_pad = g.precision == 1
+                         ? ((ni + FP64_THREADS - 1) / FP64_THREADS) * FP64_THREADS
+                         : ((ni + regf_variant(variant).itile() - 1) / regf_variant(variant).itile()) *
+                               regf_variant(variant).itile();
+  if (finish_lists(ni, nnbmax, S, ni_pad, o, 0, st) != GPUNB_OK) return;
+  const size_t out_bytes = (size_t)7 * ni * sizeof(double) + (size_t)ni * sizeof(int);
+  if (!g.hout.ensure(out_bytes + 2 * sizeof(int))) return;
+  char *hob = g.hout.as<char>();
+  int *h_total = (int *)(hob + out_bytes);
+  int *h_err = h_total + 1;
+  CUDA_OR(cudaMemcpyAsync(hob, ob, out_bytes, cudaMemcpyDeviceToHost, st), );
+  CUDA_OR(cudaMemcpyAsync(h_total, o.btot + nb, sizeof(int), cudaMemcpyDeviceToHost, st), );
+  CUDA_OR(cudaMemcpyAsync(h_err, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
+  CUDA_OR(cudaStreamSynchronize(st), );
+  const double t_grav = wtime();
+  g.time_grav += t_grav - t_begin;
+  if (!check_device_error(*h_err)) return;
+  const int total = *h_total;
+  if (total > 0) {
+    if (!g.hlist.ensure((size_t)total * sizeof(int))) return;
+    CUDA_OR(cudaMemcpyAsync(g.hlist.p, o.dense, (size_t)total * sizeof(int),
+                            cudaMemcpyDeviceToHost, st), );
+    CUDA_OR(cudaStreamSynchronize(st), );
+  }
+  const double *hd = (const double *)hob;
+  hcopy(acc, hd, (size_t)ni * 3 * sizeof(double));
+  hcopy(jrk, hd + 3 * (size_t)ni, (size_t)ni * 3 * sizeof(double));
+  hcopy(pot, hd + 6 * (size_t)ni, (size_t)ni * sizeof(double));
+  const int *hnnb = (const int *)(hd + 7 * (size_t)ni);
+  const int *hl = g.hlist.as<int>();
+  // host scatter of the compacted list into rows of lmax
+  if (ni < 4096) {
+    size_t o2 = 0;
+    for (int i = 0; i < ni; ++i) {
+      int *row = list + (size_t)i * lmax;
+      const int c = hnnb[i];
+      row[0] = c;
+      if (c > 0) {
+        memcpy(row + 1, hl + o2, (size_t)c * sizeof(int));
+        o2 += c;
+      }
+    }
+  } else {
+    // offsets first (sequential), then parallel copies
+    static thread_local std::vector<size_t> offs;
+    offs.resize(ni);
+    size_t o2 = 0;
+    for (int i = 0; i < ni; ++i) {
+      offs[i] = o2;
+      if (hnnb[i] > 0) o2 += hnnb[i];
+    }
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < ni; ++i) {
+      int *row = list + (size_t)i * lmax;
+      const int c = hnnb[i];
+      row[0] = c;
+      if (c > 0) memcpy(row + 1, hl + offs[i], (size_t)c * sizeof(int));
+    }
+  }
+  g.time_reduce += wtime() - t_grav;
+}
+
+}  // namespace gpunb
+
+// ===========================================================================
+// C ABI
+using namespace gpunb;
+
+extern "C" {
+
+void gpunb_devinit_(int *irank) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  devinit(irank ? *irank : 0);
+}
+
+void gpunb_open_(int *nbmax, int *irank) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  const int rank = irank ? *irank : 0;
+  g.time_send = g.time_grav = g.time_reduce = g.time_out = 0.0;
+  g.num_inter = 0;
+  g.icall = g.ini = g.isend = 0;
+  if (!devinit(rank)) return;
+  if (g.is_open) {
+    fprintf(stderr, "gpunb: it is already open\n");
+    return;
+  }
+  if (!nbmax || *nbmax < 0) {
+    fail(GPUNB_E_ARG, "gpunb_open_: nbmax must be >= 0");
+    return;
+  }
+  g.nbodymax = *nbmax;
+  const size_t nmax = (size_t)std::max(g.nbodymax, 1);
+  if (!g.jraw.ensure(nmax * 7 * sizeof(double)) ||
+      !g.jtiles.ensure(((nmax + JT - 1) / JT) * (size_t)TILE_BYTES) ||
+      !g.hj.ensure(nmax * 7 * sizeof(double)))
+    return;
+  g.nj = 0;
+  g.is_open = true;
+  fprintf(stderr, "# Open GPU regular force - rank: %d; nbmax: %d\n", rank, g.nbodymax);
+}
+
+void gpunb_close_(void) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!g.is_open) {
+    fprintf(stderr, "gpunb: it is already close\n");
+    return;
+  }
+  if (g.stream) cudaStreamSynchronize(g.stream);
+  g.jraw.release(); g.jtiles.release(); g.hj.release();
+  g.iraw.release(); g.part.release(); g.cnt.release(); g.rows.release();
+  g.rowlen.release(); g.off.release(); g.btot.release(); g.dense.release();
+  g.outblk.release(); g.hin.release(); g.hout.release(); g.hlist.release();
+  g.nbodymax = 0;
+  g.nj = 0;
+  g.is_open = false;
+}
+
+void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!g.is_open) { fail(GPUNB_E_NOT_OPEN, "gpunb_send_ called before gpunb_open_"); return; }
+  const int n = *nj;
+  if (n < 0 || n > g.nbodymax) {
+    fail(GPUNB_E_CAPACITY, "gpunb_send_: nj = %d outside [0, nbmax = %d]", n, g.nbodymax);
+    return;
+  }
+  const double t0 = wtime();
+  g.isend++;
+  cudaStream_t st = g.stream;
+  double *h = g.hj.as<double>();
+  hcopy(h, mj, (size_t)n * sizeof(double));
+  hcopy(h + n, xj, (size_t)n * 3 * sizeof(double));
+  hcopy(h + 4 * (size_t)n, vj, (size_t)n * 3 * sizeof(double));
+  CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
+  if (n > 0)
+    CUDA_OR(cudaMemcpyAsync(g.jraw.p, h, (size_t)n * 7 * sizeof(double), cudaMemcpyHostToDevice,
+                            st), );
+  if (send_common(n, st) != GPUNB_OK) return;
+  int herr = 0;
+  CUDA_OR(cudaMemcpyAsync(&herr, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
+  CUDA_OR(cudaStreamSynchronize(st), );
+  check_device_error(herr);
+  g.time_send += wtime() - t0;
+}
+
+void gpunb_regf_(int *ni, double h2[], double dtr[], double xi[][3], double vi[][3],
+                 double acc[][3], double jrk[][3], double pot[], int *lmax, int *nnbmax,
+                 int *list, int *m_flag) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  regf_host(*ni, h2, dtr, xi, vi, acc, jrk, pot, *lmax, *nnbmax, list, m_flag ? *m_flag : 0);
+}
+
+void gpunb_profile_(int *irank) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  const int rank = irank ? *irank : 0;
+  if (g.icall) {
+    fprintf(stderr,
+            "[R.%d GPU Reg.F ] Nsend %lld  Ngrav %lld  <Ni> %lld   send(s) %f grav(s) %f  nb(s) %f  "
+            "out(s) %f  Perf.(Gflops) %f\n",
+            rank, g.isend, g.icall, g.isend ? g.ini / g.isend : 0, g.time_send, g.time_grav,
+            g.time_reduce, g.time_out,
+            g.time_grav > 0 ? 60.e-9 * (double)g.num_inter / g.time_grav : 0.0);
+  }
+  g.time_send = g.time_grav = g.time_reduce = g.time_out = 0.0;
+  g.num_inter = 0;
+  g.icall = g.ini = g.isend = 0;
+}
+
+void gpupot_(int *irank, int *istart, int *ni, int *n, double m[], double x[][3], double pot[]) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!devinit(irank ? *irank : 0)) return;
+  const double t0 = wtime();
+  const int nn = *n, k = *ni, is0 = *istart - 1;
+  if (nn < 0 || k < 0 || is0 < 0 || is0 + k > nn) {
+    fail(GPUNB_E_ARG, "gpupot_: need 1 <= istart, istart-1+ni <= n (istart %d ni %d n %d)",
+         *istart, k, nn);
+    return;
+  }
+  if (k == 0) return;
+  cudaStream_t st = g.stream;
+  const int ntile = (nn + POT_JT - 1) / POT_JT;
+  const int itile = pot_itile();
+  const int gx = (k + itile - 1) / itile;
+  const long long want = 2ll * g.n_sm * pot_blocks_per_sm();
+  int S = (int)std::max(1ll, std::min<long long>((want + gx - 1) / gx, std::max(1, ntile / 2)));
+  const int ni_pad = gx * itile;
+  if (!g.praw.ensure((size_t)nn * 4 * sizeof(double)) || !g.hp.ensure((size_t)nn * 4 * sizeof(double)) ||
+      !g.ptiles.ensure((size_t)std::max(ntile, 1) * POT_TILE_FLOATS * sizeof(float)) ||
+      !g.ppart.ensure((size_t)S * ni_pad * sizeof(double)) ||
+      !g.pout.ensure((size_t)k * sizeof(double) + sizeof(int)))
+    return;
+  double *h = g.hp.as<double>();
+  hcopy(h, m, (size_t)nn * sizeof(double));
+  hcopy(h + nn, x, (size_t)nn * 3 * sizeof(double));
+  double *d = g.praw.as<double>();
+  CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
+  CUDA_OR(cudaMemcpyAsync(d, h, (size_t)nn * 4 * sizeof(double), cudaMemcpyHostToDevice, st), );
+  CUDA_OR(launch_pack_pot(d, d + nn, nn, g.ptiles.as<float>(), ntile, g.err.as<int>(), st), );
+  CUDA_OR(launch_pot(g.ptiles.as<float>(), ntile, d + nn, is0, k, gx, S, g.ppart.as<double>(),
+                     ni_pad, g.err.as<int>(), st), );
+  CUDA_OR(launch_pot_merge(g.ppart.as<double>(), S, k, ni_pad, g.pout.as<double>(), st), );
+  // results land in the staging buffer (reused: m/x no longer needed)
+  CUDA_OR(cudaMemcpyAsync(h, g.pout.p, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, st), );
+  int herr = 0;
+  CUDA_OR(cudaMemcpyAsync(h + k, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
+  CUDA_OR(cudaStreamSynchronize(st), );
+  memcpy(&herr, h + k, sizeof(int));
+  if (!check_device_error(herr)) return;
+  hcopy(pot, h, (size_t)k * sizeof(double));
+  fprintf(stderr, "[R.%d GPU Pot.A] Ni %d  NTOT %d  pot(s) %f\n", irank ? *irank : 0, k, nn,
+          wtime() - t0);
+}
+
+// ---- additions ------------------------------------------------------------
+
+int gpunb_last_error(void) { return g_err_code; }
+const char *gpunb_last_error_message(void) { return g_err_msg.c_str(); }
+void gpunb_clear_error(void) {
+  g_err_code = 0;
+  g_err_msg.clear();
+}
+void gpunb_set_abort_on_error(int flag) { g_abort_on_error = flag; }
+
+void gpunb_set_precision(int mode) { g.precision = mode == 1 ? 1 : 0; }
+
+void gpunb_set_launch(int variant, int splits) {
+  g.force_variant = variant;
+  g.force_splits = splits;
+}
+
+int gpunb_num_variants(void) { return regf_num_variants(); }
+
+int gpunb_variant_info(int variant, int *ipt, int *warps_i, int *warps_j) {
+  if (variant < 0 || variant >= regf_num_variants()) return -1;
+  const VariantDesc d = regf_variant(variant);
+  if (ipt) *ipt = d.ipt;
+  if (warps_i) *warps_i = d.wi;
+  if (warps_j) *warps_j = d.wj;
+  return 0;
+}
+
+void gpunb_set_timing(int flag) {
+  g.timing = flag;
+  g.evused = 0;
+}
+
+int gpunb_kernel_times(float *ms, int max) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  int n = 0;
+  for (int k = 0; k < g.evused && n < max; ++k) {
+    if (cudaEventSynchronize(g.evpool[2 * k + 1]) != cudaSuccess) break;
+    float t = 0.f;
+    cudaEventElapsedTime(&t, g.evpool[2 * k], g.evpool[2 * k + 1]);
+    ms[n++] = t;
+  }
+  if (n > 0) g.last_kernel_ms = ms[n - 1];
+  g.evused = 0;
+  return n;
+}
+
+float gpunb_last_kernel_ms(void) { return g.last_kernel_ms; }
+void gpunb_last_launch(int *variant, int *splits, int *grid_x) {
+  if (variant) *variant = g.last_variant;
+  if (splits) *splits = g.last_splits;
+  if (grid_x) *grid_x = g.last_gx;
+}
+
+int gpunb_autotune(int ni, int m_flag, int *splits, float *ms) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!g.is_open || g.nj <= 0) {
+    fail(GPUNB_E_NOT_OPEN, "gpunb_autotune needs an open library with a j-set");
+    return -1;
+  }
+  if (ni <= 0) { fail(GPUNB_E_ARG, "gpunb_autotune: ni must be positive"); return -1; }
+  // synthetic i-set: the first ni j-bodies (wrapping), h2 from the mean
+  // inter-particle spacing so that lists have realistic lengths
+  const int nj = g.nj;
+  if (!g.iraw.ensure((size_t)8 * ni * sizeof(double)) || !g.hin.ensure((size_t)8 * ni * sizeof(double)))
+    return -1;
+  std::vector<double> hj((size_t)7 * nj);
+  CUDA_OR(cudaMemcpy(hj.data(), g.jraw.p, hj.size() * sizeof(double), cudaMemcpyDeviceToHost), -1);
+  double r2s = 0.0;
+  for (int j = 0; j < nj; ++j)
+    for (int c = 0; c < 3; ++c) r2s += hj[nj + 3 * (size_t)j + c] * hj[nj + 3 * (size_t)j + c];
+  const double rms = std::sqrt(r2s / std::max(nj, 1));
+  const double h2v = std::pow(rms * std::cbrt(100.0 / std::max(nj, 1)), 2);
+  double *hin = g.hin.as<double>();
+  for (int i = 0; i < ni; ++i) {
+    const int j = i % nj;
+    hin[i] = h2v;
+    hin[ni + i] = 0.01;
+    for (int c = 0; c < 3; ++c) {
+      hin[2 * (size_t)ni + 3 * (size_t)i + c] = hj[nj + 3 * (size_t)j + c];
+      hin[5 * (size_t)ni + 3 * (size_t)i + c] = hj[4 * (size_t)nj + 3 * (size_t)j + c];
+    }
+  }
+  double *din = g.iraw.as<double>();
+  CUDA_OR(cudaMemcpy(din, hin, (size_t)8 * ni * sizeof(double), cudaMemcpyHostToDevice), -1);
+  ISet is;
+  is.h2 = din; is.dtr = din + ni; is.x = din + 2 * (size_t)ni; is.v = din + 5 * (size_t)ni;
+  is.ni = ni;
+  const int saved = g.precision;
+  g.precision = 0;
+  const int v = autotune_with(is, 1024, m_flag != 0, splits, ms);
+  g.precision = saved;
+  return v;
+}
+
+int gpunb_tune_load(const char *path) {
+  FILE *f = fopen(path, "r");
+  if (!f) return 0;
+  int n = 0;
+  long long key;
+  int v, s;
+  float ms;
+  while (fscanf(f, "%lld %d %d %f", &key, &v, &s, &ms) == 4) {
+    if (v >= 0 && v < regf_num_variants() && s > 0) {
+      g.tune[key] = TuneEntry{v, s, ms};
+      ++n;
+    }
+  }
+  fclose(f);
+  return n;
+}
+
+int gpunb_tune_save(const char *path) {
+  FILE *f = fopen(path, "w");
+  if (!f) return -1;
+  int n = 0;
+  for (const auto &kv : g.tune) {
+    fprintf(f, "%lld %d %d %.6f\n", kv.first, kv.second.variant, kv.second.splits, kv.second.ms);
+    ++n;
+  }
+  fclose(f);
+  return n;
+}
+
+int gpunb_send_device(int nj, const double *m, const double *x, const double *v, void *stream) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!g.is_open) { fail(GPUNB_E_NOT_OPEN, "gpunb_send_device before gpunb_open_"); return GPUNB_E_NOT_OPEN; }
+  if (nj < 0 || nj > g.nbodymax) {
+    fail(GPUNB_E_CAPACITY, "gpunb_send_device: nj = %d outside [0, nbmax = %d]", nj, g.nbodymax);
+    return GPUNB_E_CAPACITY;
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  double *d = g.jraw.as<double>();
+  if (nj > 0) {
+    CUDA_OR(cudaMemcpyAsync(d, m, (size_t)nj * sizeof(double), cudaMemcpyDeviceToDevice, st), GPUNB_E_CUDA);
+    CUDA_OR(cudaMemcpyAsync(d + nj, x, (size_t)nj * 3 * sizeof(double), cudaMemcpyDeviceToDevice, st), GPUNB_E_CUDA);
+    CUDA_OR(cudaMemcpyAsync(d + 4 * (size_t)nj, v, (size_t)nj * 3 * sizeof(double), cudaMemcpyDeviceToDevice, st), GPUNB_E_CUDA);
+  }
+  return send_common(nj, st);
+}
+
+int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double *xi,
+                      const double *vi, double *acc, double *jrk, double *pot, int *nnb,
+                      int *list_off, int *list, size_t list_cap, int nnbmax, int m_flag,
+                      void *stream) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!g.is_open) { fail(GPUNB_E_NOT_OPEN, "gpunb_regf_device before gpunb_open_"); return GPUNB_E_NOT_OPEN; }
+  if (ni <= 0 || ni > kMaxNi || nnbmax < 0) {
+    fail(GPUNB_E_ARG, "gpunb_regf_device: ni %d nnbmax %d", ni, nnbmax);
+    return GPUNB_E_ARG;
+  }
+  if (list_cap < (size_t)ni * (size_t)nnbmax) {
+    fail(GPUNB_E_ARG, "gpunb_regf_device: list_cap %zu < ni*nnbmax", list_cap);
+    return GPUNB_E_ARG;
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  ISet is;
+  is.h2 = h2; is.dtr = dtr; is.x = xi; is.v = vi; is.ni = ni;
+  const bool mflag = m_flag != 0;
+  int variant, S;
+  choose_plan(ni, mflag, variant, S);
+  g.num_inter += (long long)ni * g.nj;
+  g.ini += ni;
+  g.icall++;
+  int rc = run_pair_pass(is, nnbmax, mflag, variant, S, st, false);
+  if (rc != GPUNB_OK) return rc;
+  const int nb = list_scan_blocks(ni);
+  if (!g.rowlen.ensure((size_t)ni * sizeof(int)) || !g.btot.ensure((size_t)(nb + 1) * sizeof(int)))
+    return GPUNB_E_ALLOC;
+  RegfDev o;
+  o.acc = acc; o.jrk = jrk; o.pot = pot; o.nnb = nnb;
+  o.rowlen = g.rowlen.as<int>(); o.off = list_off; o.btot = g.btot.as<int>(); o.dense = list;
+  const int ni_pad = g.precision == 1
+                         ? ((ni + FP64_THREADS - 1) / FP64_THREADS) * FP64_THREADS
+                         : ((ni + regf_variant(variant).itile() - 1) / regf_variant(variant).itile()) *
+                               regf_variant(variant).itile();
+  rc = finish_lists(ni, nnbmax, S, ni_pad, o, list_cap, st);
+  if (rc != GPUNB_OK) return rc;
+  CUDA_OR(launch_list_finalize_offsets(list_off, o.btot, ni, st), GPUNB_E_CUDA);
+  return GPUNB_OK;
+}
+
+}  // extern "C"

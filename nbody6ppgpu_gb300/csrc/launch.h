@@ -1,0 +1,50 @@
+// Host-side launchers of the device kernels (one translation unit per kernel
+// family; the engine calls only these).
+#pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "regf_kernels.cuh"
+
+namespace gpunb {
+
+struct VariantDesc {
+  int ipt, wi, wj;                       // i per thread, warps along i, warps along j
+  int threads() const { return 32 * wi * wj; }
+  int itile() const { return 32 * ipt * wi; }
+};
+
+int regf_num_variants();
+VariantDesc regf_variant(int v);
+size_t regf_ds_smem(int v);
+int regf_ds_blocks_per_sm(int v, bool mflag);
+cudaError_t launch_pack_jtiles(const double *m, const double *x, const double *v, int nj,
+                               float *tiles, int ntile, int *err, cudaStream_t st);
+cudaError_t launch_regf_ds(int v, bool mflag, int gx, int S, const JSet &js, const ISet &is,
+                           const RegfOut &out, cudaStream_t st);
+cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const ISet &is,
+                             const RegfOut &out, cudaStream_t st);
+constexpr int FP64_THREADS = 128;
+cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *cnt,
+                              int nnbmax, double *acc, double *jrk, double *pot, int *nnb,
+                              int *rowlen, cudaStream_t st);
+// scan of rowlen -> off (+ block offsets in btot, grand total at btot[nblocks])
+int list_scan_blocks(int ni);
+cudaError_t launch_list_scan(const int *rowlen, int ni, int *off, int *btot, cudaStream_t st);
+cudaError_t launch_list_gather(int *rows, int cap, const int *rowlen, const int *off,
+                               const int *btot, int ni, int *dense, cudaStream_t st);
+cudaError_t launch_list_finalize_offsets(int *off, const int *btot, int ni, cudaStream_t st);
+
+// potential
+constexpr int POT_JT = 128;
+constexpr int POT_TILE_FLOATS = 7 * POT_JT;
+cudaError_t launch_pack_pot(const double *m, const double *x, int n, float *tiles, int ntile,
+                            int *err, cudaStream_t st);
+int pot_itile();
+cudaError_t launch_pot(const float *tiles, int ntile, const double *x, int istart0, int ni,
+                       int gx, int S, double *part, int ni_pad, int *err, cudaStream_t st);
+int pot_blocks_per_sm();
+cudaError_t launch_pot_merge(const double *part, int S, int ni, int ni_pad, double *pot,
+                             cudaStream_t st);
+
+}  // namespace gpunb

@@ -1,0 +1,182 @@
+// Potential kernels for the energy check (gpupot_).
+//
+// Reference replaced: src/Main/gpupot.gpu.cu:32-57 (pot_kernel) and the
+// host side of gpupot.gpu.cu:61-114.  Semantics: pot_i = sum over all j with
+// r_ij^2 > 0 of m_j / r_ij (positive sign, no neighbour exclusion).
+#include "common.cuh"
+#include "launch.h"
+
+namespace gpunb {
+
+constexpr int PJT = 128;
+enum PField { P_XH = 0, P_YH, P_ZH, P_XL, P_YL, P_ZL, P_MN, P_NFIELD };
+constexpr int PTILE_FLOATS = P_NFIELD * PJT;
+constexpr int PTILE_BYTES = PTILE_FLOATS * 4;
+static_assert(PTILE_BYTES % 16 == 0, "tile must be a multiple of 16 bytes");
+
+__global__ void __launch_bounds__(PJT) pack_pot_tiles_kernel(const double *__restrict__ m,
+                                                             const double *__restrict__ x, int n,
+                                                             float *__restrict__ tiles,
+                                                             int *err) {
+  const int t = blockIdx.x, l = threadIdx.x, j = t * PJT + l;
+  float *T = tiles + (size_t)t * PTILE_FLOATS;
+  if (j < n) {
+    const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2], mj = m[j];
+    if (isnan(x0) || isnan(x1) || isnan(x2) || isnan(mj)) raise_error(err, GPUNB_E_NAN);
+    float h, lo;
+    ds_split(x0, h, lo); T[P_XH * PJT + l] = h; T[P_XL * PJT + l] = lo;
+    ds_split(x1, h, lo); T[P_YH * PJT + l] = h; T[P_YL * PJT + l] = lo;
+    ds_split(x2, h, lo); T[P_ZH * PJT + l] = h; T[P_ZL * PJT + l] = lo;
+    T[P_MN * PJT + l] = (float)(-0.5 * mj);
+  } else {
+    T[P_XH * PJT + l] = 1.0e15f; T[P_XL * PJT + l] = 0.f;
+    T[P_YH * PJT + l] = 1.0e15f; T[P_YL * PJT + l] = 0.f;
+    T[P_ZH * PJT + l] = 1.0e15f; T[P_ZL * PJT + l] = 0.f;
+    T[P_MN * PJT + l] = -0.f;
+  }
+}
+
+constexpr int PSTAGE = 4;
+
+// Grid (ceil(ni / (32*IPT*WI)), S).  i = istart0 + local index (0-based).
+template <int IPT, int WI>
+__global__ void __launch_bounds__(32 * WI) pot_ds_kernel(const float *__restrict__ tiles,
+                                                         int ntile, const double *__restrict__ x,
+                                                         int istart0, int ni,
+                                                         double *__restrict__ part, int ni_pad,
+                                                         int *err) {
+  constexpr int ITILE = 32 * IPT * WI;
+  extern __shared__ __align__(128) float smem[];
+  __shared__ __align__(8) uint64_t bar[PSTAGE];
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ns = gridDim.y, sy = blockIdx.y;
+  const int t0 = (int)(((long long)ntile * sy) / ns);
+  const int t1 = (int)(((long long)ntile * (sy + 1)) / ns);
+  const int nt = t1 - t0;
+  if (tid == 0) {
+    for (int s = 0; s < PSTAGE; ++s) mbar_init(&bar[s], 1);
+    fence_mbar_init();
+    s_abort = 0;
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int s = 0; s < PSTAGE && s < nt; ++s) {
+      mbar_expect_tx(&bar[s], PTILE_BYTES);
+      bulk_g2s(smem + s * PTILE_FLOATS, tiles + (size_t)(t0 + s) * PTILE_FLOATS, PTILE_BYTES,
+               &bar[s]);
+    }
+  f2 nxh[IPT], nyh[IPT], nzh[IPT], nxl[IPT], nyl[IPT], nzl[IPT];
+  f2 q[IPT];
+  float hi[IPT], lo[IPT];
+  int iloc[IPT];
+#pragma unroll
+  for (int k = 0; k < IPT; ++k) {
+    const int il = blockIdx.x * ITILE + warp * 32 * IPT + k * 32 + lane;
+    iloc[k] = il < ni ? il : -1;
+    const int i = istart0 + (il < ni ? il : 0);
+    float h, l;
+    ds_split(x[3 * i], h, l); nxh[k] = mk2(-h); nxl[k] = mk2(-l);
+    ds_split(x[3 * i + 1], h, l); nyh[k] = mk2(-h); nyl[k] = mk2(-l);
+    ds_split(x[3 * i + 2], h, l); nzh[k] = mk2(-h); nzl[k] = mk2(-l);
+    q[k] = make_float2(0.f, 0.f);
+    hi[k] = lo[k] = 0.f;
+  }
+  int t = 0;
+  for (; t < nt; ++t) {
+    const int s = t % PSTAGE;
+    if (!mbar_wait_bounded(&bar[s], (uint32_t)(t / PSTAGE) & 1u)) s_abort = 1;
+    const float *T = smem + s * PTILE_FLOATS;
+#pragma unroll 4
+    for (int jj = 0; jj < PJT; jj += 2) {
+      const f2 xh = *(const f2 *)(T + P_XH * PJT + jj);
+      const f2 yh = *(const f2 *)(T + P_YH * PJT + jj);
+      const f2 zh = *(const f2 *)(T + P_ZH * PJT + jj);
+      const f2 xl = *(const f2 *)(T + P_XL * PJT + jj);
+      const f2 yl = *(const f2 *)(T + P_YL * PJT + jj);
+      const f2 zl = *(const f2 *)(T + P_ZL * PJT + jj);
+      const f2 mn = *(const f2 *)(T + P_MN * PJT + jj);
+#pragma unroll
+      for (int k = 0; k < IPT; ++k) {
+        const f2 dx = add2(add2(xh, nxh[k]), add2(xl, nxl[k]));
+        const f2 dy = add2(add2(yh, nyh[k]), add2(yl, nyl[k]));
+        const f2 dz = add2(add2(zh, nzh[k]), add2(zl, nzl[k]));
+        const f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+        const f2 y0 = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        f2 z = mul2(y0, fma2(mul2(r2, y0), y0, mk2(-3.0f)));   // -2/r
+        z.x = r2.x > 0.f ? z.x : 0.f;                         // skip coincident bodies
+        z.y = r2.y > 0.f ? z.y : 0.f;
+        q[k] = fma2(mn, z, q[k]);                              // += m/r
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+      ff_accum(hi[k], lo[k], __fadd_rn(q[k].x, q[k].y));
+      q[k] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (s_abort) break;
+    if (tid == 0 && t + PSTAGE < nt) {
+      mbar_expect_tx(&bar[s], PTILE_BYTES);
+      bulk_g2s(smem + s * PTILE_FLOATS, tiles + (size_t)(t0 + t + PSTAGE) * PTILE_FLOATS,
+               PTILE_BYTES, &bar[s]);
+    }
+  }
+  if (s_abort) {
+    if (tid == 0) {
+      for (int u = t + 1; u < nt && u < t + PSTAGE; ++u)
+        mbar_wait_bounded(&bar[u % PSTAGE], (uint32_t)(u / PSTAGE) & 1u, 1u << 16);
+      raise_error(err, GPUNB_E_TIMEOUT);
+    }
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < IPT; ++k)
+    if (iloc[k] >= 0) part[(size_t)sy * ni_pad + iloc[k]] = (double)hi[k] + (double)lo[k];
+}
+
+__global__ void pot_merge_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
+                                 double *__restrict__ pot) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ni) return;
+  double s = 0.0;
+  for (int k = 0; k < S; ++k) s += part[(size_t)k * ni_pad + i];
+  pot[i] = s;
+}
+
+// host launchers
+static_assert(PJT == POT_JT && PTILE_FLOATS == POT_TILE_FLOATS, "pot tile layout");
+constexpr int POT_IPT = 2, POT_WI = 4;
+
+int pot_itile() { return 32 * POT_IPT * POT_WI; }
+
+int pot_blocks_per_sm() {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pot_ds_kernel<POT_IPT, POT_WI>,
+                                                    32 * POT_WI,
+                                                    (size_t)PSTAGE * PTILE_BYTES) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_pack_pot(const double *m, const double *x, int n, float *tiles, int ntile,
+                            int *err, cudaStream_t st) {
+  if (ntile <= 0) return cudaSuccess;
+  pack_pot_tiles_kernel<<<ntile, PJT, 0, st>>>(m, x, n, tiles, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pot(const float *tiles, int ntile, const double *x, int istart0, int ni,
+                       int gx, int S, double *part, int ni_pad, int *err, cudaStream_t st) {
+  pot_ds_kernel<POT_IPT, POT_WI><<<dim3(gx, S), 32 * POT_WI, (size_t)PSTAGE * PTILE_BYTES, st>>>(
+      tiles, ntile, x, istart0, ni, part, ni_pad, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pot_merge(const double *part, int S, int ni, int ni_pad, double *pot,
+                             cudaStream_t st) {
+  pot_merge_kernel<<<(ni + 255) / 256, 256, 0, st>>>(part, S, ni, ni_pad, pot);
+  return cudaGetLastError();
+}
+
+}  // namespace gpunb

@@ -1,0 +1,706 @@
+// Regular force + jerk + potential + neighbour-list kernels for sm_103a.
+//
+// Reference device path replaced: src/Main/gpunb.velocity.cu:162-552
+// (dev_gravity, gravity_kernel(_m), force_reduce_kernel, gather_nb_kernel) and
+// the host prefix sum / merge of gpunb.velocity.cu:793-878.
+//
+// Pipeline for one gpunb_regf_ call (all on one stream):
+//   regf_ds_kernel<...>   pair loop, grid (i-tiles x j-splits), partial sums
+//   regf_merge_kernel     FP64 sum of the j-split partials in fixed order,
+//                         neighbour count -> in-band overflow flag
+//   list_scan_*           exclusive scan of accepted row lengths
+//   list_gather_kernel    per-row sort (ascending j) + compaction
+#include "regf_kernels.cuh"
+#include "launch.h"
+
+#include <cfloat>
+#include <climits>
+
+namespace gpunb {
+
+// ---------------------------------------------------------------------------
+// j packing: FP64 (as sent) -> split-precision SoA tiles + tile metadata.
+// One block of JT threads per tile.  Replaces the host-side Jparticle packing
+// of gpunb.velocity.cu:716-727 (which also drops positions to plain FP32).
+__global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restrict__ m,
+                                                         const double *__restrict__ x,
+                                                         const double *__restrict__ v, int nj,
+                                                         float *__restrict__ tiles, int *err) {
+  const int t = blockIdx.x, l = threadIdx.x, j = t * JT + l;
+  float *T = tiles + (size_t)t * TILE_FLOATS;
+  double vabs = 0.0, mj = 0.0;
+  int real = 0;
+  if (j < nj) {
+    const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+    const double v0 = v[3 * j], v1 = v[3 * j + 1], v2 = v[3 * j + 2];
+    mj = m[j];
+    if (isnan(x0) || isnan(x1) || isnan(x2) || isnan(v0) || isnan(v1) || isnan(v2) || isnan(mj))
+      raise_error(err, GPUNB_E_NAN);
+    float h, lo;
+    ds_split(x0, h, lo); T[F_XH * JT + l] = h; T[F_XL * JT + l] = lo;
+    ds_split(x1, h, lo); T[F_YH * JT + l] = h; T[F_YL * JT + l] = lo;
+    ds_split(x2, h, lo); T[F_ZH * JT + l] = h; T[F_ZL * JT + l] = lo;
+    T[F_VX * JT + l] = (float)v0;
+    T[F_VY * JT + l] = (float)v1;
+    T[F_VZ * JT + l] = (float)v2;
+    T[F_MN * JT + l] = (float)(-0.5 * mj);
+    vabs = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+    real = 1;
+  } else {
+    // padding body: massless and far away, never a neighbour candidate
+    T[F_XH * JT + l] = 1.0e15f; T[F_XL * JT + l] = 0.f;
+    T[F_YH * JT + l] = 1.0e15f; T[F_YL * JT + l] = 0.f;
+    T[F_ZH * JT + l] = 1.0e15f; T[F_ZL * JT + l] = 0.f;
+    T[F_VX * JT + l] = 0.f; T[F_VY * JT + l] = 0.f; T[F_VZ * JT + l] = 0.f;
+    T[F_MN * JT + l] = -0.f;
+  }
+  // tile maxima of |v| and m (block reduction), rounded up when narrowed
+  __shared__ double s_v[JT / 32], s_m[JT / 32];
+  __shared__ int s_n[JT / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    vabs = fmax(vabs, __shfl_xor_sync(0xffffffffu, vabs, o));
+    mj = fmax(mj, __shfl_xor_sync(0xffffffffu, mj, o));
+    real += __shfl_xor_sync(0xffffffffu, real, o);
+  }
+  if ((l & 31) == 0) { s_v[l >> 5] = vabs; s_m[l >> 5] = mj; s_n[l >> 5] = real; }
+  __syncthreads();
+  if (l == 0) {
+    double vm = 0.0, mm = 0.0;
+    int nr = 0;
+    for (int w = 0; w < JT / 32; ++w) { vm = fmax(vm, s_v[w]); mm = fmax(mm, s_m[w]); nr += s_n[w]; }
+    T[NFIELD * JT + 0] = (float)(vm * (1.0 + 0x1p-20));
+    T[NFIELD * JT + 1] = (float)(sqrt(fmax(mm, 0.0)) * (1.0 + 0x1p-20));
+    T[NFIELD * JT + 2] = (float)nr;
+    T[NFIELD * JT + 3] = 0.f;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Exact FP64 neighbour decision, in the expression order of the FP64 oracle
+// (no contraction: explicit round-to-nearest mul/add).
+__device__ __forceinline__ bool nb_test_fp64(const ISet &is, int i, const JSet &js, int j,
+                                             bool mflag) {
+  const double xi0 = is.x[3 * i], xi1 = is.x[3 * i + 1], xi2 = is.x[3 * i + 2];
+  const double vi0 = is.v[3 * i], vi1 = is.v[3 * i + 1], vi2 = is.v[3 * i + 2];
+  const double dx = __dadd_rn(js.x64[3 * j], -xi0);
+  const double dy = __dadd_rn(js.x64[3 * j + 1], -xi1);
+  const double dz = __dadd_rn(js.x64[3 * j + 2], -xi2);
+  const double dvx = __dadd_rn(js.v64[3 * j], -vi0);
+  const double dvy = __dadd_rn(js.v64[3 * j + 1], -vi1);
+  const double dvz = __dadd_rn(js.v64[3 * j + 2], -vi2);
+  const double dtr = is.dtr[i];
+  const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  const double px = __dadd_rn(dx, __dmul_rn(dvx, dtr));
+  const double py = __dadd_rn(dy, __dmul_rn(dvy, dtr));
+  const double pz = __dadd_rn(dz, __dmul_rn(dvz, dtr));
+  const double r2p = __dadd_rn(__dadd_rn(__dmul_rn(px, px), __dmul_rn(py, py)), __dmul_rn(pz, pz));
+  const double r2min = r2 < r2p ? r2 : r2p;
+  const double crit = mflag ? __dmul_rn(js.m64[j], is.h2[i]) : is.h2[i];
+  return r2min < crit;
+}
+
+// ---------------------------------------------------------------------------
+// Per-i register state of the split-precision kernel.
+struct IState {
+  f2 nxh, nyh, nzh, nxl, nyl, nzl;  // -(hi, lo) of the position, duplicated
+  f2 nvx, nvy, nvz;                 // -velocity, duplicated
+  float s;                          // sqrt(h2) * (1 + 2^-12)  (filter radius)
+  float dv;                         // |dtr| * (1 + 2^-12)
+  float va;                         // |v_i| * (1 + 2^-12)
+  float h2f, dtrf;
+  int i;
+};
+
+__device__ __forceinline__ void load_istate(IState &I, const ISet &is, int i, bool valid,
+                                            int *err, bool report) {
+  double x0 = 0, x1 = 0, x2 = 0, v0 = 0, v1 = 0, v2 = 0, h2 = -1.0, dtr = 0;
+  if (valid) {
+    x0 = is.x[3 * i]; x1 = is.x[3 * i + 1]; x2 = is.x[3 * i + 2];
+    v0 = is.v[3 * i]; v1 = is.v[3 * i + 1]; v2 = is.v[3 * i + 2];
+    h2 = is.h2[i]; dtr = is.dtr[i];
+    if (report && (isnan(x0) || isnan(x1) || isnan(x2) || isnan(v0) || isnan(v1) ||
+                   isnan(v2) || isnan(h2) || isnan(dtr)))
+      raise_error(err, GPUNB_E_NAN);
+  }
+  float h, l;
+  ds_split(x0, h, l); I.nxh = mk2(-h); I.nxl = mk2(-l);
+  ds_split(x1, h, l); I.nyh = mk2(-h); I.nyl = mk2(-l);
+  ds_split(x2, h, l); I.nzh = mk2(-h); I.nzl = mk2(-l);
+  I.nvx = mk2(-(float)v0); I.nvy = mk2(-(float)v1); I.nvz = mk2(-(float)v2);
+  const double grow = 1.0 + 0x1p-12;
+  I.s = valid ? (float)(sqrt(fmax(h2, 0.0)) * grow) : -1.0f;
+  I.dv = (float)(fabs(dtr) * grow);
+  I.va = (float)(sqrt(v0 * v0 + v1 * v1 + v2 * v2) * grow);
+  I.h2f = (float)h2;
+  I.dtrf = (float)dtr;
+  I.i = valid ? i : -1;
+}
+
+// Decide one candidate pair (rare path).  FP32 decision, FP64 re-test when
+// the FP32 value lies inside a conservative error band around the criterion.
+template <bool MFLAG>
+__device__ __noinline__ bool decide_pair(const IState &I, const ISet &is, const JSet &js, int jg,
+                                         float dx, float dy, float dz, float dvx, float dvy,
+                                         float dvz, float r2, float mneg_half) {
+  const float px = fmaf(I.dtrf, dvx, dx);
+  const float py = fmaf(I.dtrf, dvy, dy);
+  const float pz = fmaf(I.dtrf, dvz, dz);
+  const float r2p = fmaf(px, px, fmaf(py, py, pz * pz));
+  const float r2min = fminf(r2, r2p);
+  const float crit = MFLAG ? (-2.0f * mneg_half) * I.h2f : I.h2f;
+  bool in = r2min < crit;
+  // error band: FP32 rounding of positions' differences, velocities, h2 and
+  // the products, bounded generously by 2^-14 of the magnitudes involved
+  const float dv = sqrtf(fmaf(dvx, dvx, fmaf(dvy, dvy, dvz * dvz)));
+  const float w = 2.0f * fabsf(I.dtrf) * (I.va + dv);
+  const float band = 0x1p-14f * (fabsf(crit) + r2 + w * w);
+  if (fabsf(r2min - crit) <= band) in = nb_test_fp64(is, I.i, js, jg, MFLAG);
+  return in;
+}
+
+__device__ __forceinline__ void record_neighbour(const RegfOut &out, int i, int j) {
+  const int slot = atomicAdd(out.cnt + i, 1);
+  if (slot < out.cap) out.rows[(size_t)i * out.cap + slot] = j;
+}
+
+// ---------------------------------------------------------------------------
+// Split-precision pair kernel.
+//   IPT : i-particles per thread (independent chains)
+//   WI  : warps along i;  WJ : warps splitting each j tile (same i's)
+//   NSTAGE : j tiles in flight (bulk-async ring)
+// Grid: (ceil(ni / (32*IPT*WI)), S); split s covers tiles [s*ntile/S, (s+1)*ntile/S).
+constexpr int NSTAGE = 4;
+
+template <int IPT, int WI, int WJ, bool MFLAG>
+__global__ void __launch_bounds__(32 * WI * WJ)
+    regf_ds_kernel(const JSet js, const ISet is, const RegfOut out) {
+  constexpr int NT = 32 * WI * WJ;
+  constexpr int ITILE = 32 * IPT * WI;
+  constexpr int JW = JT / WJ;
+  static_assert(JW % 2 == 0, "j per warp must be even");
+  extern __shared__ __align__(128) float smem[];
+  float *ring = smem;                                   // NSTAGE * TILE_FLOATS
+  float *ffs = smem + NSTAGE * TILE_FLOATS;             // [2][NQ][IPT][NT] float-float
+  __shared__ __align__(8) uint64_t bar[NSTAGE];
+  __shared__ int s_abort;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wi = warp % WI, wj = warp / WI;
+  const int ns = gridDim.y, sy = blockIdx.y;
+  const int t0 = (int)(((long long)js.ntile * sy) / ns);
+  const int t1 = (int)(((long long)js.ntile * (sy + 1)) / ns);
+  const int nt = t1 - t0;
+
+  if (tid == 0) {
+    for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+    fence_mbar_init();
+    s_abort = 0;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int s = 0; s < NSTAGE && s < nt; ++s) {
+      mbar_expect_tx(&bar[s], TILE_BYTES);
+      bulk_g2s(ring + s * TILE_FLOATS, js.tiles + (size_t)(t0 + s) * TILE_FLOATS, TILE_BYTES,
+               &bar[s]);
+    }
+  }
+
+  IState I[IPT];
+  f2 q[IPT][NQ];
+#pragma unroll
+  for (int k = 0; k < IPT; ++k) {
+    const int i = blockIdx.x * ITILE + wi * 32 * IPT + k * 32 + lane;
+    load_istate(I[k], is, i, i < is.ni, out.err, sy == 0 && wj == 0);
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) {
+      q[k][c] = make_float2(0.f, 0.f);
+      ffs[((0 * NQ + c) * IPT + k) * NT + tid] = 0.f;
+      ffs[((1 * NQ + c) * IPT + k) * NT + tid] = 0.f;
+    }
+  }
+
+  int t = 0;
+  for (; t < nt; ++t) {
+    const int s = t % NSTAGE;
+    const uint32_t par = (uint32_t)(t / NSTAGE) & 1u;
+    if (!mbar_wait_bounded(&bar[s], par)) s_abort = 1;
+    const float *T = ring + s * TILE_FLOATS;
+    const float vmax = T[NFIELD * JT + 0];
+    const float smax = T[NFIELD * JT + 1];
+    float H[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+      const float base = I[k].dv * (I[k].va + vmax);
+      const float b = MFLAG ? fmaf(I[k].s, smax, base) : I[k].s + base;
+      H[k] = (I[k].s < 0.f) ? -1.0f : b * b;
+    }
+    const int jbeg = wj * JW;
+#pragma unroll 2
+    for (int jj = jbeg; jj < jbeg + JW; jj += 2) {
+      const f2 xh = *(const f2 *)(T + F_XH * JT + jj);
+      const f2 yh = *(const f2 *)(T + F_YH * JT + jj);
+      const f2 zh = *(const f2 *)(T + F_ZH * JT + jj);
+      const f2 xl = *(const f2 *)(T + F_XL * JT + jj);
+      const f2 yl = *(const f2 *)(T + F_YL * JT + jj);
+      const f2 zl = *(const f2 *)(T + F_ZL * JT + jj);
+      const f2 vx = *(const f2 *)(T + F_VX * JT + jj);
+      const f2 vy = *(const f2 *)(T + F_VY * JT + jj);
+      const f2 vz = *(const f2 *)(T + F_VZ * JT + jj);
+      const f2 mn = *(const f2 *)(T + F_MN * JT + jj);
+      f2 dx[IPT], dy[IPT], dz[IPT], dvx[IPT], dvy[IPT], dvz[IPT], r2[IPT], rv[IPT], z[IPT];
+      bool cand = false;
+#pragma unroll
+      for (int k = 0; k < IPT; ++k) {
+        // double-single coordinate difference: (hi_j - hi_i) + (lo_j - lo_i)
+        dx[k] = add2(add2(xh, I[k].nxh), add2(xl, I[k].nxl));
+        dy[k] = add2(add2(yh, I[k].nyh), add2(yl, I[k].nyl));
+        dz[k] = add2(add2(zh, I[k].nzh), add2(zl, I[k].nzl));
+        dvx[k] = add2(vx, I[k].nvx);
+        dvy[k] = add2(vy, I[k].nvy);
+        dvz[k] = add2(vz, I[k].nvz);
+        r2[k] = fma2(dz[k], dz[k], fma2(dy[k], dy[k], mul2(dx[k], dx[k])));
+        rv[k] = fma2(dz[k], dvz[k], fma2(dy[k], dvy[k], mul2(dx[k], dvx[k])));
+        // rsqrt estimate + one Newton step, scaled: z = y0 (x y0^2 - 3) = -2/r
+        const f2 y0 = make_float2(rsqrtf(r2[k].x), rsqrtf(r2[k].y));
+        const f2 a = mul2(r2[k], y0);
+        z[k] = mul2(y0, fma2(a, y0, mk2(-3.0f)));
+        cand |= (r2[k].x < H[k]) | (r2[k].y < H[k]);
+      }
+      if (__any_sync(0xffffffffu, cand)) {
+        const int jg0 = (t0 + t) * JT + jj;
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+          if (r2[k].x < H[k] && jg0 < js.nj) {   // padding bodies never qualify
+            if (decide_pair<MFLAG>(I[k], is, js, jg0, dx[k].x, dy[k].x, dz[k].x, dvx[k].x,
+                                   dvy[k].x, dvz[k].x, r2[k].x, mn.x)) {
+              record_neighbour(out, I[k].i, jg0);
+              z[k].x = 0.f;
+            }
+          }
+          if (r2[k].y < H[k] && jg0 + 1 < js.nj) {
+            if (decide_pair<MFLAG>(I[k], is, js, jg0 + 1, dx[k].y, dy[k].y, dz[k].y, dvx[k].y,
+                                   dvy[k].y, dvz[k].y, r2[k].y, mn.y)) {
+              record_neighbour(out, I[k].i, jg0 + 1);
+              z[k].y = 0.f;
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < IPT; ++k) {
+        const f2 mr = mul2(mn, z[k]);          // m/r
+        const f2 z2 = mul2(z[k], z[k]);        // 4/r^2
+        const f2 mr3 = mul2(mr, z2);           // 4 m/r^3
+        q[k][6] = add2(q[k][6], mr);
+        q[k][0] = fma2(mr3, dx[k], q[k][0]);
+        q[k][1] = fma2(mr3, dy[k], q[k][1]);
+        q[k][2] = fma2(mr3, dz[k], q[k][2]);
+        const f2 al = mul2(mul2(rv[k], z2), mk2(-0.75f));   // -3 (r.v)/r^2
+        q[k][3] = fma2(mr3, fma2(al, dx[k], dvx[k]), q[k][3]);
+        q[k][4] = fma2(mr3, fma2(al, dy[k], dvy[k]), q[k][4]);
+        q[k][5] = fma2(mr3, fma2(al, dz[k], dvz[k]), q[k][5]);
+      }
+    }
+    // fold the tile's FP32 chunk sums into the float-float accumulators
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+#pragma unroll
+      for (int c = 0; c < NQ; ++c) {
+        float &hi = ffs[((0 * NQ + c) * IPT + k) * NT + tid];
+        float &lo = ffs[((1 * NQ + c) * IPT + k) * NT + tid];
+        float h = hi, l = lo;
+        ff_accum(h, l, __fadd_rn(q[k][c].x, q[k][c].y));
+        hi = h; lo = l;
+        q[k][c] = make_float2(0.f, 0.f);
+      }
+    }
+    __syncthreads();
+    if (s_abort) break;
+    if (tid == 0 && t + NSTAGE < nt) {
+      mbar_expect_tx(&bar[s], TILE_BYTES);
+      bulk_g2s(ring + s * TILE_FLOATS, js.tiles + (size_t)(t0 + t + NSTAGE) * TILE_FLOATS,
+               TILE_BYTES, &bar[s]);
+    }
+  }
+  if (s_abort) {
+    // let any copy still in flight land before the block exits
+    if (tid == 0) {
+      for (int u = t + 1; u < nt && u < t + NSTAGE; ++u)
+        mbar_wait_bounded(&bar[u % NSTAGE], (uint32_t)(u / NSTAGE) & 1u, 1u << 16);
+      raise_error(out.err, GPUNB_E_TIMEOUT);
+    }
+    return;
+  }
+
+  // fixed-order merge of the WJ j-subranges (warps wj > 0 into wj == 0)
+  if (WJ > 1) {
+    if (wj == 0) {
+#pragma unroll
+      for (int k = 0; k < IPT; ++k)
+#pragma unroll
+        for (int c = 0; c < NQ; ++c) {
+          float h = ffs[((0 * NQ + c) * IPT + k) * NT + tid];
+          float l = ffs[((1 * NQ + c) * IPT + k) * NT + tid];
+          for (int w = 1; w < WJ; ++w) {
+            const int src = tid + w * 32 * WI;
+            ff_add(h, l, ffs[((0 * NQ + c) * IPT + k) * NT + src],
+                   ffs[((1 * NQ + c) * IPT + k) * NT + src]);
+          }
+          ffs[((0 * NQ + c) * IPT + k) * NT + tid] = h;
+          ffs[((1 * NQ + c) * IPT + k) * NT + tid] = l;
+        }
+    }
+  }
+  if (wj == 0) {
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+      const int i = I[k].i;
+      if (i < 0) continue;
+#pragma unroll
+      for (int c = 0; c < NQ; ++c) {
+        const double v = (double)ffs[((0 * NQ + c) * IPT + k) * NT + tid] +
+                         (double)ffs[((1 * NQ + c) * IPT + k) * NT + tid];
+        out.part[((size_t)sy * NQ + c) * out.ni_pad + i] = v;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plain FP64 pair kernel (the FP64 baseline of the metric): regint.f:39-79
+// arithmetic, j in FP64 staged through shared memory, one i per thread.
+template <bool MFLAG>
+__global__ void __launch_bounds__(128) regf_fp64_kernel(const JSet js, const ISet is,
+                                                        const RegfOut out) {
+  constexpr int NT = 128;
+  __shared__ double sx[JT64 * 3], sv[JT64 * 3], sm[JT64];
+  const int tid = threadIdx.x;
+  const int i = blockIdx.x * NT + tid;
+  const bool valid = i < is.ni;
+  const int ns = gridDim.y, sy = blockIdx.y;
+  const int t0 = (int)(((long long)js.ntile64 * sy) / ns);
+  const int t1 = (int)(((long long)js.ntile64 * (sy + 1)) / ns);
+  double xi0 = 0, xi1 = 0, xi2 = 0, vi0 = 0, vi1 = 0, vi2 = 0, h2 = -1, dtr = 0;
+  if (valid) {
+    xi0 = is.x[3 * i]; xi1 = is.x[3 * i + 1]; xi2 = is.x[3 * i + 2];
+    vi0 = is.v[3 * i]; vi1 = is.v[3 * i + 1]; vi2 = is.v[3 * i + 2];
+    h2 = is.h2[i]; dtr = is.dtr[i];
+  }
+  double ax = 0, ay = 0, az = 0, jx = 0, jy = 0, jz = 0, po = 0;
+  for (int t = t0; t < t1; ++t) {
+    const int jb = t * JT64;
+    const int n = min(JT64, js.nj - jb);
+    __syncthreads();
+    for (int u = tid; u < 3 * n; u += NT) { sx[u] = js.x64[3 * jb + u]; sv[u] = js.v64[3 * jb + u]; }
+    for (int u = tid; u < n; u += NT) sm[u] = js.m64[jb + u];
+    __syncthreads();
+    if (!valid) continue;
+    for (int jj = 0; jj < n; ++jj) {
+      const double dx = __dadd_rn(sx[3 * jj], -xi0);
+      const double dy = __dadd_rn(sx[3 * jj + 1], -xi1);
+      const double dz = __dadd_rn(sx[3 * jj + 2], -xi2);
+      const double dvx = __dadd_rn(sv[3 * jj], -vi0);
+      const double dvy = __dadd_rn(sv[3 * jj + 1], -vi1);
+      const double dvz = __dadd_rn(sv[3 * jj + 2], -vi2);
+      const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+      const double px = __dadd_rn(dx, __dmul_rn(dvx, dtr));
+      const double py = __dadd_rn(dy, __dmul_rn(dvy, dtr));
+      const double pz = __dadd_rn(dz, __dmul_rn(dvz, dtr));
+      const double r2p = __dadd_rn(__dadd_rn(__dmul_rn(px, px), __dmul_rn(py, py)), __dmul_rn(pz, pz));
+      const double r2min = r2 < r2p ? r2 : r2p;
+      const double crit = MFLAG ? __dmul_rn(sm[jj], h2) : h2;
+      if (r2min < crit) {
+        record_neighbour(out, i, jb + jj);
+        continue;
+      }
+      const double dr2i = 1.0 / r2;
+      const double dr3i = sm[jj] * dr2i * sqrt(dr2i);
+      const double drdp = 3.0 * (dx * dvx + dy * dvy + dz * dvz) * dr2i;
+      ax += dx * dr3i; ay += dy * dr3i; az += dz * dr3i;
+      jx += (dvx - dx * drdp) * dr3i;
+      jy += (dvy - dy * drdp) * dr3i;
+      jz += (dvz - dz * drdp) * dr3i;
+      po += dr3i * r2;
+    }
+  }
+  if (valid) {
+    // same partial layout as the split kernel, which stores 4x acc/jrk
+    double *p = out.part + (size_t)sy * NQ * out.ni_pad + i;
+    p[0 * out.ni_pad] = 4.0 * ax; p[1 * out.ni_pad] = 4.0 * ay; p[2 * out.ni_pad] = 4.0 * az;
+    p[3 * out.ni_pad] = 4.0 * jx; p[4 * out.ni_pad] = 4.0 * jy; p[5 * out.ni_pad] = 4.0 * jz;
+    p[6 * out.ni_pad] = po;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Merge of the S j-split partials in FP64, fixed order s = 0..S-1 (the
+// deterministic replacement of force_reduce_kernel + the host sum over GPUs,
+// gpunb.velocity.cu:441-496,822-845).  Also turns counts into the in-band
+// overflow flag of gpunb.velocity.cu:872-877 / reg.avx.cpp:320-321.
+__global__ void regf_merge_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
+                                  const int *__restrict__ cnt, int nnbmax,
+                                  double *__restrict__ acc, double *__restrict__ jrk,
+                                  double *__restrict__ pot, int *__restrict__ nnb,
+                                  int *__restrict__ rowlen) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ni) return;
+  double s[NQ];
+#pragma unroll
+  for (int c = 0; c < NQ; ++c) s[c] = 0.0;
+  for (int k = 0; k < S; ++k) {
+    const double *p = part + (size_t)k * NQ * ni_pad + i;
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * ni_pad];
+  }
+  acc[3 * i + 0] = 0.25 * s[0];
+  acc[3 * i + 1] = 0.25 * s[1];
+  acc[3 * i + 2] = 0.25 * s[2];
+  jrk[3 * i + 0] = 0.25 * s[3];
+  jrk[3 * i + 1] = 0.25 * s[4];
+  jrk[3 * i + 2] = 0.25 * s[5];
+  pot[i] = s[6];
+  const int c = cnt[i];
+  const bool over = c > nnbmax;
+  nnb[i] = over ? -c : c;
+  rowlen[i] = over ? 0 : c;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of row lengths: per-block scan (SCAN_ITEMS per block) with
+// block totals, then one block scanning the totals.  The gather adds the
+// block offset, so no third pass is needed.
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_PER_THREAD = 4;
+constexpr int SCAN_ITEMS = SCAN_THREADS * SCAN_PER_THREAD;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *sh, int &total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    sh[lane] = w;
+  }
+  __syncthreads();
+  const int before = (warp > 0) ? sh[warp - 1] : 0;
+  total = sh[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) list_scan_blocks_kernel(
+    const int *__restrict__ len, int n, int *__restrict__ off, int *__restrict__ btotal) {
+  __shared__ int sh[32];
+  const int base = blockIdx.x * SCAN_ITEMS + threadIdx.x * SCAN_PER_THREAD;
+  int v[SCAN_PER_THREAD], sum = 0;
+#pragma unroll
+  for (int u = 0; u < SCAN_PER_THREAD; ++u) {
+    v[u] = (base + u < n) ? len[base + u] : 0;
+    sum += v[u];
+  }
+  int total;
+  int ex = block_exclusive_scan(sum, sh, total);
+#pragma unroll
+  for (int u = 0; u < SCAN_PER_THREAD; ++u) {
+    if (base + u < n) off[base + u] = ex;
+    ex += v[u];
+  }
+  if (threadIdx.x == 0) btotal[blockIdx.x] = total;
+}
+
+// scans up to SCAN_THREADS*SCAN_PER_THREAD block totals in place; writes the
+// grand total to btotal[nb]
+__global__ void __launch_bounds__(SCAN_THREADS) list_scan_totals_kernel(int *btotal, int nb) {
+  __shared__ int sh[32];
+  const int base = threadIdx.x * SCAN_PER_THREAD;
+  int v[SCAN_PER_THREAD], sum = 0;
+#pragma unroll
+  for (int u = 0; u < SCAN_PER_THREAD; ++u) {
+    v[u] = (base + u < nb) ? btotal[base + u] : 0;
+    sum += v[u];
+  }
+  int total;
+  int ex = block_exclusive_scan(sum, sh, total);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < SCAN_PER_THREAD; ++u) {
+    if (base + u < nb) btotal[base + u] = ex;
+    ex += v[u];
+  }
+  if (threadIdx.x == 0) btotal[nb] = total;
+}
+
+// One warp per row: sort the row's ids ascending (bitonic, in shared memory)
+// and write them at the row's offset of the dense list.  Rows longer than
+// GATHER_SMEM_IDS are sorted in place in global memory by the same network.
+constexpr int GATHER_WARPS = 8;
+constexpr int GATHER_SMEM_IDS = 1024;
+
+__global__ void __launch_bounds__(32 * GATHER_WARPS) list_gather_kernel(
+    int *__restrict__ rows, int cap, const int *__restrict__ len, const int *__restrict__ off,
+    const int *__restrict__ boff, int ni, int *__restrict__ dense) {
+  __shared__ int buf[GATHER_WARPS][GATHER_SMEM_IDS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = blockIdx.x * GATHER_WARPS + warp;
+  if (i >= ni) return;
+  const int n = len[i];
+  if (n == 0) return;
+  int *row = rows + (size_t)i * cap;
+  const bool in_smem = n <= GATHER_SMEM_IDS;
+  int *a = in_smem ? buf[warp] : row;
+  int p2 = 1;
+  while (p2 < n) p2 <<= 1;
+  if (in_smem) {
+    for (int u = lane; u < p2; u += 32) a[u] = (u < n) ? row[u] : INT_MAX;
+  }
+  __syncwarp();
+  if (!in_smem) p2 = n;  // global fallback: odd-even transposition below
+  if (in_smem) {
+    for (int k = 2; k <= p2; k <<= 1) {
+      for (int jd = k >> 1; jd > 0; jd >>= 1) {
+        for (int u = lane; u < p2; u += 32) {
+          const int l = u ^ jd;
+          if (l > u) {
+            const int x = a[u], y = a[l];
+            const bool up = (u & k) == 0;
+            if ((x > y) == up) { a[u] = y; a[l] = x; }
+          }
+        }
+        __syncwarp();
+      }
+    }
+  } else {
+    for (int phase = 0; phase < n; ++phase) {
+      for (int u = 2 * lane + (phase & 1); u + 1 < n; u += 64) {
+        const int x = a[u], y = a[u + 1];
+        if (x > y) { a[u] = y; a[u + 1] = x; }
+      }
+      __syncwarp();
+    }
+  }
+  const int o = off[i] + boff[i / SCAN_ITEMS];
+  for (int u = lane; u < n; u += 32) dense[o + u] = a[u];
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// Finalise the list offsets for the device-resident API: off[i] += block
+// offset, off[ni] = grand total.
+__global__ void list_finalize_offsets_kernel(int *off, const int *btot, int ni, int nb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ni) off[i] += btot[i / SCAN_ITEMS];
+  if (i == 0) off[ni] = btot[nb];
+}
+
+static const VariantDesc kVariants[] = {{2, 4, 1}, {2, 2, 2}, {1, 1, 8}, {1, 4, 1}};
+constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+
+int regf_num_variants() { return kNumVariants; }
+VariantDesc regf_variant(int v) { return kVariants[v]; }
+
+size_t regf_ds_smem(int v) {
+  const VariantDesc d = kVariants[v];
+  return (size_t)NSTAGE * TILE_BYTES + 2u * NQ * d.ipt * d.threads() * sizeof(float);
+}
+
+typedef void (*regf_fn)(JSet, ISet, RegfOut);
+static regf_fn regf_kernel_ptr(int v, bool mflag) {
+  switch (v) {
+    case 0: return mflag ? regf_ds_kernel<2, 4, 1, true> : regf_ds_kernel<2, 4, 1, false>;
+    case 1: return mflag ? regf_ds_kernel<2, 2, 2, true> : regf_ds_kernel<2, 2, 2, false>;
+    case 2: return mflag ? regf_ds_kernel<1, 1, 8, true> : regf_ds_kernel<1, 1, 8, false>;
+    default: return mflag ? regf_ds_kernel<1, 4, 1, true> : regf_ds_kernel<1, 4, 1, false>;
+  }
+}
+
+int regf_ds_blocks_per_sm(int v, bool mflag) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, regf_kernel_ptr(v, mflag),
+                                                    kVariants[v].threads(),
+                                                    regf_ds_smem(v)) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_pack_jtiles(const double *m, const double *x, const double *v, int nj,
+                               float *tiles, int ntile, int *err, cudaStream_t st) {
+  if (ntile <= 0) return cudaSuccess;
+  pack_jtiles_kernel<<<ntile, JT, 0, st>>>(m, x, v, nj, tiles, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_regf_ds(int v, bool mflag, int gx, int S, const JSet &js, const ISet &is,
+                           const RegfOut &out, cudaStream_t st) {
+  const VariantDesc d = kVariants[v];
+  regf_fn fn = regf_kernel_ptr(v, mflag);
+  const size_t smem = regf_ds_smem(v);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  fn<<<dim3(gx, S), d.threads(), smem, st>>>(js, is, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const ISet &is,
+                             const RegfOut &out, cudaStream_t st) {
+  if (mflag)
+    regf_fp64_kernel<true><<<dim3(gx, S), FP64_THREADS, 0, st>>>(js, is, out);
+  else
+    regf_fp64_kernel<false><<<dim3(gx, S), FP64_THREADS, 0, st>>>(js, is, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *cnt,
+                              int nnbmax, double *acc, double *jrk, double *pot, int *nnb,
+                              int *rowlen, cudaStream_t st) {
+  regf_merge_kernel<<<(ni + 255) / 256, 256, 0, st>>>(part, S, ni, ni_pad, cnt, nnbmax, acc, jrk,
+                                                      pot, nnb, rowlen);
+  return cudaGetLastError();
+}
+
+int list_scan_blocks(int ni) { return (ni + SCAN_ITEMS - 1) / SCAN_ITEMS; }
+
+cudaError_t launch_list_scan(const int *rowlen, int ni, int *off, int *btot, cudaStream_t st) {
+  const int nb = list_scan_blocks(ni);
+  list_scan_blocks_kernel<<<nb, SCAN_THREADS, 0, st>>>(rowlen, ni, off, btot);
+  list_scan_totals_kernel<<<1, SCAN_THREADS, 0, st>>>(btot, nb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_list_gather(int *rows, int cap, const int *rowlen, const int *off,
+                               const int *btot, int ni, int *dense, cudaStream_t st) {
+  list_gather_kernel<<<(ni + GATHER_WARPS - 1) / GATHER_WARPS, 32 * GATHER_WARPS, 0, st>>>(
+      rows, cap, rowlen, off, btot, ni, dense);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_list_finalize_offsets(int *off, const int *btot, int ni, cudaStream_t st) {
+  list_finalize_offsets_kernel<<<(ni + 255) / 256, 256, 0, st>>>(off, btot, ni,
+                                                                 list_scan_blocks(ni));
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// explicit instantiations exported to the host side
+template __global__ void regf_ds_kernel<2, 4, 1, false>(JSet, ISet, RegfOut);
+template __global__ void regf_ds_kernel<2, 4, 1, true>(JSet, ISet, RegfOut);
+template __global__ void regf_ds_kernel<2, 2, 2, false>(JSet, ISet, RegfOut);
+template __global__ void regf_ds_kernel<2, 2, 2, true>(JSet, ISet, RegfOut);
+template __global__ void regf_ds_kernel<1, 1, 8, false>(JSet, ISet, RegfOut);
+template __global__ void regf_ds_kernel<1, 1, 8, true>(JSet, ISet, RegfOut);
+template __global__ void regf_ds_kernel<1, 4, 1, false>(JSet, ISet, RegfOut);
+template __global__ void regf_ds_kernel<1, 4, 1, true>(JSet, ISet, RegfOut);
+template __global__ void regf_fp64_kernel<false>(JSet, ISet, RegfOut);
+template __global__ void regf_fp64_kernel<true>(JSet, ISet, RegfOut);
+
+}  // namespace gpunb

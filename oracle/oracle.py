@@ -1,0 +1,186 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, as the checker or the timed CPU baseline; the product never imports it.
+
+    regf_fp64(...)  FP64 truth with the gpunb_regf_ contract (oracle_fp64.c)
+    pot_fp64(...)   FP64 gpupot_ semantics
+    Port            portable FP32 restatement of src/Main/reg.avx.cpp / pot.avx.cpp
+    RefAVX          the reference's own reg.avx.cpp / pot.avx.cpp compiled from
+                    its sources into oracle/_ref (x86_64 hosts only)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import platform
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_lib = None
+
+
+def build(ref: bool = False) -> None:
+    """make liboracle.so (and the reference AVX libraries when ref=True and
+    the reference sources are present)."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
+    if ref and platform.machine() == "x86_64" and Path(os.environ.get(
+            "REF", "/root/reference")).joinpath("src/Main/reg.avx.cpp").exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True,
+                       capture_output=True)
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = HERE / "liboracle.so"
+        srcs = [HERE / "oracle_fp64.c", HERE / "port_fp32.c", HERE / "Makefile"]
+        if not path.exists() or any(s.stat().st_mtime > path.stat().st_mtime for s in srcs):
+            build()
+        _lib = C.CDLL(str(path))
+        _lib.oracle_regf_fp64.argtypes = [C.c_int, _D, _D, _D, C.c_int, _D, _D, _D, _D, _D, _D,
+                                          _D, C.c_int, C.c_int, _I, C.c_int, _D, _D]
+        _lib.oracle_pot_fp64.argtypes = [C.c_int, C.c_int, C.c_int, _D, _D, _D]
+        _lib.port_send_fp32.argtypes = [C.c_int, _D, _D, _D]
+        _lib.port_regf_fp32.argtypes = [C.c_int, _D, _D, _D, _D, _D, _D, _D, C.c_int, C.c_int,
+                                        _I, C.c_int]
+        _lib.port_pot_fp32.argtypes = [C.c_int, C.c_int, C.c_int, _D, _D, _D]
+        _lib.oracle_num_threads.restype = C.c_int
+    return _lib
+
+
+def _c(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a.reshape(shape) if shape is not None else a
+
+
+def _dp(a):
+    return a.ctypes.data_as(_D)
+
+
+def num_threads() -> int:
+    return lib().oracle_num_threads()
+
+
+def regf_fp64(m, x, v, h2, dtr, xi, vi, lmax, nnbmax, m_flag=0, with_abs=False):
+    """FP64 oracle of gpunb_regf_ against the j-set (m, x, v).
+    Returns acc, jrk, pot, list [, accabs, jrkabs]."""
+    m = _c(m); n = m.shape[0]
+    x = _c(x, (n, 3)); v = _c(v, (n, 3))
+    h2 = _c(h2); ni = h2.shape[0]
+    dtr = _c(dtr, (ni,)); xi = _c(xi, (ni, 3)); vi = _c(vi, (ni, 3))
+    acc = np.empty((ni, 3)); jrk = np.empty((ni, 3)); pot = np.empty(ni)
+    lst = np.zeros((ni, lmax), dtype=np.int32)
+    aa = np.empty(ni); ja = np.empty(ni)
+    lib().oracle_regf_fp64(n, _dp(m), _dp(x), _dp(v), ni, _dp(h2), _dp(dtr), _dp(xi), _dp(vi),
+                           _dp(acc), _dp(jrk), _dp(pot), lmax, nnbmax,
+                           lst.ctypes.data_as(_I), int(m_flag), _dp(aa), _dp(ja))
+    if with_abs:
+        return acc, jrk, pot, lst, aa, ja
+    return acc, jrk, pot, lst
+
+
+def pot_fp64(m, x, istart=1, ni=None):
+    m = _c(m); n = m.shape[0]; x = _c(x, (n, 3))
+    if ni is None:
+        ni = n - istart + 1
+    pot = np.empty(ni)
+    lib().oracle_pot_fp64(int(istart), int(ni), n, _dp(m), _dp(x), _dp(pot))
+    return pot
+
+
+class Port:
+    """Portable FP32 restatement of the reference CPU path (the CPU baseline)."""
+
+    def send(self, m, x, v):
+        m = _c(m); n = m.shape[0]
+        self._keep = (m, _c(x, (n, 3)), _c(v, (n, 3)))
+        lib().port_send_fp32(n, _dp(self._keep[0]), _dp(self._keep[1]), _dp(self._keep[2]))
+
+    def regf(self, h2, dtr, xi, vi, lmax, nnbmax, m_flag=0):
+        h2 = _c(h2); ni = h2.shape[0]
+        dtr = _c(dtr, (ni,)); xi = _c(xi, (ni, 3)); vi = _c(vi, (ni, 3))
+        acc = np.empty((ni, 3)); jrk = np.empty((ni, 3)); pot = np.empty(ni)
+        lst = np.zeros((ni, lmax), dtype=np.int32)
+        lib().port_regf_fp32(ni, _dp(h2), _dp(dtr), _dp(xi), _dp(vi), _dp(acc), _dp(jrk),
+                             _dp(pot), lmax, nnbmax, lst.ctypes.data_as(_I), int(m_flag))
+        return acc, jrk, pot, lst
+
+    @staticmethod
+    def pot(m, x, istart=1, ni=None):
+        m = _c(m); n = m.shape[0]; x = _c(x, (n, 3))
+        if ni is None:
+            ni = n - istart + 1
+        pot = np.empty(ni)
+        lib().port_pot_fp32(int(istart), int(ni), n, _dp(m), _dp(x), _dp(pot))
+        return pot
+
+
+class RefAVX:
+    """The reference's own CPU regular-force and potential code, compiled from
+    src/Main/reg.avx.cpp and pot.avx.cpp into oracle/_ref (x86_64 only)."""
+
+    REG = HERE / "_ref" / "libref_reg_avx.so"
+    POT = HERE / "_ref" / "libref_pot_avx.so"
+
+    @classmethod
+    def available(cls) -> bool:
+        return cls.REG.exists() and cls.POT.exists() and platform.machine() == "x86_64"
+
+    def __init__(self, nbmax: int):
+        self.reg = C.CDLL(str(self.REG))
+        self.potlib = C.CDLL(str(self.POT))
+        ip = C.POINTER(C.c_int)
+        self.reg.gpunb_open_.argtypes = [ip, ip]
+        self.reg.gpunb_send_.argtypes = [ip, _D, _D, _D]
+        self.reg.gpunb_regf_.argtypes = [ip, _D, _D, _D, _D, _D, _D, _D, ip, ip, ip, ip]
+        self.potlib.gpupot_.argtypes = [ip, ip, ip, ip, _D, _D, _D]
+        a, r = C.c_int(nbmax), C.c_int(0)
+        self.reg.gpunb_open_(C.byref(a), C.byref(r))
+
+    def close(self):
+        self.reg.gpunb_close_()
+
+    def send(self, m, x, v):
+        m = _c(m); n = m.shape[0]
+        self._keep = (m, _c(x, (n, 3)), _c(v, (n, 3)))
+        nj = C.c_int(n)
+        self.reg.gpunb_send_(C.byref(nj), *[_dp(a) for a in self._keep])
+
+    def regf(self, h2, dtr, xi, vi, lmax, nnbmax, m_flag=0):
+        """The AVX loop reads and writes i in groups of 4: pad the arrays."""
+        h2 = _c(h2); ni = h2.shape[0]
+        pad = (ni + 3) // 4 * 4 + 4
+        def padded(a, shape):
+            out = np.zeros(shape)
+            out[:ni] = a
+            return out
+        h2p = padded(h2, (pad,)); dtp = padded(_c(dtr, (ni,)), (pad,))
+        xp = padded(_c(xi, (ni, 3)), (pad, 3)); vp = padded(_c(vi, (ni, 3)), (pad, 3))
+        acc = np.zeros((pad, 3)); jrk = np.zeros((pad, 3)); pot = np.zeros(pad)
+        lst = np.zeros((pad, lmax), dtype=np.int32)
+        a = [C.c_int(ni), C.c_int(lmax), C.c_int(nnbmax), C.c_int(m_flag)]
+        self.reg.gpunb_regf_(C.byref(a[0]), _dp(h2p), _dp(dtp), _dp(xp), _dp(vp), _dp(acc),
+                             _dp(jrk), _dp(pot), C.byref(a[1]), C.byref(a[2]),
+                             lst.ctypes.data_as(_I), C.byref(a[3]))
+        return acc[:ni], jrk[:ni], pot[:ni], lst[:ni]
+
+    def pot(self, m, x, istart=1, ni=None):
+        """pot.avx.cpp reads particles and writes results 8 at a time, and
+        indexes its output by absolute i (pot.avx.cpp:87-137), unlike the GPU
+        version (gpupot.gpu.cu:101-105) whose output starts at istart; the
+        result is returned istart-relative here."""
+        m = _c(m); n = m.shape[0]
+        if ni is None:
+            ni = n - istart + 1
+        mp = np.zeros(n + 16); mp[:n] = m
+        xp = np.zeros((n + 16, 3)); xp[:n] = _c(x, (n, 3))
+        pot = np.zeros(istart - 1 + ni + 16)
+        a = [C.c_int(0), C.c_int(istart), C.c_int(ni), C.c_int(n)]
+        self.potlib.gpupot_(*[C.byref(v) for v in a], _dp(mp), _dp(xp), _dp(pot))
+        return pot[istart - 1:istart - 1 + ni]

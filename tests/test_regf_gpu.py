@@ -1,0 +1,204 @@
+"""GPU parity of gpunb_regf_ / gpupot_ (through the C ABI) against the FP64
+oracle and the golden vectors of the reference's CPU path.
+
+Tolerances (FP64 oracle as truth):
+  * split precision: per-particle |dF|/|F| <= 1e-6 for force, jerk and
+    potential at the 99th percentile, <= 1e-5 maximum, and the error measured
+    against sum_j |f_j| (well defined where |F| ~ 0) <= 1e-6 everywhere;
+  * plain FP64 kernel: <= 1e-12;
+  * neighbour lists: identical to the oracle, bit for bit (counts, overflow
+    flags and ids in ascending order).
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_vec_err, rows_equal, unpack_list
+from nbody6ppgpu_gb300 import ics
+from nbody6ppgpu_gb300.gpunb import GpuNb, GpunbError, gpupot, load
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SPLIT_P99 = 1e-6
+SPLIT_MAX = 1e-5
+SPLIT_ABS = 1e-6
+FP64_TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return load()
+
+
+def check_forces(res, acc, jrk, pot, accabs=None, jrkabs=None, p99=SPLIT_P99, mx=SPLIT_MAX,
+                 absn=SPLIT_ABS, rows=None):
+    ok = res.list[:, 0] >= 0 if rows is None else rows
+    ea = rel_vec_err(res.acc[ok], acc[ok])
+    ej = rel_vec_err(res.jrk[ok], jrk[ok])
+    ep = np.abs(res.pot[ok] - pot[ok]) / np.abs(pot[ok])
+    for name, e in (("acc", ea), ("jrk", ej), ("pot", ep)):
+        assert np.percentile(e, 99) <= p99, (name, np.percentile(e, 99))
+        assert e.max() <= mx, (name, e.max())
+    if accabs is not None:
+        na = np.linalg.norm(res.acc[ok] - acc[ok], axis=1) / accabs[ok]
+        nj = np.linalg.norm(res.jrk[ok] - jrk[ok], axis=1) / jrkabs[ok]
+        assert na.max() <= absn, ("acc/sum|f|", na.max())
+        assert nj.max() <= absn, ("jrk/sum|f|", nj.max())
+
+
+def run_golden(g, precision="split", variant=-1, splits=0):
+    n = len(g["m"])
+    with GpuNb(max(n, 1)) as nb:
+        nb.set_precision(precision)
+        nb.set_launch(variant, splits)
+        nb.send(g["m"], g["x"], g["v"])
+        ii = g["ii"]
+        return nb.regf(g["h2"], g["dtr"], g["x"][ii], g["v"][ii], int(g["lmax"]),
+                       int(g["nnbmax"]), int(g["m_flag"]))
+
+
+@pytest.mark.parametrize("name", ["cfg1_plummer2048", "mflag_plummer512",
+                                  "overflow_plummer512", "ragged_n37"])
+@pytest.mark.parametrize("precision", ["split", "fp64"])
+def test_golden_cases(lib, name, precision):
+    g = load_golden(name)
+    res = run_golden(g, precision)
+    lmax = int(g["lmax"])
+    assert rows_equal(res.list, unpack_list(g["fp64_cnt"], g["fp64_ids"], lmax)) == []
+    # and therefore identical to the reference CPU path's lists too
+    assert rows_equal(res.list, unpack_list(g["ref_cnt"], g["ref_ids"], lmax)) == []
+    if precision == "split":
+        check_forces(res, g["fp64_acc"], g["fp64_jrk"], g["fp64_pot"], g["fp64_accabs"],
+                     g["fp64_jrkabs"])
+    else:
+        ok = res.list[:, 0] >= 0
+        np.testing.assert_allclose(res.acc[ok], g["fp64_acc"][ok], rtol=FP64_TOL, atol=1e-14)
+        np.testing.assert_allclose(res.pot[ok], g["fp64_pot"][ok], rtol=FP64_TOL)
+
+
+def test_all_launch_shapes_agree_and_are_deterministic(lib):
+    g = load_golden("cfg1_plummer2048")
+    base = run_golden(g, "split", 0, 0)
+    again = run_golden(g, "split", 0, 0)
+    assert np.array_equal(base.acc, again.acc) and np.array_equal(base.list, again.list)
+    nv = lib.gpunb_num_variants()
+    for v in range(nv):
+        for s in (1, 3, 16):
+            r = run_golden(g, "split", v, s)
+            assert rows_equal(r.list, base.list) == [], (v, s)
+            check_forces(r, g["fp64_acc"], g["fp64_jrk"], g["fp64_pot"], g["fp64_accabs"],
+                         g["fp64_jrkabs"])
+
+
+@pytest.fixture(scope="module")
+def plummer64k():
+    c = ics.plummer(65536, seed=2, masses="kroupa", nb_target=100.0)
+    return c
+
+
+@pytest.mark.parametrize("ni", [1, 32, 1024, 16384])
+def test_config2_block_sizes(lib, plummer64k, ni):
+    """Plummer N=65536, Kroupa masses, target 100, nbmax 512; the oracle is
+    evaluated on (a sample of) the same active block."""
+    c = plummer64k
+    act = ics.active_set(c.n, ni, seed=ni)
+    with GpuNb(c.n) as nb:
+        nb.send(c.m, c.x, c.v)
+        res = nb.regf(c.h2()[act], c.dtr[act], c.x[act], c.v[act], 513, 512)
+    samp = np.arange(ni) if ni <= 1024 else np.linspace(0, ni - 1, 512).astype(int)
+    a = act[samp]
+    acc, jrk, pot, lst, aa, ja = O.regf_fp64(c.m, c.x, c.v, c.h2()[a], c.dtr[a], c.x[a], c.v[a],
+                                             513, 512, with_abs=True)
+    sub = type(res)(acc=res.acc[samp], jrk=res.jrk[samp], pot=res.pot[samp], list=res.list[samp])
+    assert rows_equal(sub.list, lst) == []
+    check_forces(sub, acc, jrk, pot, aa, ja)
+
+
+def test_fp64_kernel_matches_oracle(lib, plummer64k):
+    c = plummer64k
+    act = ics.active_set(c.n, 300, seed=5)
+    with GpuNb(c.n) as nb:
+        nb.set_precision("fp64")
+        nb.send(c.m, c.x, c.v)
+        res = nb.regf(c.h2()[act], c.dtr[act], c.x[act], c.v[act], 513, 512)
+    acc, jrk, pot, lst = O.regf_fp64(c.m, c.x, c.v, c.h2()[act], c.dtr[act], c.x[act], c.v[act],
+                                     513, 512)
+    assert rows_equal(res.list, lst) == []
+    assert rel_vec_err(res.acc, acc).max() < FP64_TOL
+    assert rel_vec_err(res.jrk, jrk).max() < 1e-10
+
+
+def test_edge_cases(lib):
+    c = ics.plummer(300, seed=8, nb_target=10.0)
+    with GpuNb(1000) as nb:
+        # empty j-set: no force, no neighbours
+        nb.send(np.zeros(0), np.zeros((0, 3)), np.zeros((0, 3)))
+        r = nb.regf(c.h2()[:3], c.dtr[:3], c.x[:3], c.v[:3], 8, 7)
+        assert np.all(r.acc == 0) and np.all(r.pot == 0) and np.all(r.list[:, 0] == 0)
+        # a single body: only itself as neighbour
+        nb.send(c.m[:1], c.x[:1], c.v[:1])
+        r = nb.regf(c.h2()[:1], c.dtr[:1], c.x[:1], c.v[:1], 8, 7)
+        assert list(r.list[0, :2]) == [1, 0] and np.all(r.acc == 0)
+        # ragged ni, tiny h2 (self only), nnbmax = 0 -> every row overflows (-1)
+        nb.send(c.m, c.x, c.v)
+        h2 = np.full(7, 1e-30)
+        r = nb.regf(h2, c.dtr[:7], c.x[:7], c.v[:7], 4, 3)
+        assert np.all(r.list[:, 0] == 1) and np.array_equal(r.list[:, 1], np.arange(7))
+        r = nb.regf(h2, c.dtr[:7], c.x[:7], c.v[:7], 4, 0)
+        assert np.all(r.list[:, 0] == -1)
+        acc, jrk, pot, lst = O.regf_fp64(c.m, c.x, c.v, h2, c.dtr[:7], c.x[:7], c.v[:7], 4, 3)
+        r = nb.regf(h2, c.dtr[:7], c.x[:7], c.v[:7], 4, 3)
+        check_forces(r, acc, jrk, pot)
+        # i-particles not in the j-set (no self) and h2 on an exact boundary
+        xi = c.x[:2] + 0.5
+        acc, jrk, pot, lst = O.regf_fp64(c.m, c.x, c.v, c.h2()[:2], c.dtr[:2], xi, c.v[:2], 64, 63)
+        r = nb.regf(c.h2()[:2], c.dtr[:2], xi, c.v[:2], 64, 63)
+        assert rows_equal(r.list, lst) == []
+        d2 = np.sum((c.x[5] - c.x[0]) ** 2)   # body 5 exactly at r2 == h2: not a neighbour
+        acc, jrk, pot, lst = O.regf_fp64(c.m, c.x, c.v, [d2], [0.0], c.x[:1], c.v[:1], 64, 63)
+        r = nb.regf([d2], [0.0], c.x[:1], c.v[:1], 64, 63)
+        assert rows_equal(r.list, lst) == [] and 5 not in r.neighbours(0)
+
+
+def test_errors_are_reported(lib):
+    c = ics.plummer(64, seed=1, nb_target=5.0)
+    with GpuNb(64) as nb:
+        with pytest.raises(GpunbError) as e:
+            nb.send(np.ones(65), np.zeros((65, 3)), np.zeros((65, 3)))
+        assert e.value.code == 5
+        x = c.x.copy()
+        x[3, 1] = np.nan
+        with pytest.raises(GpunbError) as e:
+            nb.send(c.m, x, c.v)
+        assert e.value.code == 3
+        nb.send(c.m, c.x, c.v)
+        with pytest.raises(GpunbError) as e:
+            nb.regf(c.h2()[:4], c.dtr[:4], c.x[:4], c.v[:4], 8, 8)   # nnbmax > lmax-1
+        assert e.value.code == 2
+        xi = c.x[:4].copy()
+        xi[0, 0] = np.nan
+        with pytest.raises(GpunbError) as e:
+            nb.regf(c.h2()[:4], c.dtr[:4], xi, c.v[:4], 8, 7)
+        assert e.value.code == 3
+        # the library stays usable after a reported error
+        r = nb.regf(c.h2()[:4], c.dtr[:4], c.x[:4], c.v[:4], 8, 7)
+        assert np.all(np.isfinite(r.acc))
+
+
+def test_gpupot_golden(lib):
+    g = load_golden("pot_plummer2048")
+    p = gpupot(g["m"], g["x"])
+    assert (np.abs(p - g["fp64_all"]) / g["fp64_all"]).max() < 1e-6
+    p = gpupot(g["m"], g["x"], istart=int(g["istart"]), ni=int(g["ni"]))
+    assert (np.abs(p - g["fp64_sub"]) / g["fp64_sub"]).max() < 1e-6
+
+
+def test_gpupot_coincident_and_large(lib):
+    c = ics.plummer(20000, seed=3, masses="kroupa")
+    m, x = c.m.copy(), c.x.copy()
+    x[10] = x[11]                      # coincident pair: skipped both ways
+    p = gpupot(m, x)
+    samp = np.arange(0, 20000, 97)
+    o = np.array([O.pot_fp64(m, x, int(i) + 1, 1)[0] for i in samp])
+    assert (np.abs(p[samp] - o) / o).max() < 1e-6
+    assert np.isfinite(p[10]) and np.isfinite(p[11])
