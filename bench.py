@@ -1,0 +1,405 @@
+"""Benchmark of the regular-force hot path (gpunb_send_ + gpunb_regf_).
+
+Workload (default): Plummer N = 65536 in Henon units, Kroupa masses, RS for a
+mean of 100 neighbours, nbmax 512.  One step = the five regular blocks of a
+block-time-step hierarchy, ni in {1, 32, 1024, 16384, 65536}; each block is a
+full j-set upload (send) plus one regf call, as the integrator does it
+(src/Main/intgrt.F:912-944).  Metric: pairs (ni * N summed over the blocks)
+per second, in Gpairs/s.
+
+  value  device-resident inputs (j- and i-arrays already in HBM), timed with
+         CUDA events on the stream the library launches on;
+  e2e    the same step through the C ABI with host arrays (gpunb_send_,
+         gpunb_regf_), host<->device copies included, wall clock;
+  fp64   the plain FP64 kernel on the same step (the metric's "vs FP64").
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+BLOCKS = [1, 32, 1024, 16384, 65536]
+N = 65536
+NB_TARGET = 100.0
+NNBMAX = 512
+LMAX = NNBMAX + 1
+FLOPS_PER_PAIR = 60          # the reference's convention (gpunb.velocity.cu:894)
+METRIC = "regular force+jerk+NB Gpairs/s on 1 GB300: split-FP32 vs FP64 at rel.err<=1e-6"
+WORKLOAD = "plummer65536_kroupa_blocks_1_32_1024_16384_65536"
+
+
+def make_inputs(seed: int = 2):
+    from nbody6ppgpu_gb300 import ics
+    c = ics.plummer(N, seed=seed, masses="kroupa", nb_target=NB_TARGET)
+    acts = {ni: ics.active_set(N, ni, seed=ni) for ni in BLOCKS}
+    return c, acts
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path("/tmp") / f"bench_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        self.path.unlink(missing_ok=True)
+        load = [s for s in sm if smax and s > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+def gpu_info():
+    import torch
+    p = torch.cuda.get_device_properties(0)
+    return p.name, p.multi_processor_count
+
+
+def fp32_peak_tflops(n_sm: int, mhz: float) -> float:
+    # 128 FP32 lanes per SM, 2 flops per FMA
+    return n_sm * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def read_traffic():
+    """DRAM bytes per launch of the pair kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "regf_ds_kernel_plummer65536.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+# --------------------------------------------------------------------------
+def cpu_baseline(c, acts, budget_s: float = 10.0):
+    """The portable FP32 restatement of the reference CPU path (OpenMP, all
+    host cores) on whole steps of the same workload, as many as fit in
+    about budget_s (at least one)."""
+    from oracle import oracle as O
+    port = O.Port()
+    h2 = c.h2()
+    pairs = 0
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        for ni in BLOCKS:
+            a = acts[ni]
+            port.send(c.m, c.x, c.v)
+            port.regf(h2[a], c.dtr[a], c.x[a], c.v[a], LMAX, NNBMAX)
+            pairs += ni * N
+        steps += 1
+        if time.perf_counter() - t0 > budget_s or steps >= 20:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": pairs / dt / 1e9, "unit": "Gpairs/s", "cores": O.num_threads(),
+            "kind": "port",
+            "sample": f"{steps} full step(s) of the workload ({pairs:.3e} pairs) with the FP32 "
+                      f"restatement of src/Main/reg.avx.cpp (x86 AVX source does not build on "
+                      f"this aarch64 host)"}, pairs / dt
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the reference's CPU path (portable restatement) timed
+    on the host cores; each step is one full step of the workload."""
+    if rank != 0:
+        return 0
+    c, acts = make_inputs()
+    from oracle import oracle as O
+    port = O.Port()
+    h2 = c.h2()
+
+    def step():
+        for ni in BLOCKS:
+            a = acts[ni]
+            port.send(c.m, c.x, c.v)
+            port.regf(h2[a], c.dtr[a], c.x[a], c.v[a], LMAX, NNBMAX)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    pairs = N * sum(BLOCKS) * args.steps
+    v = pairs / dt / 1e9
+    line = {"metric": METRIC, "value": v, "unit": "Gpairs/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Plummer/Kroupa)",
+            "config": {"workload": WORKLOAD, "N": N, "blocks": BLOCKS, "nnbmax": NNBMAX,
+                       "host_threads": O.num_threads()},
+            "cpu_baseline": {"value": v, "unit": "Gpairs/s", "cores": O.num_threads(),
+                             "kind": "port",
+                             "sample": "every step = the full workload step on the host cores "
+                                       "(FP32 restatement of src/Main/reg.avx.cpp; the x86 AVX "
+                                       "source does not build on the aarch64 host)"},
+            "e2e": {"value": v, "unit": "Gpairs/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from nbody6ppgpu_gb300.gpunb import GpuNb, load
+    lib = load()
+    c, acts = make_inputs()
+    h2 = c.h2()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def T(a, dt=torch.float64):
+        return torch.as_tensor(np.ascontiguousarray(a)).to(dev, dtype=dt)
+
+    jm, jx, jv = T(c.m), T(c.x), T(c.v)
+    blk = {}
+    for ni in BLOCKS:
+        a = acts[ni]
+        blk[ni] = dict(h2=T(h2[a]), dtr=T(c.dtr[a]), x=T(c.x[a]), v=T(c.v[a]),
+                       acc=torch.empty((ni, 3), dtype=torch.float64, device=dev),
+                       jrk=torch.empty((ni, 3), dtype=torch.float64, device=dev),
+                       pot=torch.empty(ni, dtype=torch.float64, device=dev),
+                       nnb=torch.empty(ni, dtype=torch.int32, device=dev),
+                       off=torch.empty(ni + 1, dtype=torch.int32, device=dev),
+                       lst=torch.empty(ni * NNBMAX, dtype=torch.int32, device=dev))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > L2 (126 MB)
+
+    nb = GpuNb(N)
+
+    def dev_step():
+        for ni in BLOCKS:
+            b = blk[ni]
+            rc = lib.gpunb_send_device(N, jm.data_ptr(), jx.data_ptr(), jv.data_ptr(), sp)
+            assert rc == 0, rc
+            rc = lib.gpunb_regf_device(ni, b["h2"].data_ptr(), b["dtr"].data_ptr(),
+                                       b["x"].data_ptr(), b["v"].data_ptr(),
+                                       b["acc"].data_ptr(), b["jrk"].data_ptr(),
+                                       b["pot"].data_ptr(), b["nnb"].data_ptr(),
+                                       b["off"].data_ptr(), b["lst"].data_ptr(),
+                                       ni * NNBMAX, NNBMAX, 0, sp)
+            assert rc == 0, rc
+
+    def timed_steps(k, precision):
+        nb.set_precision(precision)
+        for _ in range(args.warmup):
+            dev_step()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        lib.gpunb_set_timing(1)
+        evs = []
+        for _ in range(k):
+            flush.zero_()                      # L2 flush between steps (untimed)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dev_step()
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        kt = nb.kernel_times(max_n=64 * k + 64)
+        lib.gpunb_set_timing(0)
+        if dist:
+            dist.barrier()
+        ms = [a.elapsed_time(b) for a, b in evs]
+        return ms, kt
+
+    # ---- split-precision product path, device-resident -------------------
+    clocks = Clocks(local)
+    clocks.start()
+    t_wall = time.perf_counter()
+    ms, kt = timed_steps(args.steps, "split")
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    step_ms = float(sum(ms) / len(ms))
+    if dist:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    pairs_per_step = N * sum(BLOCKS)
+    value = ws * pairs_per_step / (step_ms * 1e-3) / 1e9
+    # pair-kernel launches of the dominant block (ni = N), in launch order
+    kt = np.asarray(kt).reshape(args.steps, len(BLOCKS))
+    big = kt[:, BLOCKS.index(65536)]
+    k_ms = float(np.mean(big))
+    pairs_big = 65536 * N
+    achieved_tflops = pairs_big * FLOPS_PER_PAIR / (k_ms * 1e-3) / 1e12
+    name, n_sm = gpu_info()
+    peak_mhz = clk.get("sm_max_mhz") or 2070.0
+    peak = fp32_peak_tflops(n_sm, peak_mhz)
+    load_mhz = clk.get("sm_mhz") or peak_mhz
+
+    # ---- accuracy of the split kernel against the FP64 kernel ------------
+    nb.set_precision("split")
+    dev_step()
+    torch.cuda.synchronize()
+    res_split = {ni: (blk[ni]["acc"].cpu().numpy().copy(), blk[ni]["jrk"].cpu().numpy().copy(),
+                      blk[ni]["pot"].cpu().numpy().copy()) for ni in (1024, 16384)}
+    fp64_ms, fp64_kt = timed_steps(max(1, args.fp64_steps), "fp64")
+    fp64_value = ws * pairs_per_step / (float(np.mean(fp64_ms)) * 1e-3) / 1e9
+    errs = {}
+    for ni in (1024, 16384):
+        a64 = blk[ni]["acc"].cpu().numpy(); j64 = blk[ni]["jrk"].cpu().numpy()
+        p64 = blk[ni]["pot"].cpu().numpy()
+        a, j, p = res_split[ni]
+        ea = np.linalg.norm(a - a64, axis=1) / np.linalg.norm(a64, axis=1)
+        ej = np.linalg.norm(j - j64, axis=1) / np.linalg.norm(j64, axis=1)
+        ep = np.abs(p - p64) / np.abs(p64)
+        errs[str(ni)] = {"acc_p99": float(np.percentile(ea, 99)), "acc_max": float(ea.max()),
+                         "jrk_p99": float(np.percentile(ej, 99)), "jrk_max": float(ej.max()),
+                         "pot_max": float(ep.max())}
+    fp64_big = np.asarray(fp64_kt).reshape(-1, len(BLOCKS))[:, BLOCKS.index(65536)]
+
+    # ---- end to end through the C ABI with host arrays --------------------
+    nb.set_precision("split")
+    hin = {ni: (h2[acts[ni]].copy(), c.dtr[acts[ni]].copy(), c.x[acts[ni]].copy(),
+                c.v[acts[ni]].copy()) for ni in BLOCKS}
+    outs = {}
+
+    def host_step():
+        for ni in BLOCKS:
+            nb.send(c.m, c.x, c.v)
+            outs[ni] = nb.regf(*hin[ni], LMAX, NNBMAX, out=outs.get(ni))
+
+    for _ in range(args.warmup):
+        host_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = sum(56 * N + 64 * ni for ni in BLOCKS)
+    d2h = sum(60 * ni + 4 * int(np.maximum(outs[ni].list[:, 0], 0).sum()) for ni in BLOCKS)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu, _ = cpu_baseline(c, acts)
+
+    launches_per_block = 7   # pack, pair kernel, merge, 2x scan, gather, offsets
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Plummer sphere, Kroupa IMF, Henon units)",
+        "config": {"workload": WORKLOAD, "N": N, "blocks": BLOCKS, "nb_target": NB_TARGET,
+                   "nnbmax": NNBMAX, "precision": "split FP32 (double-single positions)",
+                   "l2": "flushed (256 MB write) between timed steps",
+                   "parallelism": f"replicas x{ws}"},
+        "fp64": {"value": fp64_value, "unit": "Gpairs/s",
+                 "kernel_ms_ni65536": float(np.mean(fp64_big)),
+                 "speedup_split_over_fp64_kernel": float(np.mean(fp64_big)) / k_ms},
+        "rel_err_vs_fp64_kernel": errs,
+        "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved_tflops / peak,
+                     "frac_at_load_clock": achieved_tflops / fp32_peak_tflops(n_sm, load_mhz),
+                     "traffic": read_traffic(),
+                     "kernel": "regf_ds_kernel (ni=65536 block)",
+                     "kernel_ms": k_ms, "flops_per_pair": FLOPS_PER_PAIR,
+                     "peak_source": f"nominal FP32: {n_sm} SMs x 128 lanes x 2 x {peak_mhz:.0f} MHz"
+                                    " (MEASURED_PEAKS.json has no FP32 entry)"},
+        "e2e": {"value": ws * pairs_per_step / e2e_s / 1e9, "unit": "Gpairs/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches_per_block * len(BLOCKS) * args.steps,
+        "clocks": clk,
+        "wall_s_timed_region": t_wall,
+        "device": name,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    nb.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -158,6 +158,7 @@ struct Engine {
   DevBuf iraw;     // h2[ni] | dtr[ni] | x[ni][3] | v[ni][3]
   DevBuf part, cnt, rows, rowlen, off, btot, dense, outblk, err;
   PinBuf hin, hout, hlist;
+  std::vector<size_t> host_offs;  // row offsets of the compacted list (host)
   // configuration
   int precision = 0;
   int force_variant = -1, force_splits = 0;
@@ -526,6 +527,15 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   if (ni < 4096) {
     size_t o2 = 0;
     for (int i = 0; i < ni; ++i) {
+      const int c = hnnb[i];
+      if (c > 0) o2 += c;
+    }
+    if (o2 != (size_t)std::max(total, 0)) {
+      fail(GPUNB_E_CUDA, "list length mismatch: device %d, host %zu", total, o2);
+      return;
+    }
+    o2 = 0;
+    for (int i = 0; i < ni; ++i) {
       int *row = list + (size_t)i * lmax;
       const int c = hnnb[i];
       row[0] = c;
@@ -535,13 +545,18 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
       }
     }
   } else {
-    // offsets first (sequential), then parallel copies
-    static thread_local std::vector<size_t> offs;
-    offs.resize(ni);
+    // offsets first (sequential), then parallel copies; the offsets live in
+    // an engine-owned buffer shared by all worker threads
+    g.host_offs.resize(ni);
+    size_t *offs = g.host_offs.data();
     size_t o2 = 0;
     for (int i = 0; i < ni; ++i) {
       offs[i] = o2;
       if (hnnb[i] > 0) o2 += hnnb[i];
+    }
+    if (o2 != (size_t)std::max(total, 0)) {
+      fail(GPUNB_E_CUDA, "list length mismatch: device %d, host %zu", total, o2);
+      return;
     }
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < ni; ++i) {
@@ -589,6 +604,12 @@ void gpunb_open_(int *nbmax, int *irank) {
       !g.hj.ensure(nmax * 7 * sizeof(double)))
     return;
   g.nj = 0;
+  // a new run starts from the default configuration
+  g.precision = 0;
+  g.force_variant = -1;
+  g.force_splits = 0;
+  g.timing = 0;
+  g.evused = 0;
   g.is_open = true;
   fprintf(stderr, "# Open GPU regular force - rank: %d; nbmax: %d\n", rank, g.nbodymax);
 }

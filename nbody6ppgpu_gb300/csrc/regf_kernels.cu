@@ -385,6 +385,9 @@ __global__ void __launch_bounds__(128) regf_fp64_kernel(const JSet js, const ISe
     xi0 = is.x[3 * i]; xi1 = is.x[3 * i + 1]; xi2 = is.x[3 * i + 2];
     vi0 = is.v[3 * i]; vi1 = is.v[3 * i + 1]; vi2 = is.v[3 * i + 2];
     h2 = is.h2[i]; dtr = is.dtr[i];
+    if (sy == 0 && (isnan(xi0) || isnan(xi1) || isnan(xi2) || isnan(vi0) || isnan(vi1) ||
+                    isnan(vi2) || isnan(h2) || isnan(dtr)))
+      raise_error(out.err, GPUNB_E_NAN);
   }
   double ax = 0, ay = 0, az = 0, jx = 0, jy = 0, jz = 0, po = 0;
   for (int t = t0; t < t1; ++t) {
