@@ -227,8 +227,11 @@ def main():
     c, acts = make_inputs()
     h2 = c.h2()
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the library and the timing events share it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
+    assert sp != 0
 
     def T(a, dt=torch.float64):
         return torch.as_tensor(np.ascontiguousarray(a)).to(dev, dtype=dt)

@@ -157,6 +157,10 @@ struct Engine {
   // i-set and work buffers
   DevBuf iraw;     // h2[ni] | dtr[ni] | x[ni][3] | v[ni][3]
   DevBuf part, cnt, rows, rowlen, off, btot, dense, outblk, err;
+  // spatial ordering: j permutation (tile slot -> sent index), i permutation,
+  // bounding box of the j-set, sort scratch
+  DevBuf jperm, iperm, bbox, okeys, okeys_alt, ovals_alt, otemp;
+  DevBuf queue;    // work-item counter of the persistent pair kernel
   PinBuf hin, hout, hlist;
   std::vector<size_t> host_offs;  // row offsets of the compacted list (host)
   // configuration
@@ -203,7 +207,9 @@ static bool devinit(int irank) {
   CUDA_OR(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking), false);
   CUDA_OR(cudaEventCreate(&g.ek0), false);
   CUDA_OR(cudaEventCreate(&g.ek1), false);
-  if (!g.err.ensure(sizeof(int))) return false;
+  if (!g.err.ensure(sizeof(int)) || !g.bbox.ensure(8 * sizeof(int)) ||
+      !g.queue.ensure(sizeof(int)))
+    return false;
   char host[150] = {0};
   gethostname(host, sizeof(host) - 1);
   fprintf(stderr, "# GPU initialization - rank: %d; HOST %s; NGPU 1; device: %d %s\n", irank,
@@ -226,14 +232,47 @@ static bool check_device_error(int code_from_device) {
 
 // ---------------------------------------------------------------------------
 // j-set upload: FP64 arrays on the device + split-precision tiles
+// Morton ordering scratch: keys, alternate keys/values and the sort's temp.
+static bool ensure_order_scratch(int n) {
+  const size_t nn = (size_t)std::max(n, 1);
+  return g.okeys.ensure(nn * sizeof(unsigned long long)) &&
+         g.okeys_alt.ensure(nn * sizeof(unsigned long long)) &&
+         g.ovals_alt.ensure(nn * sizeof(int)) && g.otemp.ensure(order_temp_bytes((int)nn));
+}
+
 static int send_common(int nj, cudaStream_t st) {
   const int ntile = (nj + JT - 1) / JT;
-  if (!g.jtiles.ensure((size_t)std::max(ntile, 1) * TILE_BYTES)) return GPUNB_E_ALLOC;
+  if (!g.jtiles.ensure((size_t)std::max(ntile, 1) * TILE_BYTES) ||
+      !g.jperm.ensure((size_t)std::max(nj, 1) * sizeof(int)) || !ensure_order_scratch(nj))
+    return GPUNB_E_ALLOC;
   double *m = g.jraw.as<double>();
-  CUDA_OR(launch_pack_jtiles(m, m + nj, m + 4 * (size_t)nj, nj, g.jtiles.as<float>(), ntile,
-                             g.err.as<int>(), st),
+  const double *x = m + nj;
+  // spatial order of the j-set: bounding box, Morton keys, stable sort
+  CUDA_OR(launch_bbox(x, nj, g.bbox.as<int>(), st), GPUNB_E_CUDA);
+  CUDA_OR(launch_order(x, nj, g.bbox.as<int>(), g.okeys.as<unsigned long long>(),
+                       g.okeys_alt.as<unsigned long long>(), g.ovals_alt.as<int>(),
+                       g.jperm.as<int>(), g.otemp.p, g.otemp.bytes, st),
+          GPUNB_E_CUDA);
+  CUDA_OR(launch_pack_jtiles(m, x, m + 4 * (size_t)nj, nj, g.jperm.as<int>(),
+                             g.jtiles.as<float>(), ntile, g.err.as<int>(), st),
           GPUNB_E_CUDA);
   g.nj = nj;
+  return GPUNB_OK;
+}
+
+// Morton order of an active block (within the j-set's bounding box); blocks
+// too small to gain from it keep the caller's order (perm = null).
+constexpr int kOrderMinNi = 256;
+static int order_iset(ISet &is, cudaStream_t st) {
+  is.perm = nullptr;
+  if (is.ni < kOrderMinNi || g.nj <= 0) return GPUNB_OK;
+  if (!g.iperm.ensure((size_t)is.ni * sizeof(int)) || !ensure_order_scratch(is.ni))
+    return GPUNB_E_ALLOC;
+  CUDA_OR(launch_order(is.x, is.ni, g.bbox.as<int>(), g.okeys.as<unsigned long long>(),
+                       g.okeys_alt.as<unsigned long long>(), g.ovals_alt.as<int>(),
+                       g.iperm.as<int>(), g.otemp.p, g.otemp.bytes, st),
+          GPUNB_E_CUDA);
+  is.perm = g.iperm.as<int>();
   return GPUNB_OK;
 }
 
@@ -244,6 +283,7 @@ static JSet jset() {
   js.m64 = m;
   js.x64 = m + g.nj;
   js.v64 = m + 4 * (size_t)g.nj;
+  js.perm = g.jperm.as<int>();
   js.nj = g.nj;
   js.ntile = (g.nj + JT - 1) / JT;
   js.ntile64 = (g.nj + JT64 - 1) / JT64;
@@ -263,20 +303,23 @@ static long long tune_key(int nj, int ni, int mflag, int prec) {
   return ((long long)bucket(nj) << 24) | ((long long)bucket(ni) << 8) | (mflag << 1) | prec;
 }
 
-static void heuristic_plan(int ni, int ntile, bool mflag, int &variant, int &splits) {
-  if (ni >= 16384) variant = 0;
-  else if (ni >= 2048) variant = 1;
-  else if (ni >= 256) variant = 3;
-  else variant = 2;
+// j-splits for a persistent launch: about 8 work items per resident block
+// for load balance, each item at least 4 tiles long.
+static int plan_splits(int variant, int ni, int ntile, bool mflag) {
   const VariantDesc d = regf_variant(variant);
   const int gx = (ni + d.itile() - 1) / d.itile();
   const int bps = regf_ds_blocks_per_sm(variant, mflag);
-  const long long want = 2ll * g.n_sm * bps;  // two waves of resident blocks
+  const long long want = 8ll * g.n_sm * bps;
   long long s = (want + gx - 1) / gx;
-  const int smax = std::max(1, ntile);
+  const int smax = std::max(1, ntile / 4);
   if (s > smax) s = smax;
   if (s < 1) s = 1;
-  splits = (int)s;
+  return (int)s;
+}
+
+static void heuristic_plan(int ni, int ntile, bool mflag, int &variant, int &splits) {
+  variant = (ni >= 256) ? 3 : 2;
+  splits = plan_splits(variant, ni, ntile, mflag);
 }
 
 static void fp64_plan(int ni, int ntile64, int &gx, int &splits) {
@@ -342,7 +385,11 @@ static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, in
   if (g.precision == 1) {
     CUDA_OR(launch_regf_fp64(mflag, gx, S, js, is, out, st), GPUNB_E_CUDA);
   } else {
-    CUDA_OR(launch_regf_ds(variant, mflag, gx, S, js, is, out, st), GPUNB_E_CUDA);
+    const long long items = (long long)gx * S;
+    const long long resident = (long long)g.n_sm * regf_ds_blocks_per_sm(variant, mflag);
+    const int grid = (int)std::max(1ll, std::min(items, resident));
+    CUDA_OR(launch_regf_ds(variant, mflag, gx, S, grid, g.queue.as<int>(), js, is, out, st),
+            GPUNB_E_CUDA);
   }
   if (timed || pooled) CUDA_OR(cudaEventRecord(e1, st), GPUNB_E_CUDA);
   g.last_variant = g.precision == 1 ? -1 : variant;
@@ -392,18 +439,13 @@ static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out
   float best = 1e30f;
   cudaStream_t st = g.stream;
   for (int v = 0; v < regf_num_variants(); ++v) {
-    int hv, hs;
-    const int saved = g.force_variant;
-    g.force_variant = -1;
-    heuristic_plan(ni, js.ntile, mflag, hv, hs);
-    g.force_variant = saved;
-    const VariantDesc d = regf_variant(v);
-    const int gx = (ni + d.itile() - 1) / d.itile();
-    const int bps = regf_ds_blocks_per_sm(v, mflag);
-    const long long base = std::max(1ll, (2ll * g.n_sm * bps + gx - 1) / gx);
+    const long long base = plan_splits(v, ni, js.ntile, mflag);
     const long long cands[5] = {base / 4, base / 2, base, base * 2, base * 4};
+    int last_s = -1;
     for (long long sc : cands) {
       int s = (int)std::max(1ll, std::min<long long>(sc, std::max(1, js.ntile)));
+      if (s == last_s) continue;
+      last_s = s;
       float tot = 0.f;
       const int reps = 3;
       bool ok = true;
@@ -468,6 +510,8 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   is.x = din + 2 * (size_t)ni;
   is.v = din + 5 * (size_t)ni;
   is.ni = ni;
+  is.perm = nullptr;
+  if (g.precision == 0 && order_iset(is, st) != GPUNB_OK) return;
 
   int variant, S;
   if (g.autotune_on && g.precision == 0 && g.force_variant < 0 &&
@@ -625,6 +669,8 @@ void gpunb_close_(void) {
   g.iraw.release(); g.part.release(); g.cnt.release(); g.rows.release();
   g.rowlen.release(); g.off.release(); g.btot.release(); g.dense.release();
   g.outblk.release(); g.hin.release(); g.hout.release(); g.hlist.release();
+  g.jperm.release(); g.iperm.release(); g.okeys.release(); g.okeys_alt.release();
+  g.ovals_alt.release(); g.otemp.release();
   g.nbodymax = 0;
   g.nj = 0;
   g.is_open = false;
@@ -813,6 +859,7 @@ int gpunb_autotune(int ni, int m_flag, int *splits, float *ms) {
   ISet is;
   is.h2 = din; is.dtr = din + ni; is.x = din + 2 * (size_t)ni; is.v = din + 5 * (size_t)ni;
   is.ni = ni;
+  if (order_iset(is, g.stream) != GPUNB_OK) return -1;
   const int saved = g.precision;
   g.precision = 0;
   const int v = autotune_with(is, 1024, m_flag != 0, splits, ms);
@@ -883,6 +930,8 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
   cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
   ISet is;
   is.h2 = h2; is.dtr = dtr; is.x = xi; is.v = vi; is.ni = ni;
+  is.perm = nullptr;
+  if (g.precision == 0 && order_iset(is, st) != GPUNB_OK) return GPUNB_E_ALLOC;
   const bool mflag = m_flag != 0;
   int variant, S;
   choose_plan(ni, mflag, variant, S);

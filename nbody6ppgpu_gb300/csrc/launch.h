@@ -18,10 +18,11 @@ int regf_num_variants();
 VariantDesc regf_variant(int v);
 size_t regf_ds_smem(int v);
 int regf_ds_blocks_per_sm(int v, bool mflag);
-cudaError_t launch_pack_jtiles(const double *m, const double *x, const double *v, int nj,
+cudaError_t launch_pack_jtiles(const double *m, const double *x, const double *v, int nj, const int *perm,
                                float *tiles, int ntile, int *err, cudaStream_t st);
-cudaError_t launch_regf_ds(int v, bool mflag, int gx, int S, const JSet &js, const ISet &is,
-                           const RegfOut &out, cudaStream_t st);
+// persistent launch: `grid` blocks drain n_itiles * S work items from `queue`
+cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int *queue,
+                           const JSet &js, const ISet &is, const RegfOut &out, cudaStream_t st);
 cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const ISet &is,
                              const RegfOut &out, cudaStream_t st);
 constexpr int FP64_THREADS = 128;
@@ -34,6 +35,13 @@ cudaError_t launch_list_scan(const int *rowlen, int ni, int *off, int *btot, cud
 cudaError_t launch_list_gather(int *rows, int cap, const int *rowlen, const int *off,
                                const int *btot, int ni, int *dense, cudaStream_t st);
 cudaError_t launch_list_finalize_offsets(int *off, const int *btot, int ni, cudaStream_t st);
+
+// spatial (Morton) ordering
+size_t order_temp_bytes(int n);
+cudaError_t launch_bbox(const double *x, int n, int *bb, cudaStream_t st);
+cudaError_t launch_order(const double *x, int n, const int *bb, unsigned long long *keys,
+                         unsigned long long *keys_alt, int *vals_alt, int *perm, void *temp,
+                         size_t temp_bytes, cudaStream_t st);
 
 // potential
 constexpr int POT_JT = 128;

@@ -1,0 +1,118 @@
+// Spatial ordering of bodies along a Morton (Z-order) curve.
+//
+// No reference counterpart: the reference packs j in the caller's order and
+// runs i in the caller's order (gpunb.velocity.cu:716-727,757-762).  Ordering
+// both sets spatially makes the neighbour-candidate branch of the pair kernel
+// coherent: the i-particles of one warp are close to each other, so the j
+// bodies that can be their neighbours arrive in the same few tiles and the
+// warp enters the branch rarely and with many lanes active.  Results do not
+// depend on the order beyond FP32 summation order; the order itself is a pure
+// function of the positions (deterministic bounding box, stable radix sort).
+#include <algorithm>
+#include <cub/device/device_radix_sort.cuh>
+
+#include "common.cuh"
+#include "launch.h"
+
+namespace gpunb {
+
+// order-preserving float <-> int mapping for deterministic atomic min/max
+__device__ __forceinline__ int f2ord(float f) {
+  const int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__global__ void bbox_init_kernel(int *bb) {
+  if (threadIdx.x < 3) bb[threadIdx.x] = f2ord(INFINITY);
+  else if (threadIdx.x < 6) bb[threadIdx.x] = f2ord(-INFINITY);
+}
+
+// bb[0..2] = min, bb[3..5] = max of the FP32-rounded coordinates
+__global__ void bbox_kernel(const double *__restrict__ x, int n, int *bb) {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float v = (float)x[3 * i + c];
+      lo[c] = fminf(lo[c], v);
+      hi[c] = fmaxf(hi[c], v);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+      hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      atomicMin(bb + c, f2ord(lo[c]));
+      atomicMax(bb + 3 + c, f2ord(hi[c]));
+    }
+  }
+}
+
+// spread the low 16 bits of v to every third bit
+__device__ __forceinline__ unsigned long long spread3(unsigned int v) {
+  unsigned long long x = v & 0xffffu;
+  x = (x | (x << 32)) & 0x001f00000000ffffull;
+  x = (x | (x << 16)) & 0x001f0000ff0000ffull;
+  x = (x | (x << 8)) & 0x100f00f00f00f00full;
+  x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+  x = (x | (x << 2)) & 0x1249249249249249ull;
+  return x;
+}
+
+// 48-bit Morton key (16 bits per axis inside the bounding box) and identity
+// values for the sort.
+__global__ void morton_kernel(const double *__restrict__ x, int n, const int *__restrict__ bb,
+                              unsigned long long *__restrict__ key, int *__restrict__ val) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned int q[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float lo = ord2f(bb[c]), hi = ord2f(bb[3 + c]);
+    const float span = hi - lo;
+    const float s = span > 0.f ? 65535.0f / span : 0.f;
+    float u = ((float)x[3 * i + c] - lo) * s;
+    u = fminf(fmaxf(u, 0.f), 65535.f);
+    q[c] = (unsigned int)u;
+  }
+  key[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+  val[i] = i;
+}
+
+size_t order_temp_bytes(int n) {
+  size_t tb = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tb, (const unsigned long long *)nullptr,
+                                  (unsigned long long *)nullptr, (const int *)nullptr,
+                                  (int *)nullptr, n, 0, 48);
+  return tb;
+}
+
+cudaError_t launch_bbox(const double *x, int n, int *bb, cudaStream_t st) {
+  bbox_init_kernel<<<1, 32, 0, st>>>(bb);
+  if (n > 0) {
+    const int blocks = std::min(1024, (n + 255) / 256);
+    bbox_kernel<<<blocks, 256, 0, st>>>(x, n, bb);
+  }
+  return cudaGetLastError();
+}
+
+// perm[0..n) = indices of x sorted by Morton key within bounding box bb.
+cudaError_t launch_order(const double *x, int n, const int *bb, unsigned long long *keys,
+                         unsigned long long *keys_alt, int *vals_alt, int *perm, void *temp,
+                         size_t temp_bytes, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  morton_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, n, bb, keys, vals_alt);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  size_t tb = temp_bytes;
+  return cub::DeviceRadixSort::SortPairs(temp, tb, keys, keys_alt, vals_alt, perm, n, 0, 48, st);
+}
+
+}  // namespace gpunb

@@ -22,15 +22,18 @@ namespace gpunb {
 // j packing: FP64 (as sent) -> split-precision SoA tiles + tile metadata.
 // One block of JT threads per tile.  Replaces the host-side Jparticle packing
 // of gpunb.velocity.cu:716-727 (which also drops positions to plain FP32).
+// Tile slot p holds body perm[p] (identity when perm is null).
 __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restrict__ m,
                                                          const double *__restrict__ x,
                                                          const double *__restrict__ v, int nj,
+                                                         const int *__restrict__ perm,
                                                          float *__restrict__ tiles, int *err) {
-  const int t = blockIdx.x, l = threadIdx.x, j = t * JT + l;
+  const int t = blockIdx.x, l = threadIdx.x, p = t * JT + l;
   float *T = tiles + (size_t)t * TILE_FLOATS;
   double vabs = 0.0, mj = 0.0;
   int real = 0;
-  if (j < nj) {
+  if (p < nj) {
+    const int j = perm ? perm[p] : p;
     const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
     const double v0 = v[3 * j], v1 = v[3 * j + 1], v2 = v[3 * j + 2];
     mj = m[j];
@@ -136,12 +139,23 @@ __device__ __forceinline__ void load_istate(IState &I, const ISet &is, int i, bo
   I.i = valid ? i : -1;
 }
 
+// Exact FP64 decision for a pair whose FP32 criterion value fell inside the
+// error band (very rare): kept out of line so that the common path carries
+// no call frame.
+template <bool MFLAG>
+__device__ __noinline__ bool decide_pair_fp64(const ISet &is, int i, const JSet &js, int jg) {
+  return nb_test_fp64(is, i, js, jg, MFLAG);
+}
+
 // Decide one candidate pair (rare path).  FP32 decision, FP64 re-test when
 // the FP32 value lies inside a conservative error band around the criterion.
+// The band bounds the FP32 rounding of the coordinate and velocity
+// differences, of h2 and of the products by 2^-14 of the magnitudes involved
+// (|dv| bounded by its L1 norm).
 template <bool MFLAG>
-__device__ __noinline__ bool decide_pair(const IState &I, const ISet &is, const JSet &js, int jg,
-                                         float dx, float dy, float dz, float dvx, float dvy,
-                                         float dvz, float r2, float mneg_half) {
+__device__ __forceinline__ bool decide_pair(const IState &I, const ISet &is, const JSet &js,
+                                            int jg, float dx, float dy, float dz, float dvx,
+                                            float dvy, float dvz, float r2, float mneg_half) {
   const float px = fmaf(I.dtrf, dvx, dx);
   const float py = fmaf(I.dtrf, dvy, dy);
   const float pz = fmaf(I.dtrf, dvz, dz);
@@ -149,12 +163,10 @@ __device__ __noinline__ bool decide_pair(const IState &I, const ISet &is, const 
   const float r2min = fminf(r2, r2p);
   const float crit = MFLAG ? (-2.0f * mneg_half) * I.h2f : I.h2f;
   bool in = r2min < crit;
-  // error band: FP32 rounding of positions' differences, velocities, h2 and
-  // the products, bounded generously by 2^-14 of the magnitudes involved
-  const float dv = sqrtf(fmaf(dvx, dvx, fmaf(dvy, dvy, dvz * dvz)));
-  const float w = 2.0f * fabsf(I.dtrf) * (I.va + dv);
+  const float dv1 = fabsf(dvx) + fabsf(dvy) + fabsf(dvz);
+  const float w = 2.0f * fabsf(I.dtrf) * (I.va + dv1);
   const float band = 0x1p-14f * (fabsf(crit) + r2 + w * w);
-  if (fabsf(r2min - crit) <= band) in = nb_test_fp64(is, I.i, js, jg, MFLAG);
+  if (fabsf(r2min - crit) <= band) in = decide_pair_fp64<MFLAG>(is, I.i, js, jg);
   return in;
 }
 
@@ -164,17 +176,29 @@ __device__ __forceinline__ void record_neighbour(const RegfOut &out, int i, int 
 }
 
 // ---------------------------------------------------------------------------
-// Split-precision pair kernel.
+// Split-precision pair kernel, persistent.
 //   IPT : i-particles per thread (independent chains)
 //   WI  : warps along i;  WJ : warps splitting each j tile (same i's)
-//   NSTAGE : j tiles in flight (bulk-async ring)
-// Grid: (ceil(ni / (32*IPT*WI)), S); split s covers tiles [s*ntile/S, (s+1)*ntile/S).
+// Work items are (i-tile it, j-split s) pairs, item = s * n_itiles + it, split
+// s covering tiles [s*ntile/S, (s+1)*ntile/S); a block takes items from the
+// device queue until it is empty.  The j tiles of an item stream through a
+// NSTAGE-deep shared-memory ring filled by bulk-async copies; the last warp
+// to finish with a stage refills it, so warps are never held at a block-wide
+// barrier inside an item.  Stage phases run on a per-block tile counter g
+// that continues across items.
 constexpr int NSTAGE = 4;
+
+struct RegfWork {
+  int *queue;      // item counter, zeroed before the launch
+  int n_itiles;
+  int S;
+};
 
 template <int IPT, int WI, int WJ, bool MFLAG>
 __global__ void __launch_bounds__(32 * WI * WJ)
-    regf_ds_kernel(const JSet js, const ISet is, const RegfOut out) {
+    regf_ds_kernel(const JSet js, const ISet is, const RegfOut out, const RegfWork w) {
   constexpr int NT = 32 * WI * WJ;
+  constexpr int NW = NT / 32;
   constexpr int ITILE = 32 * IPT * WI;
   constexpr int JW = JT / WJ;
   static_assert(JW % 2 == 0, "j per warp must be even");
@@ -182,167 +206,177 @@ __global__ void __launch_bounds__(32 * WI * WJ)
   float *ring = smem;                                   // NSTAGE * TILE_FLOATS
   float *ffs = smem + NSTAGE * TILE_FLOATS;             // [2][NQ][IPT][NT] float-float
   __shared__ __align__(8) uint64_t bar[NSTAGE];
-  __shared__ int s_abort;
+  __shared__ int s_rel[NSTAGE];                         // warps done with the stage
+  __shared__ int s_iss[NSTAGE];                         // copies issued into the stage
+  __shared__ int s_item, s_abort;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wi = warp % WI, wj = warp / WI;
-  const int ns = gridDim.y, sy = blockIdx.y;
-  const int t0 = (int)(((long long)js.ntile * sy) / ns);
-  const int t1 = (int)(((long long)js.ntile * (sy + 1)) / ns);
-  const int nt = t1 - t0;
+  const int n_items = w.n_itiles * w.S;
 
   if (tid == 0) {
-    for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+    for (int u = 0; u < NSTAGE; ++u) {
+      mbar_init(&bar[u], 1);
+      s_rel[u] = 0;
+      s_iss[u] = 0;
+    }
     fence_mbar_init();
     s_abort = 0;
   }
   __syncthreads();
-  if (tid == 0) {
-    for (int s = 0; s < NSTAGE && s < nt; ++s) {
-      mbar_expect_tx(&bar[s], TILE_BYTES);
-      bulk_g2s(ring + s * TILE_FLOATS, js.tiles + (size_t)(t0 + s) * TILE_FLOATS, TILE_BYTES,
-               &bar[s]);
-    }
-  }
 
-  IState I[IPT];
-  f2 q[IPT][NQ];
-#pragma unroll
-  for (int k = 0; k < IPT; ++k) {
-    const int i = blockIdx.x * ITILE + wi * 32 * IPT + k * 32 + lane;
-    load_istate(I[k], is, i, i < is.ni, out.err, sy == 0 && wj == 0);
-#pragma unroll
-    for (int c = 0; c < NQ; ++c) {
-      q[k][c] = make_float2(0.f, 0.f);
-      ffs[((0 * NQ + c) * IPT + k) * NT + tid] = 0.f;
-      ffs[((1 * NQ + c) * IPT + k) * NT + tid] = 0.f;
+  int g = 0;   // tiles consumed by this block so far (uniform)
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(w.queue, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= n_items || s_abort) break;
+    const int sy = item / w.n_itiles, it = item - sy * w.n_itiles;
+    const int t0 = (int)(((long long)js.ntile * sy) / w.S);
+    const int t1 = (int)(((long long)js.ntile * (sy + 1)) / w.S);
+    const int nt = t1 - t0;
+    if (tid == 0) {
+      for (int u = 0; u < NSTAGE && u < nt; ++u) {
+        const int st = (g + u) % NSTAGE;
+        s_iss[st]++;
+        mbar_expect_tx(&bar[st], TILE_BYTES);
+        bulk_g2s(ring + st * TILE_FLOATS, js.tiles + (size_t)(t0 + u) * TILE_FLOATS, TILE_BYTES,
+                 &bar[st]);
+      }
     }
-  }
 
-  int t = 0;
-  for (; t < nt; ++t) {
-    const int s = t % NSTAGE;
-    const uint32_t par = (uint32_t)(t / NSTAGE) & 1u;
-    if (!mbar_wait_bounded(&bar[s], par)) s_abort = 1;
-    const float *T = ring + s * TILE_FLOATS;
-    const float vmax = T[NFIELD * JT + 0];
-    const float smax = T[NFIELD * JT + 1];
-    float H[IPT];
+    IState I[IPT];
+    f2 q[IPT][NQ];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
-      const float base = I[k].dv * (I[k].va + vmax);
-      const float b = MFLAG ? fmaf(I[k].s, smax, base) : I[k].s + base;
-      H[k] = (I[k].s < 0.f) ? -1.0f : b * b;
+      const int slot = it * ITILE + wi * 32 * IPT + k * 32 + lane;
+      const bool valid = slot < is.ni;
+      const int i = valid ? (is.perm ? is.perm[slot] : slot) : -1;
+      load_istate(I[k], is, i, valid, out.err, sy == 0 && wj == 0);
+#pragma unroll
+      for (int c = 0; c < NQ; ++c) {
+        q[k][c] = make_float2(0.f, 0.f);
+        ffs[((0 * NQ + c) * IPT + k) * NT + tid] = 0.f;
+        ffs[((1 * NQ + c) * IPT + k) * NT + tid] = 0.f;
+      }
     }
-    const int jbeg = wj * JW;
-#pragma unroll 2
-    for (int jj = jbeg; jj < jbeg + JW; jj += 2) {
-      const f2 xh = *(const f2 *)(T + F_XH * JT + jj);
-      const f2 yh = *(const f2 *)(T + F_YH * JT + jj);
-      const f2 zh = *(const f2 *)(T + F_ZH * JT + jj);
-      const f2 xl = *(const f2 *)(T + F_XL * JT + jj);
-      const f2 yl = *(const f2 *)(T + F_YL * JT + jj);
-      const f2 zl = *(const f2 *)(T + F_ZL * JT + jj);
-      const f2 vx = *(const f2 *)(T + F_VX * JT + jj);
-      const f2 vy = *(const f2 *)(T + F_VY * JT + jj);
-      const f2 vz = *(const f2 *)(T + F_VZ * JT + jj);
-      const f2 mn = *(const f2 *)(T + F_MN * JT + jj);
-      f2 dx[IPT], dy[IPT], dz[IPT], dvx[IPT], dvy[IPT], dvz[IPT], r2[IPT], rv[IPT], z[IPT];
-      bool cand = false;
+
+    for (int t = 0; t < nt; ++t) {
+      const int st = (g + t) % NSTAGE;
+      const uint32_t par = (uint32_t)((g + t) / NSTAGE) & 1u;
+      if (!mbar_wait_bounded(&bar[st], par)) s_abort = 1;
+      if (*(volatile int *)&s_abort) break;
+      const float *T = ring + st * TILE_FLOATS;
+      const float vmax = T[NFIELD * JT + 0];
+      const float smax = T[NFIELD * JT + 1];
+      const int jbeg = wj * JW;
 #pragma unroll
       for (int k = 0; k < IPT; ++k) {
-        // double-single coordinate difference: (hi_j - hi_i) + (lo_j - lo_i)
-        dx[k] = add2(add2(xh, I[k].nxh), add2(xl, I[k].nxl));
-        dy[k] = add2(add2(yh, I[k].nyh), add2(yl, I[k].nyl));
-        dz[k] = add2(add2(zh, I[k].nzh), add2(zl, I[k].nzl));
-        dvx[k] = add2(vx, I[k].nvx);
-        dvy[k] = add2(vy, I[k].nvy);
-        dvz[k] = add2(vz, I[k].nvz);
-        r2[k] = fma2(dz[k], dz[k], fma2(dy[k], dy[k], mul2(dx[k], dx[k])));
-        rv[k] = fma2(dz[k], dvz[k], fma2(dy[k], dvy[k], mul2(dx[k], dvx[k])));
-        // rsqrt estimate + one Newton step, scaled: z = y0 (x y0^2 - 3) = -2/r
-        const f2 y0 = make_float2(rsqrtf(r2[k].x), rsqrtf(r2[k].y));
-        const f2 a = mul2(r2[k], y0);
-        z[k] = mul2(y0, fma2(a, y0, mk2(-3.0f)));
-        cand |= (r2[k].x < H[k]) | (r2[k].y < H[k]);
-      }
-      if (__any_sync(0xffffffffu, cand)) {
-        const int jg0 = (t0 + t) * JT + jj;
-#pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-          if (r2[k].x < H[k] && jg0 < js.nj) {   // padding bodies never qualify
-            if (decide_pair<MFLAG>(I[k], is, js, jg0, dx[k].x, dy[k].x, dz[k].x, dvx[k].x,
-                                   dvy[k].x, dvz[k].x, r2[k].x, mn.x)) {
-              record_neighbour(out, I[k].i, jg0);
-              z[k].x = 0.f;
+        const float base = I[k].dv * (I[k].va + vmax);
+        const float b = MFLAG ? fmaf(I[k].s, smax, base) : I[k].s + base;
+        const float H = (I[k].s < 0.f) ? -1.0f : b * b;
+#pragma unroll 2
+        for (int jj = jbeg; jj < jbeg + JW; jj += 2) {
+          const f2 xh = *(const f2 *)(T + F_XH * JT + jj);
+          const f2 yh = *(const f2 *)(T + F_YH * JT + jj);
+          const f2 zh = *(const f2 *)(T + F_ZH * JT + jj);
+          const f2 xl = *(const f2 *)(T + F_XL * JT + jj);
+          const f2 yl = *(const f2 *)(T + F_YL * JT + jj);
+          const f2 zl = *(const f2 *)(T + F_ZL * JT + jj);
+          const f2 vx = *(const f2 *)(T + F_VX * JT + jj);
+          const f2 vy = *(const f2 *)(T + F_VY * JT + jj);
+          const f2 vz = *(const f2 *)(T + F_VZ * JT + jj);
+          const f2 mn = *(const f2 *)(T + F_MN * JT + jj);
+          // double-single coordinate difference: (hi_j - hi_i) + (lo_j - lo_i)
+          const f2 dx = add2(add2(xh, I[k].nxh), add2(xl, I[k].nxl));
+          const f2 dy = add2(add2(yh, I[k].nyh), add2(yl, I[k].nyl));
+          const f2 dz = add2(add2(zh, I[k].nzh), add2(zl, I[k].nzl));
+          const f2 dvx = add2(vx, I[k].nvx);
+          const f2 dvy = add2(vy, I[k].nvy);
+          const f2 dvz = add2(vz, I[k].nvz);
+          const f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+          const f2 rv = fma2(dz, dvz, fma2(dy, dvy, mul2(dx, dvx)));
+          // rsqrt estimate + one Newton step, scaled: z = y0 (x y0^2 - 3) = -2/r
+          const f2 y0 = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+          f2 z = mul2(y0, fma2(mul2(r2, y0), y0, mk2(-3.0f)));
+          const bool c0 = r2.x < H, c1 = r2.y < H;
+          if (__any_sync(0xffffffffu, c0 | c1)) {
+            const int jg0 = (t0 + t) * JT + jj;
+            // slots >= nj are padding and never qualify; ids are reported in
+            // the caller's numbering (perm maps tile slot -> sent index)
+            if (c0 && jg0 < js.nj) {
+              const int jo = js.perm ? js.perm[jg0] : jg0;
+              if (decide_pair<MFLAG>(I[k], is, js, jo, dx.x, dy.x, dz.x, dvx.x, dvy.x, dvz.x,
+                                     r2.x, mn.x)) {
+                record_neighbour(out, I[k].i, jo);
+                z.x = 0.f;
+              }
+            }
+            if (c1 && jg0 + 1 < js.nj) {
+              const int jo = js.perm ? js.perm[jg0 + 1] : jg0 + 1;
+              if (decide_pair<MFLAG>(I[k], is, js, jo, dx.y, dy.y, dz.y, dvx.y, dvy.y, dvz.y,
+                                     r2.y, mn.y)) {
+                record_neighbour(out, I[k].i, jo);
+                z.y = 0.f;
+              }
             }
           }
-          if (r2[k].y < H[k] && jg0 + 1 < js.nj) {
-            if (decide_pair<MFLAG>(I[k], is, js, jg0 + 1, dx[k].y, dy[k].y, dz[k].y, dvx[k].y,
-                                   dvy[k].y, dvz[k].y, r2[k].y, mn.y)) {
-              record_neighbour(out, I[k].i, jg0 + 1);
-              z[k].y = 0.f;
-            }
+          const f2 mr = mul2(mn, z);            // m/r
+          const f2 z2 = mul2(z, z);             // 4/r^2
+          const f2 mr3 = mul2(mr, z2);          // 4 m/r^3
+          q[k][6] = add2(q[k][6], mr);
+          q[k][0] = fma2(mr3, dx, q[k][0]);
+          q[k][1] = fma2(mr3, dy, q[k][1]);
+          q[k][2] = fma2(mr3, dz, q[k][2]);
+          const f2 al = mul2(mul2(rv, z2), mk2(-0.75f));   // -3 (r.v)/r^2
+          q[k][3] = fma2(mr3, fma2(al, dx, dvx), q[k][3]);
+          q[k][4] = fma2(mr3, fma2(al, dy, dvy), q[k][4]);
+          q[k][5] = fma2(mr3, fma2(al, dz, dvz), q[k][5]);
+        }
+      }
+      // fold the tile's FP32 chunk sums into the float-float accumulators
+#pragma unroll
+      for (int k = 0; k < IPT; ++k) {
+#pragma unroll
+        for (int c = 0; c < NQ; ++c) {
+          float &hi = ffs[((0 * NQ + c) * IPT + k) * NT + tid];
+          float &lo = ffs[((1 * NQ + c) * IPT + k) * NT + tid];
+          float h = hi, l = lo;
+          ff_accum(h, l, __fadd_rn(q[k][c].x, q[k][c].y));
+          hi = h; lo = l;
+          q[k][c] = make_float2(0.f, 0.f);
+        }
+      }
+      // release the stage; the last warp out refills it with tile t + NSTAGE
+      __syncwarp();
+      if (lane == 0) {
+        __threadfence_block();
+        const int done = atomicAdd(&s_rel[st], 1);
+        if (done == NW - 1) {
+          s_rel[st] = 0;
+          if (t + NSTAGE < nt) {
+            s_iss[st]++;
+            mbar_expect_tx(&bar[st], TILE_BYTES);
+            bulk_g2s(ring + st * TILE_FLOATS, js.tiles + (size_t)(t0 + t + NSTAGE) * TILE_FLOATS,
+                     TILE_BYTES, &bar[st]);
           }
         }
       }
-#pragma unroll
-      for (int k = 0; k < IPT; ++k) {
-        const f2 mr = mul2(mn, z[k]);          // m/r
-        const f2 z2 = mul2(z[k], z[k]);        // 4/r^2
-        const f2 mr3 = mul2(mr, z2);           // 4 m/r^3
-        q[k][6] = add2(q[k][6], mr);
-        q[k][0] = fma2(mr3, dx[k], q[k][0]);
-        q[k][1] = fma2(mr3, dy[k], q[k][1]);
-        q[k][2] = fma2(mr3, dz[k], q[k][2]);
-        const f2 al = mul2(mul2(rv[k], z2), mk2(-0.75f));   // -3 (r.v)/r^2
-        q[k][3] = fma2(mr3, fma2(al, dx[k], dvx[k]), q[k][3]);
-        q[k][4] = fma2(mr3, fma2(al, dy[k], dvy[k]), q[k][4]);
-        q[k][5] = fma2(mr3, fma2(al, dz[k], dvz[k]), q[k][5]);
-      }
     }
-    // fold the tile's FP32 chunk sums into the float-float accumulators
-#pragma unroll
-    for (int k = 0; k < IPT; ++k) {
-#pragma unroll
-      for (int c = 0; c < NQ; ++c) {
-        float &hi = ffs[((0 * NQ + c) * IPT + k) * NT + tid];
-        float &lo = ffs[((1 * NQ + c) * IPT + k) * NT + tid];
-        float h = hi, l = lo;
-        ff_accum(h, l, __fadd_rn(q[k][c].x, q[k][c].y));
-        hi = h; lo = l;
-        q[k][c] = make_float2(0.f, 0.f);
-      }
-    }
+    g += nt;
     __syncthreads();
     if (s_abort) break;
-    if (tid == 0 && t + NSTAGE < nt) {
-      mbar_expect_tx(&bar[s], TILE_BYTES);
-      bulk_g2s(ring + s * TILE_FLOATS, js.tiles + (size_t)(t0 + t + NSTAGE) * TILE_FLOATS,
-               TILE_BYTES, &bar[s]);
-    }
-  }
-  if (s_abort) {
-    // let any copy still in flight land before the block exits
-    if (tid == 0) {
-      for (int u = t + 1; u < nt && u < t + NSTAGE; ++u)
-        mbar_wait_bounded(&bar[u % NSTAGE], (uint32_t)(u / NSTAGE) & 1u, 1u << 16);
-      raise_error(out.err, GPUNB_E_TIMEOUT);
-    }
-    return;
-  }
 
-  // fixed-order merge of the WJ j-subranges (warps wj > 0 into wj == 0)
-  if (WJ > 1) {
-    if (wj == 0) {
+    // fixed-order merge of the WJ j-subranges (warps wj > 0 into wj == 0)
+    if (WJ > 1 && wj == 0) {
 #pragma unroll
       for (int k = 0; k < IPT; ++k)
 #pragma unroll
         for (int c = 0; c < NQ; ++c) {
           float h = ffs[((0 * NQ + c) * IPT + k) * NT + tid];
           float l = ffs[((1 * NQ + c) * IPT + k) * NT + tid];
-          for (int w = 1; w < WJ; ++w) {
-            const int src = tid + w * 32 * WI;
+          for (int u = 1; u < WJ; ++u) {
+            const int src = tid + u * 32 * WI;
             ff_add(h, l, ffs[((0 * NQ + c) * IPT + k) * NT + src],
                    ffs[((1 * NQ + c) * IPT + k) * NT + src]);
           }
@@ -350,19 +384,26 @@ __global__ void __launch_bounds__(32 * WI * WJ)
           ffs[((1 * NQ + c) * IPT + k) * NT + tid] = l;
         }
     }
-  }
-  if (wj == 0) {
+    if (wj == 0) {
 #pragma unroll
-    for (int k = 0; k < IPT; ++k) {
-      const int i = I[k].i;
-      if (i < 0) continue;
+      for (int k = 0; k < IPT; ++k) {
+        const int i = I[k].i;
+        if (i < 0) continue;
 #pragma unroll
-      for (int c = 0; c < NQ; ++c) {
-        const double v = (double)ffs[((0 * NQ + c) * IPT + k) * NT + tid] +
-                         (double)ffs[((1 * NQ + c) * IPT + k) * NT + tid];
-        out.part[((size_t)sy * NQ + c) * out.ni_pad + i] = v;
+        for (int c = 0; c < NQ; ++c) {
+          const double v = (double)ffs[((0 * NQ + c) * IPT + k) * NT + tid] +
+                           (double)ffs[((1 * NQ + c) * IPT + k) * NT + tid];
+          out.part[((size_t)sy * NQ + c) * out.ni_pad + i] = v;
+        }
       }
     }
+    __syncthreads();   // ffs and s_item are reused by the next item
+  }
+  if (s_abort && tid == 0) {
+    // let copies still in flight land before the block exits
+    for (int u = 0; u < NSTAGE; ++u)
+      if (s_iss[u] > 0) mbar_wait_bounded(&bar[u], (uint32_t)(s_iss[u] - 1) & 1u, 1u << 16);
+    raise_error(out.err, GPUNB_E_TIMEOUT);
   }
 }
 
@@ -615,7 +656,7 @@ size_t regf_ds_smem(int v) {
   return (size_t)NSTAGE * TILE_BYTES + 2u * NQ * d.ipt * d.threads() * sizeof(float);
 }
 
-typedef void (*regf_fn)(JSet, ISet, RegfOut);
+typedef void (*regf_fn)(JSet, ISet, RegfOut, RegfWork);
 static regf_fn regf_kernel_ptr(int v, bool mflag) {
   switch (v) {
     case 0: return mflag ? regf_ds_kernel<2, 4, 1, true> : regf_ds_kernel<2, 4, 1, false>;
@@ -634,15 +675,15 @@ int regf_ds_blocks_per_sm(int v, bool mflag) {
   return n > 0 ? n : 1;
 }
 
-cudaError_t launch_pack_jtiles(const double *m, const double *x, const double *v, int nj,
+cudaError_t launch_pack_jtiles(const double *m, const double *x, const double *v, int nj, const int *perm,
                                float *tiles, int ntile, int *err, cudaStream_t st) {
   if (ntile <= 0) return cudaSuccess;
-  pack_jtiles_kernel<<<ntile, JT, 0, st>>>(m, x, v, nj, tiles, err);
+  pack_jtiles_kernel<<<ntile, JT, 0, st>>>(m, x, v, nj, perm, tiles, err);
   return cudaGetLastError();
 }
 
-cudaError_t launch_regf_ds(int v, bool mflag, int gx, int S, const JSet &js, const ISet &is,
-                           const RegfOut &out, cudaStream_t st) {
+cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int *queue,
+                           const JSet &js, const ISet &is, const RegfOut &out, cudaStream_t st) {
   const VariantDesc d = kVariants[v];
   regf_fn fn = regf_kernel_ptr(v, mflag);
   const size_t smem = regf_ds_smem(v);
@@ -650,7 +691,13 @@ cudaError_t launch_regf_ds(int v, bool mflag, int gx, int S, const JSet &js, con
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  fn<<<dim3(gx, S), d.threads(), smem, st>>>(js, is, out);
+  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  RegfWork w;
+  w.queue = queue;
+  w.n_itiles = n_itiles;
+  w.S = S;
+  fn<<<grid, d.threads(), smem, st>>>(js, is, out, w);
   return cudaGetLastError();
 }
 
@@ -692,18 +739,5 @@ cudaError_t launch_list_finalize_offsets(int *off, const int *btot, int ni, cuda
                                                                  list_scan_blocks(ni));
   return cudaGetLastError();
 }
-
-// ---------------------------------------------------------------------------
-// explicit instantiations exported to the host side
-template __global__ void regf_ds_kernel<2, 4, 1, false>(JSet, ISet, RegfOut);
-template __global__ void regf_ds_kernel<2, 4, 1, true>(JSet, ISet, RegfOut);
-template __global__ void regf_ds_kernel<2, 2, 2, false>(JSet, ISet, RegfOut);
-template __global__ void regf_ds_kernel<2, 2, 2, true>(JSet, ISet, RegfOut);
-template __global__ void regf_ds_kernel<1, 1, 8, false>(JSet, ISet, RegfOut);
-template __global__ void regf_ds_kernel<1, 1, 8, true>(JSet, ISet, RegfOut);
-template __global__ void regf_ds_kernel<1, 4, 1, false>(JSet, ISet, RegfOut);
-template __global__ void regf_ds_kernel<1, 4, 1, true>(JSet, ISet, RegfOut);
-template __global__ void regf_fp64_kernel<false>(JSet, ISet, RegfOut);
-template __global__ void regf_fp64_kernel<true>(JSet, ISet, RegfOut);
 
 }  // namespace gpunb

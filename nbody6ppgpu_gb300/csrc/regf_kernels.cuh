@@ -31,6 +31,7 @@ struct JSet {
   const double *m64;     // [nj]
   const double *x64;     // [nj][3]
   const double *v64;     // [nj][3]
+  const int *perm;       // tile slot -> index into the sent arrays (Morton order)
   int nj;
   int ntile;             // ceil(nj / JT)
   int ntile64;           // ceil(nj / JT64)
@@ -41,6 +42,7 @@ struct ISet {
   const double *dtr;     // [ni]
   const double *x;       // [ni][3]
   const double *v;       // [ni][3]
+  const int *perm;       // processing slot -> i index (Morton order), or null
   int ni;
 };
 
