@@ -122,6 +122,21 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
                       int *list_off, int *list, size_t list_cap, int nnbmax, int m_flag,
                       void *stream);
 
+/* Potential of gpupot_ for callers that cannot allocate device memory (no
+ * counterpart in the reference).  Meant for code that must not call
+ * cudaMalloc: an energy check issued from inside a CUDA-graph-captured step,
+ * or a host program whose own caching allocator already holds the free device
+ * memory.  All pointers are device memory (m[n], x[n][3], pot[ni]); work is
+ * queued on `stream` (a cudaStream_t).  The scratch is a fixed 4 MiB array in
+ * the library image, present on every GPU that loads the library; the call
+ * allocates nothing.  Limits: 1 <= n <= 65536, 1 <= istart, istart-1+ni <= n;
+ * anything else returns GPUNB_E_ARG without launching.  The first call on a
+ * device looks up the array's device address, so make it before any stream
+ * capture.  Calls share the scratch: calls that overlap on the GPU race, so
+ * serialise them on one stream.  Returns 0 or an error code. */
+int gpupot_device_noalloc(int istart, int ni, int n, const double *m, const double *x,
+                          double *pot, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
