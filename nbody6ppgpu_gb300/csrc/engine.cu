@@ -161,6 +161,7 @@ struct Engine {
   // bounding box of the j-set, sort scratch
   DevBuf jperm, iperm, bbox, okeys, okeys_alt, ovals_alt, otemp;
   DevBuf queue;    // work-item counter of the persistent pair kernel
+  DevBuf irec;     // FP32 i-records of the current active block
   PinBuf hin, hout, hlist;
   std::vector<size_t> host_offs;  // row offsets of the compacted list (host)
   // configuration
@@ -263,16 +264,23 @@ static int send_common(int nj, cudaStream_t st) {
 // Morton order of an active block (within the j-set's bounding box); blocks
 // too small to gain from it keep the caller's order (perm = null).
 constexpr int kOrderMinNi = 256;
+// Prepares an active block for the split-precision kernel: Morton order
+// (skipped for small blocks) and the FP32 i-records in that order.
 static int order_iset(ISet &is, cudaStream_t st) {
   is.perm = nullptr;
-  if (is.ni < kOrderMinNi || g.nj <= 0) return GPUNB_OK;
-  if (!g.iperm.ensure((size_t)is.ni * sizeof(int)) || !ensure_order_scratch(is.ni))
-    return GPUNB_E_ALLOC;
-  CUDA_OR(launch_order(is.x, is.ni, g.bbox.as<int>(), g.okeys.as<unsigned long long>(),
-                       g.okeys_alt.as<unsigned long long>(), g.ovals_alt.as<int>(),
-                       g.iperm.as<int>(), g.otemp.p, g.otemp.bytes, st),
-          GPUNB_E_CUDA);
-  is.perm = g.iperm.as<int>();
+  is.rec = nullptr;
+  if (is.ni >= kOrderMinNi && g.nj > 0) {
+    if (!g.iperm.ensure((size_t)is.ni * sizeof(int)) || !ensure_order_scratch(is.ni))
+      return GPUNB_E_ALLOC;
+    CUDA_OR(launch_order(is.x, is.ni, g.bbox.as<int>(), g.okeys.as<unsigned long long>(),
+                         g.okeys_alt.as<unsigned long long>(), g.ovals_alt.as<int>(),
+                         g.iperm.as<int>(), g.otemp.p, g.otemp.bytes, st),
+            GPUNB_E_CUDA);
+    is.perm = g.iperm.as<int>();
+  }
+  if (!g.irec.ensure((size_t)std::max(is.ni, 1) * 4 * sizeof(float4))) return GPUNB_E_ALLOC;
+  CUDA_OR(launch_regf_prep(is, g.irec.as<float4>(), g.err.as<int>(), st), GPUNB_E_CUDA);
+  is.rec = g.irec.as<float4>();
   return GPUNB_OK;
 }
 
@@ -303,22 +311,26 @@ static long long tune_key(int nj, int ni, int mflag, int prec) {
   return ((long long)bucket(nj) << 24) | ((long long)bucket(ni) << 8) | (mflag << 1) | prec;
 }
 
-// j-splits for a persistent launch: about 8 work items per resident block
-// for load balance, each item at least 4 tiles long.
+// j-splits for a persistent launch: about 32 work items per resident block,
+// so that the last round of items leaves little of the machine idle, with
+// at least 2 tiles per item.
 static int plan_splits(int variant, int ni, int ntile, bool mflag) {
   const VariantDesc d = regf_variant(variant);
   const int gx = (ni + d.itile() - 1) / d.itile();
   const int bps = regf_ds_blocks_per_sm(variant, mflag);
-  const long long want = 8ll * g.n_sm * bps;
+  const long long want = 32ll * g.n_sm * bps;
   long long s = (want + gx - 1) / gx;
-  const int smax = std::max(1, ntile / 4);
+  const int smax = std::max(1, ntile / 2);
   if (s > smax) s = smax;
   if (s < 1) s = 1;
   return (int)s;
 }
 
+// Shapes measured on GB300 (N = 65536 Plummer, all shapes and split counts):
+// 4 warps along i with 128-bit j loads for blocks of 512 and more, one warp
+// of 32 i-particles with the j tile split over 8 warps below.
 static void heuristic_plan(int ni, int ntile, bool mflag, int &variant, int &splits) {
-  variant = (ni >= 256) ? 3 : 2;
+  variant = (ni >= 512) ? 4 : 2;
   splits = plan_splits(variant, ni, ntile, mflag);
 }
 
@@ -511,6 +523,7 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   is.v = din + 5 * (size_t)ni;
   is.ni = ni;
   is.perm = nullptr;
+  is.rec = nullptr;
   if (g.precision == 0 && order_iset(is, st) != GPUNB_OK) return;
 
   int variant, S;
@@ -670,7 +683,7 @@ void gpunb_close_(void) {
   g.rowlen.release(); g.off.release(); g.btot.release(); g.dense.release();
   g.outblk.release(); g.hin.release(); g.hout.release(); g.hlist.release();
   g.jperm.release(); g.iperm.release(); g.okeys.release(); g.okeys_alt.release();
-  g.ovals_alt.release(); g.otemp.release();
+  g.ovals_alt.release(); g.otemp.release(); g.irec.release();
   g.nbodymax = 0;
   g.nj = 0;
   g.is_open = false;
@@ -931,6 +944,7 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
   ISet is;
   is.h2 = h2; is.dtr = dtr; is.x = xi; is.v = vi; is.ni = ni;
   is.perm = nullptr;
+  is.rec = nullptr;
   if (g.precision == 0 && order_iset(is, st) != GPUNB_OK) return GPUNB_E_ALLOC;
   const bool mflag = m_flag != 0;
   int variant, S;

@@ -10,6 +10,7 @@ namespace gpunb {
 
 struct VariantDesc {
   int ipt, wi, wj;                       // i per thread, warps along i, warps along j
+  int jv;                                // j read per shared-memory load (2 or 4)
   int threads() const { return 32 * wi * wj; }
   int itile() const { return 32 * ipt * wi; }
 };
@@ -29,6 +30,8 @@ constexpr int FP64_THREADS = 128;
 cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *cnt,
                               int nnbmax, double *acc, double *jrk, double *pot, int *nnb,
                               int *rowlen, cudaStream_t st);
+// FP32 i-records in processing order (NaN check of the i inputs included)
+cudaError_t launch_regf_prep(const ISet &is, float4 *rec, int *err, cudaStream_t st);
 // scan of rowlen -> off (+ block offsets in btot, grand total at btot[nblocks])
 int list_scan_blocks(int ni);
 cudaError_t launch_list_scan(const int *rowlen, int ni, int *off, int *btot, cudaStream_t st);

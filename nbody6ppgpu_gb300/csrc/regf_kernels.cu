@@ -114,29 +114,50 @@ struct IState {
   int i;
 };
 
-__device__ __forceinline__ void load_istate(IState &I, const ISet &is, int i, bool valid,
-                                            int *err, bool report) {
-  double x0 = 0, x1 = 0, x2 = 0, v0 = 0, v1 = 0, v2 = 0, h2 = -1.0, dtr = 0;
-  if (valid) {
-    x0 = is.x[3 * i]; x1 = is.x[3 * i + 1]; x2 = is.x[3 * i + 2];
-    v0 = is.v[3 * i]; v1 = is.v[3 * i + 1]; v2 = is.v[3 * i + 2];
-    h2 = is.h2[i]; dtr = is.dtr[i];
-    if (report && (isnan(x0) || isnan(x1) || isnan(x2) || isnan(v0) || isnan(v1) ||
-                   isnan(v2) || isnan(h2) || isnan(dtr)))
-      raise_error(err, GPUNB_E_NAN);
-  }
-  float h, l;
-  ds_split(x0, h, l); I.nxh = mk2(-h); I.nxl = mk2(-l);
-  ds_split(x1, h, l); I.nyh = mk2(-h); I.nyl = mk2(-l);
-  ds_split(x2, h, l); I.nzh = mk2(-h); I.nzl = mk2(-l);
-  I.nvx = mk2(-(float)v0); I.nvy = mk2(-(float)v1); I.nvz = mk2(-(float)v2);
+// i-record: the FP32 state of one i-particle, 64 bytes, written once per call
+// by regf_prep_kernel in processing-slot order:
+//   [0..5]  -(hi, lo) of x, y, z     [6..8]  -velocity
+//   [9]  filter radius sqrt(h2)(1 + 2^-12) (-1: no neighbour test)
+//   [10] |dtr|(1 + 2^-12)  [11] |v|(1 + 2^-12)  [12] h2  [13] dtr
+//   [14] index into the caller's i arrays (int bits)  [15] unused
+__global__ void regf_prep_kernel(const ISet is, float4 *__restrict__ rec, int *err) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= is.ni) return;
+  const int i = is.perm ? is.perm[slot] : slot;
+  const double x0 = is.x[3 * i], x1 = is.x[3 * i + 1], x2 = is.x[3 * i + 2];
+  const double v0 = is.v[3 * i], v1 = is.v[3 * i + 1], v2 = is.v[3 * i + 2];
+  const double h2 = is.h2[i], dtr = is.dtr[i];
+  if (isnan(x0) || isnan(x1) || isnan(x2) || isnan(v0) || isnan(v1) || isnan(v2) || isnan(h2) ||
+      isnan(dtr))
+    raise_error(err, GPUNB_E_NAN);
+  float xh, xl, yh, yl, zh, zl;
+  ds_split(x0, xh, xl);
+  ds_split(x1, yh, yl);
+  ds_split(x2, zh, zl);
   const double grow = 1.0 + 0x1p-12;
-  I.s = valid ? (float)(sqrt(fmax(h2, 0.0)) * grow) : -1.0f;
-  I.dv = (float)(fabs(dtr) * grow);
-  I.va = (float)(sqrt(v0 * v0 + v1 * v1 + v2 * v2) * grow);
-  I.h2f = (float)h2;
-  I.dtrf = (float)dtr;
-  I.i = valid ? i : -1;
+  float4 *r = rec + 4 * (size_t)slot;
+  r[0] = make_float4(-xh, -yh, -zh, -xl);
+  r[1] = make_float4(-yl, -zl, -(float)v0, -(float)v1);
+  r[2] = make_float4(-(float)v2, (float)(sqrt(fmax(h2, 0.0)) * grow), (float)(fabs(dtr) * grow),
+                     (float)(sqrt(v0 * v0 + v1 * v1 + v2 * v2) * grow));
+  r[3] = make_float4((float)h2, (float)dtr, __int_as_float(i), 0.f);
+}
+
+__device__ __forceinline__ void load_istate(IState &I, const float4 *__restrict__ rec, int slot,
+                                            bool valid) {
+  if (valid) {
+    const float4 *r = rec + 4 * (size_t)slot;
+    const float4 a = r[0], b = r[1], c = r[2], d = r[3];
+    I.nxh = mk2(a.x); I.nyh = mk2(a.y); I.nzh = mk2(a.z);
+    I.nxl = mk2(a.w); I.nyl = mk2(b.x); I.nzl = mk2(b.y);
+    I.nvx = mk2(b.z); I.nvy = mk2(b.w); I.nvz = mk2(c.x);
+    I.s = c.y; I.dv = c.z; I.va = c.w;
+    I.h2f = d.x; I.dtrf = d.y; I.i = __float_as_int(d.z);
+  } else {
+    I.nxh = I.nyh = I.nzh = I.nxl = I.nyl = I.nzl = mk2(0.f);
+    I.nvx = I.nvy = I.nvz = mk2(0.f);
+    I.s = -1.f; I.dv = 0.f; I.va = 0.f; I.h2f = -1.f; I.dtrf = 0.f; I.i = -1;
+  }
 }
 
 // Exact FP64 decision for a pair whose FP32 criterion value fell inside the
@@ -175,6 +196,60 @@ __device__ __forceinline__ void record_neighbour(const RegfOut &out, int i, int 
   if (slot < out.cap) out.rows[(size_t)i * out.cap + slot] = j;
 }
 
+// Two j (one f32x2 lane pair) against one i: the whole per-pair computation.
+struct JPair {
+  f2 v[NFIELD];   // indexed by JField
+};
+
+template <bool MFLAG>
+__device__ __forceinline__ void pair2(const IState &I, float H, const JPair &p, f2 (&q)[NQ],
+                                      int jg0, const JSet &js, const ISet &is,
+                                      const RegfOut &out) {
+  // double-single coordinate difference: (hi_j - hi_i) + (lo_j - lo_i)
+  const f2 dx = add2(add2(p.v[F_XH], I.nxh), add2(p.v[F_XL], I.nxl));
+  const f2 dy = add2(add2(p.v[F_YH], I.nyh), add2(p.v[F_YL], I.nyl));
+  const f2 dz = add2(add2(p.v[F_ZH], I.nzh), add2(p.v[F_ZL], I.nzl));
+  const f2 dvx = add2(p.v[F_VX], I.nvx);
+  const f2 dvy = add2(p.v[F_VY], I.nvy);
+  const f2 dvz = add2(p.v[F_VZ], I.nvz);
+  const f2 mn = p.v[F_MN];
+  const f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+  const f2 rv = fma2(dz, dvz, fma2(dy, dvy, mul2(dx, dvx)));
+  // rsqrt estimate + one Newton step, scaled: z = y0 (x y0^2 - 3) = -2/r
+  const f2 y0 = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+  f2 z = mul2(y0, fma2(mul2(r2, y0), y0, mk2(-3.0f)));
+  const bool c0 = r2.x < H, c1 = r2.y < H;
+  if (__any_sync(0xffffffffu, c0 | c1)) {
+    // slots >= nj are padding and never qualify; ids are reported in the
+    // caller's numbering (perm maps tile slot -> sent index)
+    if (c0 && jg0 < js.nj) {
+      const int jo = js.perm ? js.perm[jg0] : jg0;
+      if (decide_pair<MFLAG>(I, is, js, jo, dx.x, dy.x, dz.x, dvx.x, dvy.x, dvz.x, r2.x, mn.x)) {
+        record_neighbour(out, I.i, jo);
+        z.x = 0.f;
+      }
+    }
+    if (c1 && jg0 + 1 < js.nj) {
+      const int jo = js.perm ? js.perm[jg0 + 1] : jg0 + 1;
+      if (decide_pair<MFLAG>(I, is, js, jo, dx.y, dy.y, dz.y, dvx.y, dvy.y, dvz.y, r2.y, mn.y)) {
+        record_neighbour(out, I.i, jo);
+        z.y = 0.f;
+      }
+    }
+  }
+  const f2 mr = mul2(mn, z);            // m/r
+  const f2 z2 = mul2(z, z);             // 4/r^2
+  const f2 mr3 = mul2(mr, z2);          // 4 m/r^3
+  q[6] = add2(q[6], mr);
+  q[0] = fma2(mr3, dx, q[0]);
+  q[1] = fma2(mr3, dy, q[1]);
+  q[2] = fma2(mr3, dz, q[2]);
+  const f2 al = mul2(mul2(rv, z2), mk2(-0.75f));   // -3 (r.v)/r^2
+  q[3] = fma2(mr3, fma2(al, dx, dvx), q[3]);
+  q[4] = fma2(mr3, fma2(al, dy, dvy), q[4]);
+  q[5] = fma2(mr3, fma2(al, dz, dvz), q[5]);
+}
+
 // ---------------------------------------------------------------------------
 // Split-precision pair kernel, persistent.
 //   IPT : i-particles per thread (independent chains)
@@ -194,14 +269,14 @@ struct RegfWork {
   int S;
 };
 
-template <int IPT, int WI, int WJ, bool MFLAG>
+template <int IPT, int WI, int WJ, int JV, bool MFLAG>
 __global__ void __launch_bounds__(32 * WI * WJ)
     regf_ds_kernel(const JSet js, const ISet is, const RegfOut out, const RegfWork w) {
   constexpr int NT = 32 * WI * WJ;
   constexpr int NW = NT / 32;
   constexpr int ITILE = 32 * IPT * WI;
   constexpr int JW = JT / WJ;
-  static_assert(JW % 2 == 0, "j per warp must be even");
+  static_assert(JW % JV == 0 && (JV == 2 || JV == 4), "j per warp must be a multiple of JV");
   extern __shared__ __align__(128) float smem[];
   float *ring = smem;                                   // NSTAGE * TILE_FLOATS
   float *ffs = smem + NSTAGE * TILE_FLOATS;             // [2][NQ][IPT][NT] float-float
@@ -250,9 +325,7 @@ __global__ void __launch_bounds__(32 * WI * WJ)
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
       const int slot = it * ITILE + wi * 32 * IPT + k * 32 + lane;
-      const bool valid = slot < is.ni;
-      const int i = valid ? (is.perm ? is.perm[slot] : slot) : -1;
-      load_istate(I[k], is, i, valid, out.err, sy == 0 && wj == 0);
+      load_istate(I[k], is.rec, slot, slot < is.ni);
 #pragma unroll
       for (int c = 0; c < NQ; ++c) {
         q[k][c] = make_float2(0.f, 0.f);
@@ -275,63 +348,26 @@ __global__ void __launch_bounds__(32 * WI * WJ)
         const float base = I[k].dv * (I[k].va + vmax);
         const float b = MFLAG ? fmaf(I[k].s, smax, base) : I[k].s + base;
         const float H = (I[k].s < 0.f) ? -1.0f : b * b;
+        if (JV == 2) {
 #pragma unroll 2
-        for (int jj = jbeg; jj < jbeg + JW; jj += 2) {
-          const f2 xh = *(const f2 *)(T + F_XH * JT + jj);
-          const f2 yh = *(const f2 *)(T + F_YH * JT + jj);
-          const f2 zh = *(const f2 *)(T + F_ZH * JT + jj);
-          const f2 xl = *(const f2 *)(T + F_XL * JT + jj);
-          const f2 yl = *(const f2 *)(T + F_YL * JT + jj);
-          const f2 zl = *(const f2 *)(T + F_ZL * JT + jj);
-          const f2 vx = *(const f2 *)(T + F_VX * JT + jj);
-          const f2 vy = *(const f2 *)(T + F_VY * JT + jj);
-          const f2 vz = *(const f2 *)(T + F_VZ * JT + jj);
-          const f2 mn = *(const f2 *)(T + F_MN * JT + jj);
-          // double-single coordinate difference: (hi_j - hi_i) + (lo_j - lo_i)
-          const f2 dx = add2(add2(xh, I[k].nxh), add2(xl, I[k].nxl));
-          const f2 dy = add2(add2(yh, I[k].nyh), add2(yl, I[k].nyl));
-          const f2 dz = add2(add2(zh, I[k].nzh), add2(zl, I[k].nzl));
-          const f2 dvx = add2(vx, I[k].nvx);
-          const f2 dvy = add2(vy, I[k].nvy);
-          const f2 dvz = add2(vz, I[k].nvz);
-          const f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-          const f2 rv = fma2(dz, dvz, fma2(dy, dvy, mul2(dx, dvx)));
-          // rsqrt estimate + one Newton step, scaled: z = y0 (x y0^2 - 3) = -2/r
-          const f2 y0 = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-          f2 z = mul2(y0, fma2(mul2(r2, y0), y0, mk2(-3.0f)));
-          const bool c0 = r2.x < H, c1 = r2.y < H;
-          if (__any_sync(0xffffffffu, c0 | c1)) {
-            const int jg0 = (t0 + t) * JT + jj;
-            // slots >= nj are padding and never qualify; ids are reported in
-            // the caller's numbering (perm maps tile slot -> sent index)
-            if (c0 && jg0 < js.nj) {
-              const int jo = js.perm ? js.perm[jg0] : jg0;
-              if (decide_pair<MFLAG>(I[k], is, js, jo, dx.x, dy.x, dz.x, dvx.x, dvy.x, dvz.x,
-                                     r2.x, mn.x)) {
-                record_neighbour(out, I[k].i, jo);
-                z.x = 0.f;
-              }
-            }
-            if (c1 && jg0 + 1 < js.nj) {
-              const int jo = js.perm ? js.perm[jg0 + 1] : jg0 + 1;
-              if (decide_pair<MFLAG>(I[k], is, js, jo, dx.y, dy.y, dz.y, dvx.y, dvy.y, dvz.y,
-                                     r2.y, mn.y)) {
-                record_neighbour(out, I[k].i, jo);
-                z.y = 0.f;
-              }
-            }
+          for (int jj = jbeg; jj < jbeg + JW; jj += 2) {
+            JPair p;
+#pragma unroll
+            for (int f = 0; f < NFIELD; ++f) p.v[f] = *(const f2 *)(T + f * JT + jj);
+            pair2<MFLAG>(I[k], H, p, q[k], (t0 + t) * JT + jj, js, is, out);
           }
-          const f2 mr = mul2(mn, z);            // m/r
-          const f2 z2 = mul2(z, z);             // 4/r^2
-          const f2 mr3 = mul2(mr, z2);          // 4 m/r^3
-          q[k][6] = add2(q[k][6], mr);
-          q[k][0] = fma2(mr3, dx, q[k][0]);
-          q[k][1] = fma2(mr3, dy, q[k][1]);
-          q[k][2] = fma2(mr3, dz, q[k][2]);
-          const f2 al = mul2(mul2(rv, z2), mk2(-0.75f));   // -3 (r.v)/r^2
-          q[k][3] = fma2(mr3, fma2(al, dx, dvx), q[k][3]);
-          q[k][4] = fma2(mr3, fma2(al, dy, dvy), q[k][4]);
-          q[k][5] = fma2(mr3, fma2(al, dz, dvz), q[k][5]);
+        } else {
+          for (int jj = jbeg; jj < jbeg + JW; jj += 4) {
+            JPair p0, p1;
+#pragma unroll
+            for (int f = 0; f < NFIELD; ++f) {
+              const float4 u = *(const float4 *)(T + f * JT + jj);
+              p0.v[f] = make_float2(u.x, u.y);
+              p1.v[f] = make_float2(u.z, u.w);
+            }
+            pair2<MFLAG>(I[k], H, p0, q[k], (t0 + t) * JT + jj, js, is, out);
+            pair2<MFLAG>(I[k], H, p1, q[k], (t0 + t) * JT + jj + 2, js, is, out);
+          }
         }
       }
       // fold the tile's FP32 chunk sums into the float-float accumulators
@@ -481,6 +517,59 @@ __global__ void __launch_bounds__(128) regf_fp64_kernel(const JSet js, const ISe
 // deterministic replacement of force_reduce_kernel + the host sum over GPUs,
 // gpunb.velocity.cu:441-496,822-845).  Also turns counts into the in-band
 // overflow flag of gpunb.velocity.cu:872-877 / reg.avx.cpp:320-321.
+__device__ __forceinline__ void merge_store(const double *s, int i, const int *__restrict__ cnt,
+                                            int nnbmax, double *__restrict__ acc,
+                                            double *__restrict__ jrk, double *__restrict__ pot,
+                                            int *__restrict__ nnb, int *__restrict__ rowlen) {
+  acc[3 * i + 0] = 0.25 * s[0];
+  acc[3 * i + 1] = 0.25 * s[1];
+  acc[3 * i + 2] = 0.25 * s[2];
+  jrk[3 * i + 0] = 0.25 * s[3];
+  jrk[3 * i + 1] = 0.25 * s[4];
+  jrk[3 * i + 2] = 0.25 * s[5];
+  pot[i] = s[6];
+  const int c = cnt[i];
+  const bool over = c > nnbmax;
+  nnb[i] = over ? -c : c;
+  rowlen[i] = over ? 0 : c;
+}
+
+// Many j-splits (small active blocks): one block of MERGE_THREADS per i, each
+// thread summing a strided subset of the splits, then a fixed shared-memory
+// tree, so the order of the FP64 additions is the same in every run.
+constexpr int MERGE_THREADS = 128;
+__global__ void __launch_bounds__(MERGE_THREADS)
+    regf_merge_wide_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
+                           const int *__restrict__ cnt, int nnbmax, double *__restrict__ acc,
+                           double *__restrict__ jrk, double *__restrict__ pot,
+                           int *__restrict__ nnb, int *__restrict__ rowlen) {
+  __shared__ double sh[NQ][MERGE_THREADS];
+  const int i = blockIdx.x, t = threadIdx.x;
+  double s[NQ];
+#pragma unroll
+  for (int c = 0; c < NQ; ++c) s[c] = 0.0;
+  for (int k = t; k < S; k += MERGE_THREADS) {
+    const double *p = part + (size_t)k * NQ * ni_pad + i;
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * ni_pad];
+  }
+#pragma unroll
+  for (int c = 0; c < NQ; ++c) sh[c][t] = s[c];
+  __syncthreads();
+  for (int w = MERGE_THREADS / 2; w > 0; w >>= 1) {
+    if (t < w) {
+#pragma unroll
+      for (int c = 0; c < NQ; ++c) sh[c][t] += sh[c][t + w];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) s[c] = sh[c][0];
+    merge_store(s, i, cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
+  }
+}
+
 __global__ void regf_merge_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
                                   const int *__restrict__ cnt, int nnbmax,
                                   double *__restrict__ acc, double *__restrict__ jrk,
@@ -496,17 +585,7 @@ __global__ void regf_merge_kernel(const double *__restrict__ part, int S, int ni
 #pragma unroll
     for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * ni_pad];
   }
-  acc[3 * i + 0] = 0.25 * s[0];
-  acc[3 * i + 1] = 0.25 * s[1];
-  acc[3 * i + 2] = 0.25 * s[2];
-  jrk[3 * i + 0] = 0.25 * s[3];
-  jrk[3 * i + 1] = 0.25 * s[4];
-  jrk[3 * i + 2] = 0.25 * s[5];
-  pot[i] = s[6];
-  const int c = cnt[i];
-  const bool over = c > nnbmax;
-  nnb[i] = over ? -c : c;
-  rowlen[i] = over ? 0 : c;
+  merge_store(s, i, cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
 }
 
 // ---------------------------------------------------------------------------
@@ -645,7 +724,8 @@ __global__ void list_finalize_offsets_kernel(int *off, const int *btot, int ni, 
   if (i == 0) off[ni] = btot[nb];
 }
 
-static const VariantDesc kVariants[] = {{2, 4, 1}, {2, 2, 2}, {1, 1, 8}, {1, 4, 1}};
+static const VariantDesc kVariants[] = {{2, 4, 1, 2}, {2, 2, 2, 2}, {1, 1, 8, 2}, {1, 4, 1, 2},
+                                        {1, 4, 1, 4}, {1, 8, 1, 2}};
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 
 int regf_num_variants() { return kNumVariants; }
@@ -659,10 +739,12 @@ size_t regf_ds_smem(int v) {
 typedef void (*regf_fn)(JSet, ISet, RegfOut, RegfWork);
 static regf_fn regf_kernel_ptr(int v, bool mflag) {
   switch (v) {
-    case 0: return mflag ? regf_ds_kernel<2, 4, 1, true> : regf_ds_kernel<2, 4, 1, false>;
-    case 1: return mflag ? regf_ds_kernel<2, 2, 2, true> : regf_ds_kernel<2, 2, 2, false>;
-    case 2: return mflag ? regf_ds_kernel<1, 1, 8, true> : regf_ds_kernel<1, 1, 8, false>;
-    default: return mflag ? regf_ds_kernel<1, 4, 1, true> : regf_ds_kernel<1, 4, 1, false>;
+    case 0: return mflag ? regf_ds_kernel<2, 4, 1, 2, true> : regf_ds_kernel<2, 4, 1, 2, false>;
+    case 1: return mflag ? regf_ds_kernel<2, 2, 2, 2, true> : regf_ds_kernel<2, 2, 2, 2, false>;
+    case 2: return mflag ? regf_ds_kernel<1, 1, 8, 2, true> : regf_ds_kernel<1, 1, 8, 2, false>;
+    case 3: return mflag ? regf_ds_kernel<1, 4, 1, 2, true> : regf_ds_kernel<1, 4, 1, 2, false>;
+    case 4: return mflag ? regf_ds_kernel<1, 4, 1, 4, true> : regf_ds_kernel<1, 4, 1, 4, false>;
+    default: return mflag ? regf_ds_kernel<1, 8, 1, 2, true> : regf_ds_kernel<1, 8, 1, 2, false>;
   }
 }
 
@@ -713,8 +795,18 @@ cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const IS
 cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *cnt,
                               int nnbmax, double *acc, double *jrk, double *pot, int *nnb,
                               int *rowlen, cudaStream_t st) {
-  regf_merge_kernel<<<(ni + 255) / 256, 256, 0, st>>>(part, S, ni, ni_pad, cnt, nnbmax, acc, jrk,
-                                                      pot, nnb, rowlen);
+  if (S >= 32)
+    regf_merge_wide_kernel<<<ni, MERGE_THREADS, 0, st>>>(part, S, ni, ni_pad, cnt, nnbmax, acc,
+                                                         jrk, pot, nnb, rowlen);
+  else
+    regf_merge_kernel<<<(ni + 255) / 256, 256, 0, st>>>(part, S, ni, ni_pad, cnt, nnbmax, acc,
+                                                        jrk, pot, nnb, rowlen);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_regf_prep(const ISet &is, float4 *rec, int *err, cudaStream_t st) {
+  if (is.ni <= 0) return cudaSuccess;
+  regf_prep_kernel<<<(is.ni + 127) / 128, 128, 0, st>>>(is, rec, err);
   return cudaGetLastError();
 }
 

@@ -43,6 +43,7 @@ struct ISet {
   const double *x;       // [ni][3]
   const double *v;       // [ni][3]
   const int *perm;       // processing slot -> i index (Morton order), or null
+  const float4 *rec;     // [ni][4] FP32 i-records in slot order (regf_prep_kernel)
   int ni;
 };
 
