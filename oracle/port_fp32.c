@@ -8,6 +8,7 @@
  * too), unlike the FP64 oracle in oracle_fp64.c.
  */
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -23,13 +24,24 @@
 static float *port_j = NULL;      /* 7 arrays of port_cap: x y z m vx vy vz */
 static int port_nbody = 0, port_cap = 0;
 
-/* reciprocal square root with one Newton step, as v8sf_rsqrt
- * (reg.avx.cpp:74-77): y1 = -0.5*y0*(x*y0*y0 - 3).  The initial estimate is
- * the correctly rounded 1/sqrtf(x) here (the x86 estimate instruction has no
- * portable equivalent), so the Newton step only polishes it. */
+/* reciprocal square root: an initial estimate refined by Newton steps, as
+ * v8sf_rsqrt does (reg.avx.cpp:74-77: hardware estimate, then
+ * y1 = -0.5*y0*(x*y0*y0 - 3)).  The x86 estimate instruction has no portable
+ * equivalent; the estimate here is the published bit-level one (C. Lomont,
+ * "Fast inverse square root", 2003: i = 0x5f375a86 - (bits(x) >> 1), relative
+ * error of the raw estimate < 3.5e-2, < 1.8e-3 after one Newton step), and
+ * three Newton steps bring it to FP32 rounding level (max relative error
+ * 4.7e-6 after two).  Finite for x = 0.  It vectorises on every target (NEON
+ * on aarch64, SSE/AVX on x86). */
 static inline float port_rsqrt(float x)
 {
-    const float y = 1.0f / sqrtf(x);
+    uint32_t i;
+    memcpy(&i, &x, sizeof(i));
+    i = 0x5f375a86u - (i >> 1);
+    float y;
+    memcpy(&y, &i, sizeof(y));
+    y = (-0.5f * y) * (x * y * y - 3.0f);
+    y = (-0.5f * y) * (x * y * y - 3.0f);
     return (-0.5f * y) * (x * y * y - 3.0f);
 }
 
@@ -88,6 +100,7 @@ void port_regf_fp32(int ni, const double *h2d, const double *dtrd,
             const float xi = (float)xid[i][0], yi = (float)xid[i][1], zi = (float)xid[i][2];
             const float vxi = (float)vid[i][0], vyi = (float)vid[i][1], vzi = (float)vid[i][2];
             const float h2i = (float)h2d[i], dtri = (float)dtrd[i];
+            const float mf = m_flag ? 1.0f : 0.0f;
             float ax = 0, ay = 0, az = 0, jx = 0, jy = 0, jz = 0, po = 0;
             int nnb = 0;
             for (int jb = 0; jb < nj; jb += PORT_JB) {
@@ -104,11 +117,16 @@ void port_regf_fp32(int ni, const double *h2d, const double *dtrd,
                     float rv = dx * dvx + dy * dvy + dz * dvz;
                     const float r2p = dxp * dxp + dyp * dyp + dzp * dzp;
                     const float r2min = r2 < r2p ? r2 : r2p;
-                    const float crit = m_flag ? m[jj] * h2i : h2i;
+                    /* arithmetic instead of a select on m_flag, so that both
+                     * criteria share one vectorised loop */
+                    const float crit = h2i * (mf * m[jj] + (1.0f - mf));
                     const int in = r2min < crit;
                     flag[jj] = (unsigned char)in;
                     any |= in;
-                    float rinv1 = in ? 0.0f : port_rsqrt(r2);
+                    /* masked by multiplication, as the and-not mask of
+                     * reg.avx.cpp:292 (a select after the call would keep
+                     * the loop from vectorising) */
+                    float rinv1 = (in ? 0.0f : 1.0f) * port_rsqrt(r2);
                     const float rinv2 = rinv1 * rinv1;
                     rinv1 *= m[jj];
                     const float rinv3 = rinv1 * rinv2;
@@ -170,7 +188,7 @@ void port_pot_fp32(int istart, int ni, int n, const double *m,
             const float dy = (ph[3 * j + 1] - ph[3 * i + 1]) + (pl[3 * j + 1] - pl[3 * i + 1]);
             const float dz = (ph[3 * j + 2] - ph[3 * i + 2]) + (pl[3 * j + 2] - pl[3 * i + 2]);
             const float r2 = dx * dx + dy * dy + dz * dz;
-            float rinv = (r2 > 0.0f) ? port_rsqrt(r2) * pm[j] : 0.0f;
+            float rinv = ((r2 > 0.0f) ? pm[j] : 0.0f) * port_rsqrt(r2);
             const float t = sh;
             sh += rinv;
             sl -= (sh - t) - rinv;
