@@ -122,6 +122,23 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
                       int *list_off, int *list, size_t list_cap, int nnbmax, int m_flag,
                       void *stream);
 
+/* Batched clusters (no reference counterpart): ncl independent j-sets, each
+ * with its own active block, served by one persistent launch.  nj[] and ni[]
+ * are host arrays of ncl counts; all other pointers are device memory with
+ * the sets concatenated in order (m, x, v of all j-sets; h2, dtr, xi, vi and
+ * the outputs of all active blocks).  Each active block interacts with its
+ * own set only; neighbour ids are 0-based within the particle's own set;
+ * nnb/list_off/list are per concatenated i as in gpunb_regf_device.  The
+ * j-data are copied, so the inputs may change after the send. */
+int gpunb_batch_send_device(int ncl, const int *nj, const double *m, const double *x,
+                            const double *v, void *stream);
+int gpunb_batch_regf_device(int ncl, const int *ni, const double *h2, const double *dtr,
+                            const double *xi, const double *vi, double *acc, double *jrk,
+                            double *pot, int *nnb, int *list_off, int *list, size_t list_cap,
+                            int nnbmax, int m_flag, void *stream);
+/* Launch plan of the last batched call: kernel variant and work items. */
+int gpunb_batch_last_plan(int *variant, int *items);
+
 /* Potential of gpupot_ for callers that cannot allocate device memory (no
  * counterpart in the reference).  Meant for code that must not call
  * cudaMalloc: an energy check issued from inside a CUDA-graph-captured step,

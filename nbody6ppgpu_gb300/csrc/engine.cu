@@ -244,7 +244,7 @@ static bool ensure_order_scratch(int n) {
 static int send_common(int nj, cudaStream_t st) {
   const int ntile = (nj + JT - 1) / JT;
   if (!g.jtiles.ensure((size_t)std::max(ntile, 1) * TILE_BYTES) ||
-      !g.jperm.ensure((size_t)std::max(nj, 1) * sizeof(int)) || !ensure_order_scratch(nj))
+      !g.jperm.ensure((size_t)std::max(ntile, 1) * JT * sizeof(int)) || !ensure_order_scratch(nj))
     return GPUNB_E_ALLOC;
   double *m = g.jraw.as<double>();
   const double *x = m + nj;
@@ -254,6 +254,11 @@ static int send_common(int nj, cudaStream_t st) {
                        g.okeys_alt.as<unsigned long long>(), g.ovals_alt.as<int>(),
                        g.jperm.as<int>(), g.otemp.p, g.otemp.bytes, st),
           GPUNB_E_CUDA);
+  // padding slots of the last tile map to -1 (never a neighbour)
+  if (ntile * JT > nj)
+    CUDA_OR(cudaMemsetAsync(g.jperm.as<int>() + nj, 0xff, (size_t)(ntile * JT - nj) * sizeof(int),
+                            st),
+            GPUNB_E_CUDA);
   CUDA_OR(launch_pack_jtiles(m, x, m + 4 * (size_t)nj, nj, g.jperm.as<int>(),
                              g.jtiles.as<float>(), ntile, g.err.as<int>(), st),
           GPUNB_E_CUDA);
@@ -410,10 +415,10 @@ static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, in
   return GPUNB_OK;
 }
 
-static int finish_lists(int ni, int nnbmax, int S, int ni_pad, const RegfDev &o, size_t list_cap,
-                        cudaStream_t st) {
-  CUDA_OR(launch_regf_merge(g.part.as<double>(), S, ni, ni_pad, g.cnt.as<int>(), nnbmax, o.acc,
-                            o.jrk, o.pot, o.nnb, o.rowlen, st),
+static int finish_lists(int ni, int nnbmax, int S, int ni_pad, const int *perm, const RegfDev &o,
+                        size_t list_cap, cudaStream_t st) {
+  CUDA_OR(launch_regf_merge(g.part.as<double>(), S, ni, ni_pad, perm, g.cnt.as<int>(), nnbmax,
+                            o.acc, o.jrk, o.pot, o.nnb, o.rowlen, st),
           GPUNB_E_CUDA);
   CUDA_OR(launch_list_scan(o.rowlen, ni, o.off, o.btot, st), GPUNB_E_CUDA);
   (void)list_cap;
@@ -554,7 +559,7 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
                          ? ((ni + FP64_THREADS - 1) / FP64_THREADS) * FP64_THREADS
                          : ((ni + regf_variant(variant).itile() - 1) / regf_variant(variant).itile()) *
                                regf_variant(variant).itile();
-  if (finish_lists(ni, nnbmax, S, ni_pad, o, 0, st) != GPUNB_OK) return;
+  if (finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, 0, st) != GPUNB_OK) return;
   const size_t out_bytes = (size_t)7 * ni * sizeof(double) + (size_t)ni * sizeof(int);
   if (!g.hout.ensure(out_bytes + 2 * sizeof(int))) return;
   char *hob = g.hout.as<char>();
@@ -964,10 +969,13 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
                          ? ((ni + FP64_THREADS - 1) / FP64_THREADS) * FP64_THREADS
                          : ((ni + regf_variant(variant).itile() - 1) / regf_variant(variant).itile()) *
                                regf_variant(variant).itile();
-  rc = finish_lists(ni, nnbmax, S, ni_pad, o, list_cap, st);
+  rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, list_cap, st);
   if (rc != GPUNB_OK) return rc;
   CUDA_OR(launch_list_finalize_offsets(list_off, o.btot, ni, st), GPUNB_E_CUDA);
   return GPUNB_OK;
 }
 
 }  // extern "C"
+
+// batched clusters (shares the engine state above)
+#include "batch_impl.inc"

@@ -22,14 +22,22 @@ int regf_ds_blocks_per_sm(int v, bool mflag);
 cudaError_t launch_pack_jtiles(const double *m, const double *x, const double *v, int nj, const int *perm,
                                float *tiles, int ntile, int *err, cudaStream_t st);
 // persistent launch: `grid` blocks drain n_itiles * S work items from `queue`
+// (single j-set), or the n_items entries of `items` in `order` (batches)
 cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int *queue,
-                           const JSet &js, const ISet &is, const RegfOut &out, cudaStream_t st);
+                           const JSet &js, const ISet &is, const RegfOut &out, cudaStream_t st,
+                           const ItemDesc *items = nullptr, const int *order = nullptr,
+                           int n_items = 0);
 cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const ISet &is,
                              const RegfOut &out, cudaStream_t st);
 constexpr int FP64_THREADS = 128;
-cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *cnt,
-                              int nnbmax, double *acc, double *jrk, double *pot, int *nnb,
-                              int *rowlen, cudaStream_t st);
+cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *perm,
+                              const int *cnt, int nnbmax, double *acc, double *jrk, double *pot,
+                              int *nnb, int *rowlen, cudaStream_t st);
+// batched clusters: tiles[k] = {slot0, nslots, first partial row, number of rows}
+cudaError_t launch_regf_merge_batch(const double *part, const int4 *tiles, int ntiles, int itile,
+                                    const int *perm, const int *cnt, int nnbmax, double *acc,
+                                    double *jrk, double *pot, int *nnb, int *rowlen,
+                                    cudaStream_t st);
 // FP32 i-records in processing order (NaN check of the i inputs included)
 cudaError_t launch_regf_prep(const ISet &is, float4 *rec, int *err, cudaStream_t st);
 // scan of rowlen -> off (+ block offsets in btot, grand total at btot[nblocks])
@@ -45,6 +53,14 @@ cudaError_t launch_bbox(const double *x, int n, int *bb, cudaStream_t st);
 cudaError_t launch_order(const double *x, int n, const int *bb, unsigned long long *keys,
                          unsigned long long *keys_alt, int *vals_alt, int *perm, void *temp,
                          size_t temp_bytes, cudaStream_t st);
+
+// batched sets: order each set (off[nset+1] boundaries) along the Morton
+// curve and place set c at slots slot_off[c].. of perm (other slots -1)
+size_t order_batch_temp_bytes(int n, int nset);
+cudaError_t launch_order_batch(const double *x, int n, const int *bb, const int *off, int nset,
+                               const int *slot_off, int nslots, unsigned long long *keys,
+                               unsigned long long *keys_alt, int *vals_alt, int *sorted,
+                               int *perm, void *temp, size_t temp_bytes, cudaStream_t st);
 
 // potential
 constexpr int POT_JT = 128;

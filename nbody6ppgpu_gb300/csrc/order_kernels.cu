@@ -86,6 +86,79 @@ __global__ void morton_kernel(const double *__restrict__ x, int n, const int *__
   val[i] = i;
 }
 
+// owning set of element e: the c with off[c] <= e < off[c+1]
+__device__ __forceinline__ int owner_of(const int *__restrict__ off, int nset, int e) {
+  int lo = 0, hi = nset;   // invariant off[lo] <= e < off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= e) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Batched sets: key = (set index << 48) | Morton key, so that one stable sort
+// groups the bodies by set and orders each set along the curve.
+__global__ void morton_batch_kernel(const double *__restrict__ x, int n, const int *__restrict__ bb,
+                                    const int *__restrict__ off, int nset,
+                                    unsigned long long *__restrict__ key, int *__restrict__ val) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned int q[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float lo = ord2f(bb[c]), hi = ord2f(bb[3 + c]);
+    const float span = hi - lo;
+    const float s = span > 0.f ? 65535.0f / span : 0.f;
+    float u = ((float)x[3 * i + c] - lo) * s;
+    u = fminf(fmaxf(u, 0.f), 65535.f);
+    q[c] = (unsigned int)u;
+  }
+  const unsigned long long set = (unsigned long long)owner_of(off, nset, i);
+  key[i] = (set << 48) | spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+  val[i] = i;
+}
+
+// sorted position q (grouped by set, off[] = set boundaries) -> slot in a
+// layout where set c starts at slot_off[c]; slots not written keep -1.
+__global__ void scatter_slots_kernel(const int *__restrict__ sorted, int n,
+                                     const int *__restrict__ off, const int *__restrict__ slot_off,
+                                     int nset, int *__restrict__ perm) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int c = owner_of(off, nset, q);
+  perm[slot_off[c] + (q - off[c])] = sorted[q];
+}
+
+cudaError_t launch_order_batch(const double *x, int n, const int *bb, const int *off, int nset,
+                               const int *slot_off, int nslots, unsigned long long *keys,
+                               unsigned long long *keys_alt, int *vals_alt, int *sorted,
+                               int *perm, void *temp, size_t temp_bytes, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(perm, 0xff, (size_t)nslots * sizeof(int), st);
+  if (e != cudaSuccess || n <= 0) return e;
+  morton_batch_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, n, bb, off, nset, keys, vals_alt);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  int end_bit = 48;
+  while ((1ll << (end_bit - 48)) < nset) ++end_bit;
+  size_t tb = temp_bytes;
+  e = cub::DeviceRadixSort::SortPairs(temp, tb, keys, keys_alt, vals_alt, sorted, n, 0, end_bit,
+                                      st);
+  if (e != cudaSuccess) return e;
+  scatter_slots_kernel<<<(n + 255) / 256, 256, 0, st>>>(sorted, n, off, slot_off, nset, perm);
+  return cudaGetLastError();
+}
+
+size_t order_batch_temp_bytes(int n, int nset) {
+  int end_bit = 48;
+  while ((1ll << (end_bit - 48)) < nset) ++end_bit;
+  size_t tb = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tb, (const unsigned long long *)nullptr,
+                                  (unsigned long long *)nullptr, (const int *)nullptr,
+                                  (int *)nullptr, n, 0, end_bit);
+  return tb;
+}
+
 size_t order_temp_bytes(int n) {
   size_t tb = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tb, (const unsigned long long *)nullptr,

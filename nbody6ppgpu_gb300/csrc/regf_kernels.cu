@@ -22,7 +22,8 @@ namespace gpunb {
 // j packing: FP64 (as sent) -> split-precision SoA tiles + tile metadata.
 // One block of JT threads per tile.  Replaces the host-side Jparticle packing
 // of gpunb.velocity.cu:716-727 (which also drops positions to plain FP32).
-// Tile slot p holds body perm[p] (identity when perm is null).
+// Tile slot p holds body perm[p] (identity when perm is null; perm[p] = -1
+// marks a padding slot).
 __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restrict__ m,
                                                          const double *__restrict__ x,
                                                          const double *__restrict__ v, int nj,
@@ -32,8 +33,8 @@ __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restric
   float *T = tiles + (size_t)t * TILE_FLOATS;
   double vabs = 0.0, mj = 0.0;
   int real = 0;
-  if (p < nj) {
-    const int j = perm ? perm[p] : p;
+  const int j = perm ? perm[p] : (p < nj ? p : -1);   // -1: padding slot
+  if (j >= 0) {
     const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
     const double v0 = v[3 * j], v1 = v[3 * j + 1], v2 = v[3 * j + 2];
     mj = m[j];
@@ -124,6 +125,7 @@ __global__ void regf_prep_kernel(const ISet is, float4 *__restrict__ rec, int *e
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= is.ni) return;
   const int i = is.perm ? is.perm[slot] : slot;
+  if (i < 0) return;   // padding slot of a batched layout (never read)
   const double x0 = is.x[3 * i], x1 = is.x[3 * i + 1], x2 = is.x[3 * i + 2];
   const double v0 = is.v[3 * i], v1 = is.v[3 * i + 1], v2 = is.v[3 * i + 2];
   const double h2 = is.h2[i], dtr = is.dtr[i];
@@ -203,7 +205,7 @@ struct JPair {
 
 template <bool MFLAG>
 __device__ __forceinline__ void pair2(const IState &I, float H, const JPair &p, f2 (&q)[NQ],
-                                      int jg0, const JSet &js, const ISet &is,
+                                      int jg0, int jbase, const JSet &js, const ISet &is,
                                       const RegfOut &out) {
   // double-single coordinate difference: (hi_j - hi_i) + (lo_j - lo_i)
   const f2 dx = add2(add2(p.v[F_XH], I.nxh), add2(p.v[F_XL], I.nxl));
@@ -220,19 +222,22 @@ __device__ __forceinline__ void pair2(const IState &I, float H, const JPair &p, 
   f2 z = mul2(y0, fma2(mul2(r2, y0), y0, mk2(-3.0f)));
   const bool c0 = r2.x < H, c1 = r2.y < H;
   if (__any_sync(0xffffffffu, c0 | c1)) {
-    // slots >= nj are padding and never qualify; ids are reported in the
-    // caller's numbering (perm maps tile slot -> sent index)
-    if (c0 && jg0 < js.nj) {
-      const int jo = js.perm ? js.perm[jg0] : jg0;
-      if (decide_pair<MFLAG>(I, is, js, jo, dx.x, dy.x, dz.x, dvx.x, dvy.x, dvz.x, r2.x, mn.x)) {
-        record_neighbour(out, I.i, jo);
+    // perm maps a tile slot to the index into the sent arrays; padding slots
+    // hold -1 and never qualify.  Ids are reported relative to the owning
+    // j-set (jbase), in the caller's numbering.
+    if (c0) {
+      const int jo = js.perm[jg0];
+      if (jo >= 0 &&
+          decide_pair<MFLAG>(I, is, js, jo, dx.x, dy.x, dz.x, dvx.x, dvy.x, dvz.x, r2.x, mn.x)) {
+        record_neighbour(out, I.i, jo - jbase);
         z.x = 0.f;
       }
     }
-    if (c1 && jg0 + 1 < js.nj) {
-      const int jo = js.perm ? js.perm[jg0 + 1] : jg0 + 1;
-      if (decide_pair<MFLAG>(I, is, js, jo, dx.y, dy.y, dz.y, dvx.y, dvy.y, dvz.y, r2.y, mn.y)) {
-        record_neighbour(out, I.i, jo);
+    if (c1) {
+      const int jo = js.perm[jg0 + 1];
+      if (jo >= 0 &&
+          decide_pair<MFLAG>(I, is, js, jo, dx.y, dy.y, dz.y, dvx.y, dvy.y, dvz.y, r2.y, mn.y)) {
+        record_neighbour(out, I.i, jo - jbase);
         z.y = 0.f;
       }
     }
@@ -264,9 +269,12 @@ __device__ __forceinline__ void pair2(const IState &I, float H, const JPair &p, 
 constexpr int NSTAGE = 4;
 
 struct RegfWork {
-  int *queue;      // item counter, zeroed before the launch
-  int n_itiles;
+  int *queue;              // item counter, zeroed before the launch
+  int n_itiles;            // single j-set: items are (split, i-tile) pairs
   int S;
+  const ItemDesc *items;   // batched clusters: explicit item table (else null)
+  const int *order;        // queue position -> item (largest first), or null
+  int n_items;
 };
 
 template <int IPT, int WI, int WJ, int JV, bool MFLAG>
@@ -287,7 +295,7 @@ __global__ void __launch_bounds__(32 * WI * WJ)
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wi = warp % WI, wj = warp / WI;
-  const int n_items = w.n_itiles * w.S;
+  const int n_items = w.items ? w.n_items : w.n_itiles * w.S;
 
   if (tid == 0) {
     for (int u = 0; u < NSTAGE; ++u) {
@@ -304,11 +312,20 @@ __global__ void __launch_bounds__(32 * WI * WJ)
   for (;;) {
     if (tid == 0) s_item = atomicAdd(w.queue, 1);
     __syncthreads();
-    const int item = s_item;
-    if (item >= n_items || s_abort) break;
-    const int sy = item / w.n_itiles, it = item - sy * w.n_itiles;
-    const int t0 = (int)(((long long)js.ntile * sy) / w.S);
-    const int t1 = (int)(((long long)js.ntile * (sy + 1)) / w.S);
+    const int qpos = s_item;
+    if (qpos >= n_items || s_abort) break;
+    int slot0, slot_end, t0, t1, prow, jbase, pcol0;
+    if (w.items) {
+      const ItemDesc d = w.items[w.order ? w.order[qpos] : qpos];
+      slot0 = d.slot0; slot_end = d.slot_end; t0 = d.t0; t1 = d.t1;
+      prow = d.prow; jbase = d.jbase; pcol0 = d.pcol0;
+    } else {
+      const int sy = qpos / w.n_itiles, it = qpos - sy * w.n_itiles;
+      slot0 = it * ITILE; slot_end = is.ni;
+      t0 = (int)(((long long)js.ntile * sy) / w.S);
+      t1 = (int)(((long long)js.ntile * (sy + 1)) / w.S);
+      prow = sy; jbase = 0; pcol0 = slot0;
+    }
     const int nt = t1 - t0;
     if (tid == 0) {
       for (int u = 0; u < NSTAGE && u < nt; ++u) {
@@ -324,8 +341,8 @@ __global__ void __launch_bounds__(32 * WI * WJ)
     f2 q[IPT][NQ];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
-      const int slot = it * ITILE + wi * 32 * IPT + k * 32 + lane;
-      load_istate(I[k], is.rec, slot, slot < is.ni);
+      const int slot = slot0 + wi * 32 * IPT + k * 32 + lane;
+      load_istate(I[k], is.rec, slot, slot < slot_end);
 #pragma unroll
       for (int c = 0; c < NQ; ++c) {
         q[k][c] = make_float2(0.f, 0.f);
@@ -354,7 +371,7 @@ __global__ void __launch_bounds__(32 * WI * WJ)
             JPair p;
 #pragma unroll
             for (int f = 0; f < NFIELD; ++f) p.v[f] = *(const f2 *)(T + f * JT + jj);
-            pair2<MFLAG>(I[k], H, p, q[k], (t0 + t) * JT + jj, js, is, out);
+            pair2<MFLAG>(I[k], H, p, q[k], (t0 + t) * JT + jj, jbase, js, is, out);
           }
         } else {
           for (int jj = jbeg; jj < jbeg + JW; jj += 4) {
@@ -365,8 +382,8 @@ __global__ void __launch_bounds__(32 * WI * WJ)
               p0.v[f] = make_float2(u.x, u.y);
               p1.v[f] = make_float2(u.z, u.w);
             }
-            pair2<MFLAG>(I[k], H, p0, q[k], (t0 + t) * JT + jj, js, is, out);
-            pair2<MFLAG>(I[k], H, p1, q[k], (t0 + t) * JT + jj + 2, js, is, out);
+            pair2<MFLAG>(I[k], H, p0, q[k], (t0 + t) * JT + jj, jbase, js, is, out);
+            pair2<MFLAG>(I[k], H, p1, q[k], (t0 + t) * JT + jj + 2, jbase, js, is, out);
           }
         }
       }
@@ -423,13 +440,13 @@ __global__ void __launch_bounds__(32 * WI * WJ)
     if (wj == 0) {
 #pragma unroll
       for (int k = 0; k < IPT; ++k) {
-        const int i = I[k].i;
-        if (i < 0) continue;
+        if (I[k].i < 0) continue;
+        const int col = pcol0 + wi * 32 * IPT + k * 32 + lane;
 #pragma unroll
         for (int c = 0; c < NQ; ++c) {
           const double v = (double)ffs[((0 * NQ + c) * IPT + k) * NT + tid] +
                            (double)ffs[((1 * NQ + c) * IPT + k) * NT + tid];
-          out.part[((size_t)sy * NQ + c) * out.ni_pad + i] = v;
+          out.part[((size_t)prow * NQ + c) * out.ni_pad + col] = v;
         }
       }
     }
@@ -534,22 +551,27 @@ __device__ __forceinline__ void merge_store(const double *s, int i, const int *_
   rowlen[i] = over ? 0 : c;
 }
 
-// Many j-splits (small active blocks): one block of MERGE_THREADS per i, each
-// thread summing a strided subset of the splits, then a fixed shared-memory
-// tree, so the order of the FP64 additions is the same in every run.
+// Partial sums are stored by processing slot (column); the result of slot s
+// belongs to i = perm[s] (identity without a permutation).
+//
+// Many j-splits (small active blocks): one block of MERGE_THREADS per slot,
+// each thread summing a strided subset of the splits, then a fixed
+// shared-memory tree, so the order of the FP64 additions is the same in
+// every run.
 constexpr int MERGE_THREADS = 128;
 __global__ void __launch_bounds__(MERGE_THREADS)
     regf_merge_wide_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
-                           const int *__restrict__ cnt, int nnbmax, double *__restrict__ acc,
-                           double *__restrict__ jrk, double *__restrict__ pot,
-                           int *__restrict__ nnb, int *__restrict__ rowlen) {
+                           const int *__restrict__ perm, const int *__restrict__ cnt, int nnbmax,
+                           double *__restrict__ acc, double *__restrict__ jrk,
+                           double *__restrict__ pot, int *__restrict__ nnb,
+                           int *__restrict__ rowlen) {
   __shared__ double sh[NQ][MERGE_THREADS];
-  const int i = blockIdx.x, t = threadIdx.x;
+  const int slot = blockIdx.x, t = threadIdx.x;
   double s[NQ];
 #pragma unroll
   for (int c = 0; c < NQ; ++c) s[c] = 0.0;
   for (int k = t; k < S; k += MERGE_THREADS) {
-    const double *p = part + (size_t)k * NQ * ni_pad + i;
+    const double *p = part + (size_t)k * NQ * ni_pad + slot;
 #pragma unroll
     for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * ni_pad];
   }
@@ -566,26 +588,49 @@ __global__ void __launch_bounds__(MERGE_THREADS)
   if (t == 0) {
 #pragma unroll
     for (int c = 0; c < NQ; ++c) s[c] = sh[c][0];
-    merge_store(s, i, cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
+    merge_store(s, perm ? perm[slot] : slot, cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
   }
 }
 
 __global__ void regf_merge_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
-                                  const int *__restrict__ cnt, int nnbmax,
-                                  double *__restrict__ acc, double *__restrict__ jrk,
+                                  const int *__restrict__ perm, const int *__restrict__ cnt,
+                                  int nnbmax, double *__restrict__ acc, double *__restrict__ jrk,
                                   double *__restrict__ pot, int *__restrict__ nnb,
                                   int *__restrict__ rowlen) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ni) return;
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= ni) return;
   double s[NQ];
 #pragma unroll
   for (int c = 0; c < NQ; ++c) s[c] = 0.0;
   for (int k = 0; k < S; ++k) {
-    const double *p = part + (size_t)k * NQ * ni_pad + i;
+    const double *p = part + (size_t)k * NQ * ni_pad + slot;
 #pragma unroll
     for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * ni_pad];
   }
-  merge_store(s, i, cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
+  merge_store(s, perm ? perm[slot] : slot, cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
+}
+
+// Batched clusters: one block per i-tile; the tile's splits are the partial
+// rows row0 .. row0+nrow-1 (stride itile), summed in row order.
+__global__ void regf_merge_batch_kernel(const double *__restrict__ part,
+                                        const int4 *__restrict__ tiles, int itile,
+                                        const int *__restrict__ perm,
+                                        const int *__restrict__ cnt, int nnbmax,
+                                        double *__restrict__ acc, double *__restrict__ jrk,
+                                        double *__restrict__ pot, int *__restrict__ nnb,
+                                        int *__restrict__ rowlen) {
+  const int4 td = tiles[blockIdx.x];   // slot0, nslots, row0, nrow
+  for (int u = threadIdx.x; u < td.y; u += blockDim.x) {
+    double s[NQ];
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) s[c] = 0.0;
+    for (int k = 0; k < td.w; ++k) {
+      const double *p = part + (size_t)(td.z + k) * NQ * itile + u;
+#pragma unroll
+      for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * itile];
+    }
+    merge_store(s, perm[td.x + u], cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -765,7 +810,8 @@ cudaError_t launch_pack_jtiles(const double *m, const double *x, const double *v
 }
 
 cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int *queue,
-                           const JSet &js, const ISet &is, const RegfOut &out, cudaStream_t st) {
+                           const JSet &js, const ISet &is, const RegfOut &out, cudaStream_t st,
+                           const ItemDesc *items, const int *order, int n_items) {
   const VariantDesc d = kVariants[v];
   regf_fn fn = regf_kernel_ptr(v, mflag);
   const size_t smem = regf_ds_smem(v);
@@ -779,6 +825,9 @@ cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int
   w.queue = queue;
   w.n_itiles = n_itiles;
   w.S = S;
+  w.items = items;
+  w.order = order;
+  w.n_items = n_items;
   fn<<<grid, d.threads(), smem, st>>>(js, is, out, w);
   return cudaGetLastError();
 }
@@ -792,15 +841,25 @@ cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const IS
   return cudaGetLastError();
 }
 
-cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *cnt,
-                              int nnbmax, double *acc, double *jrk, double *pot, int *nnb,
-                              int *rowlen, cudaStream_t st) {
+cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *perm,
+                              const int *cnt, int nnbmax, double *acc, double *jrk, double *pot,
+                              int *nnb, int *rowlen, cudaStream_t st) {
   if (S >= 32)
-    regf_merge_wide_kernel<<<ni, MERGE_THREADS, 0, st>>>(part, S, ni, ni_pad, cnt, nnbmax, acc,
-                                                         jrk, pot, nnb, rowlen);
+    regf_merge_wide_kernel<<<ni, MERGE_THREADS, 0, st>>>(part, S, ni, ni_pad, perm, cnt, nnbmax,
+                                                         acc, jrk, pot, nnb, rowlen);
   else
-    regf_merge_kernel<<<(ni + 255) / 256, 256, 0, st>>>(part, S, ni, ni_pad, cnt, nnbmax, acc,
-                                                        jrk, pot, nnb, rowlen);
+    regf_merge_kernel<<<(ni + 255) / 256, 256, 0, st>>>(part, S, ni, ni_pad, perm, cnt, nnbmax,
+                                                        acc, jrk, pot, nnb, rowlen);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_regf_merge_batch(const double *part, const int4 *tiles, int ntiles, int itile,
+                                    const int *perm, const int *cnt, int nnbmax, double *acc,
+                                    double *jrk, double *pot, int *nnb, int *rowlen,
+                                    cudaStream_t st) {
+  if (ntiles <= 0) return cudaSuccess;
+  regf_merge_batch_kernel<<<ntiles, 128, 0, st>>>(part, tiles, itile, perm, cnt, nnbmax, acc,
+                                                  jrk, pot, nnb, rowlen);
   return cudaGetLastError();
 }
 

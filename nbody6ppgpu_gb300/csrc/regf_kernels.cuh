@@ -47,8 +47,20 @@ struct ISet {
   int ni;
 };
 
+// One work item of the pair kernel: an i-tile against a range of j tiles.
+// Partial sums of slot s go to part[(prow*NQ + q)*ni_pad + pcol0 + (s - slot0)].
+struct ItemDesc {
+  int slot0;      // first processing slot of the i-tile
+  int slot_end;   // end of the owning j-set's slots (exclusive)
+  int t0, t1;     // tile range [t0, t1)
+  int prow;       // partial-sum row
+  int jbase;      // first index of the owning j-set (reported ids are relative)
+  int pcol0;      // partial-sum column of slot0
+  int pad;
+};
+
 struct RegfOut {
-  double *part;          // [S][NQ][ni_pad] partial sums
+  double *part;          // [rows][NQ][ni_pad] partial sums, column = processing slot
   int *cnt;              // [ni] neighbour counters (zeroed before the launch)
   int *rows;             // [ni][cap] unsorted neighbour ids
   int cap;               // row capacity (= nnbmax)

@@ -78,6 +78,13 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "gpunb_regf_device": ([C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.c_void_p, C.c_size_t, C.c_int, C.c_int, C.c_void_p], C.c_int),
+        "gpunb_batch_send_device": ([C.c_int, ip, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p], C.c_int),
+        "gpunb_batch_regf_device": ([C.c_int, ip, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_int,
+                                     C.c_int, C.c_void_p], C.c_int),
+        "gpunb_batch_last_plan": ([ip, ip], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
