@@ -201,6 +201,75 @@ def run_reference(args, ws, rank):
 
 
 # --------------------------------------------------------------------------
+def batched_leg(lib, dev, stream, steps: int, warmup: int):
+    """configs[2]: 256 independent Plummer clusters (N log-uniform in
+    [512, 16384], active fraction log-uniform in [2^-10, 1], neighbour target
+    U[50, 150]), every step one batched send + regf in a single persistent
+    launch replayed from a CUDA graph, against one send + regf per cluster."""
+    import torch
+    from nbody6ppgpu_gb300 import workloads
+    from nbody6ppgpu_gb300.batch import DeviceBatch
+    sets, active, h2, dtr, _ = workloads.clusters256()
+    nnbmax = 512
+    b = DeviceBatch(sets, active, nnbmax, device=dev.index, stream=stream)
+    b.set_radii(h2, dtr)
+    pairs = int(sum(len(s[0]) * len(a) for s, a in zip(sets, active)))
+    lib.gpunb_set_graphs(1)
+
+    def step():
+        b.send()
+        b.regf()
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1) / steps
+    lib.gpunb_set_graphs(0)
+    variant, items = b.last_plan()
+    # one gpunb_send_device + gpunb_regf_device per cluster, same buffers
+    joff = np.concatenate([[0], np.cumsum(b.nj)])
+    ioff = np.concatenate([[0], np.cumsum(b.ni)])
+    scratch_off = torch.empty(int(b.ni.max()) + 1, dtype=torch.int32, device=dev)
+    scratch_lst = torch.empty(int(b.ni.max()) * nnbmax, dtype=torch.int32, device=dev)
+    sp = stream.cuda_stream
+
+    def seq_pass():
+        for c in range(b.ncl):
+            j0, i0, ni = int(joff[c]), int(ioff[c]), int(b.ni[c])
+            rc = lib.gpunb_send_device(int(b.nj[c]), b.m.data_ptr() + 8 * j0,
+                                       b.x.data_ptr() + 24 * j0, b.v.data_ptr() + 24 * j0, sp)
+            assert rc == 0
+            rc = lib.gpunb_regf_device(ni, b.h2.data_ptr() + 8 * i0, b.dtr.data_ptr() + 8 * i0,
+                                       b.xi.data_ptr() + 24 * i0, b.vi.data_ptr() + 24 * i0,
+                                       b.acc.data_ptr() + 24 * i0, b.jrk.data_ptr() + 24 * i0,
+                                       b.pot.data_ptr() + 8 * i0, b.nnb.data_ptr() + 4 * i0,
+                                       scratch_off.data_ptr(), scratch_lst.data_ptr(),
+                                       ni * nnbmax, nnbmax, 0, sp)
+            assert rc == 0
+
+    seq_pass()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    seq_pass()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    seq_ms = e0.elapsed_time(e1)
+    return {"workload": "256 Plummer clusters, N log-uniform [512,16384], Kroupa, active "
+                        "fraction log-uniform [2^-10,1], target U[50,150], nbmax 512",
+            "bodies": int(b.nj.sum()), "active": int(b.ni.sum()), "pairs_per_step": pairs,
+            "value": pairs / (batched_ms * 1e-3) / 1e9, "unit": "Gpairs/s",
+            "ms_per_step": batched_ms, "graph": True, "variant": variant, "work_items": items,
+            "sequential_value": pairs / (seq_ms * 1e-3) / 1e9, "sequential_ms": seq_ms,
+            "speedup_over_sequential": seq_ms / batched_ms}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -209,6 +278,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local = dist_env()
@@ -361,6 +431,10 @@ def main():
     h2d = sum(56 * N + 64 * ni for ni in BLOCKS)
     d2h = sum(60 * ni + 4 * int(np.maximum(outs[ni].list[:, 0], 0).sum()) for ni in BLOCKS)
 
+    batched = None
+    if not args.no_batched:
+        batched = batched_leg(lib, dev, stream, steps=args.steps, warmup=args.warmup)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu, _ = cpu_baseline(c, acts)
@@ -396,6 +470,8 @@ def main():
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if batched is not None:
+        line["batched_clusters"] = batched
     nb.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

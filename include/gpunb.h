@@ -139,6 +139,11 @@ int gpunb_batch_regf_device(int ncl, const int *ni, const double *h2, const doub
 /* Launch plan of the last batched call: kernel variant and work items. */
 int gpunb_batch_last_plan(int *variant, int *items);
 
+/* CUDA graphs for the batched entry points: with flag = 1, the first call of a
+ * shape (set sizes, active counts, buffers) runs normally and is then
+ * captured; later calls of that shape replay the graph.  Default 0. */
+void gpunb_set_graphs(int flag);
+
 /* Potential of gpupot_ for callers that cannot allocate device memory (no
  * counterpart in the reference).  Meant for code that must not call
  * cudaMalloc: an energy check issued from inside a CUDA-graph-captured step,

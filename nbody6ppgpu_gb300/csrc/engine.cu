@@ -67,6 +67,10 @@ static double wtime() {
 
 // ---------------------------------------------------------------------------
 // grow-only buffers
+// Incremented whenever a device buffer moves: captured CUDA graphs hold raw
+// addresses and are replayed only while this count is unchanged.
+static unsigned long long g_alloc_gen = 0;
+
 struct DevBuf {
   void *p = nullptr;
   size_t bytes = 0;
@@ -75,6 +79,7 @@ struct DevBuf {
     if (p) cudaFree(p);
     p = nullptr;
     bytes = 0;
+    ++g_alloc_gen;
     size_t want = n + n / 4 + 256;
     if (cudaMalloc(&p, want) != cudaSuccess) {
       cudaGetLastError();
@@ -85,12 +90,57 @@ struct DevBuf {
     return true;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      ++g_alloc_gen;
+    }
     p = nullptr;
     bytes = 0;
   }
   template <class T> T *as() const { return (T *)p; }
 };
+
+// A captured CUDA graph of one call shape.  The first call of a shape runs
+// eagerly (allocating what it needs), then the same launch sequence is
+// captured; later calls of that shape replay it while no buffer has moved.
+struct GraphEntry {
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long gen = 0;
+};
+
+static void graph_drop(GraphEntry &e) {
+  if (e.exec) cudaGraphExecDestroy(e.exec);
+  e.exec = nullptr;
+}
+
+// issue(st) queues the device work of one call and returns an error code;
+// it must not touch host memory that changes between calls.
+template <class F>
+static int run_graphed(GraphEntry &e, bool enabled, cudaStream_t st, F issue) {
+  if (enabled && e.exec && e.gen == g_alloc_gen) {
+    CUDA_OR(cudaGraphLaunch(e.exec, st), GPUNB_E_CUDA);
+    return GPUNB_OK;
+  }
+  int rc = issue(st);
+  if (rc != GPUNB_OK || !enabled) return rc;
+  graph_drop(e);
+  const unsigned long long gen0 = g_alloc_gen;
+  CUDA_OR(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), GPUNB_E_CUDA);
+  rc = issue(st);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+  if (rc == GPUNB_OK && ec == cudaSuccess && graph && gen0 == g_alloc_gen) {
+    if (cudaGraphInstantiate(&e.exec, graph, 0) != cudaSuccess) {
+      cudaGetLastError();
+      e.exec = nullptr;
+    }
+    e.gen = g_alloc_gen;
+  } else {
+    cudaGetLastError();
+  }
+  if (graph) cudaGraphDestroy(graph);
+  return rc;
+}
 
 struct PinBuf {
   void *p = nullptr;
@@ -631,6 +681,9 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   g.time_reduce += wtime() - t_grav;
 }
 
+// batched-cluster state lives in batch_impl.inc (end of this file)
+static void batch_release();
+
 }  // namespace gpunb
 
 // ===========================================================================
@@ -683,6 +736,7 @@ void gpunb_close_(void) {
     return;
   }
   if (g.stream) cudaStreamSynchronize(g.stream);
+  batch_release();
   g.jraw.release(); g.jtiles.release(); g.hj.release();
   g.iraw.release(); g.part.release(); g.cnt.release(); g.rows.release();
   g.rowlen.release(); g.off.release(); g.btot.release(); g.dense.release();

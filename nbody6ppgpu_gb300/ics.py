@@ -235,13 +235,15 @@ def henon_scale(m, x, v, w_pot: float | None = None):
 # --------------------------------------------------------------------------
 # neighbour radius calibration
 
-def neighbour_counts(x: np.ndarray, rs: np.ndarray, sample: np.ndarray) -> np.ndarray:
+def neighbour_counts(x: np.ndarray, rs: np.ndarray, sample: np.ndarray, tree=None) -> np.ndarray:
     """Number of other bodies within RS_i of each sampled body (self excluded).
-    KD-tree when scipy is present, chunked brute force otherwise."""
+    KD-tree when scipy is present (pass a prebuilt `tree` of x to reuse it),
+    chunked brute force otherwise."""
     try:
         from scipy.spatial import cKDTree
-        tree = cKDTree(x)
-        cnt = tree.query_ball_point(x[sample], rs[sample], return_length=True)
+        if tree is None:
+            tree = cKDTree(x)
+        cnt = tree.query_ball_point(x[sample], rs[sample], return_length=True, workers=-1)
         return np.asarray(cnt) - 1
     except ImportError:  # pragma: no cover - scipy is present on both hosts
         out = np.empty(sample.size, dtype=np.int64)
@@ -261,9 +263,11 @@ def calibrate_rs(x: np.ndarray, target: float, rng: np.random.Generator,
     sample equals ``target``."""
     n = x.shape[0]
     k = int(min(k, max(n - 1, 1)))
+    tree = None
     try:
         from scipy.spatial import cKDTree
-        dk = cKDTree(x).query(x, k=k + 1)[0][:, -1]
+        tree = cKDTree(x)
+        dk = tree.query(x, k=k + 1, workers=-1)[0][:, -1]
     except ImportError:  # pragma: no cover
         dk = np.empty(n)
         for s in range(0, n, 256):
@@ -275,7 +279,7 @@ def calibrate_rs(x: np.ndarray, target: float, rng: np.random.Generator,
     lo, hi = 0.3, 3.0
     for it in range(40):
         c = 0.5 * (lo + hi)
-        mean = neighbour_counts(x, c * base, sample).mean()
+        mean = neighbour_counts(x, c * base, sample, tree).mean()
         if mean < target:
             lo = c
         else:

@@ -76,3 +76,27 @@ def test_batch_repeatable_and_shape_independent_lists(batch_case, variant):
         assert np.array_equal(r1.acc[c], r2.acc[c]) and np.array_equal(r1.nnb[c], r2.nnb[c])
         for a, b in zip(r1.lists[c], r2.lists[c]):
             assert np.array_equal(a, b)
+
+
+def test_batch_graph_replay_matches_eager(batch_case):
+    from nbody6ppgpu_gb300.batch import DeviceBatch
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    sets, act, h2s, dtrs = batch_case
+    eager, _ = run_batch(batch_case)
+    with GpuNb(1 << 16) as nb:
+        nb.lib.gpunb_set_graphs(1)
+        try:
+            b = DeviceBatch(sets, act, NNBMAX)
+            b.set_radii(h2s, dtrs)
+            for _ in range(3):        # eager + capture, then two replays
+                b.send()
+                b.regf()
+                r = b.results()
+                for c in range(len(SPECS)):
+                    assert np.array_equal(r.acc[c], eager.acc[c])
+                    assert np.array_equal(r.pot[c], eager.pot[c])
+                    assert np.array_equal(r.nnb[c], eager.nnb[c])
+                    for a, e in zip(r.lists[c], eager.lists[c]):
+                        assert np.array_equal(a, e)
+        finally:
+            nb.lib.gpunb_set_graphs(0)
