@@ -159,6 +159,33 @@ void gpunb_set_graphs(int flag);
 int gpupot_device_noalloc(int istart, int ni, int n, const double *m, const double *x,
                           double *pot, void *stream);
 
+/* ---- Learned neighbour-radius predictor (no reference counterpart) --------
+ * An 8 -> 64 -> 64 -> 1 GELU MLP that proposes each active particle's next
+ * RS in place of the plain rule of src/Main/regcor_gpu.F:146-253; the caller
+ * falls back to that rule (and to the overflow rule of
+ * src/Main/util_gpu.F:81-97) whenever the proposal is rejected.  It never
+ * touches forces.  Parameters: P floats (gpunb_rsmlp_num_params) in the order
+ * W1[64][8] | b1[64] | W2[64][64] | b2[64] | W3[64] | b3, held as an FP32
+ * master copy `wf` and a BF16 copy `wq` (P x 2 bytes) of the same order; the
+ * kernels read matrices from `wq`, biases from `wf`, and accumulate in FP32.
+ * All pointers are device pointers; calls are asynchronous on `stream`. */
+int gpunb_rsmlp_num_params(void);
+/* wq <- bf16(wf) */
+int gpunb_rsmlp_to_bf16(const float *wf, void *wq, void *stream);
+/* y[B] <- MLP(X[B][8]) */
+int gpunb_rsmlp_forward(int B, const float *X, const void *wq, const float *wf, float *y,
+                        void *stream);
+/* grad[P] <- d/dparams of loss = (1/B) sum_b W[b] (y_b - T[b])^2 (W may be NULL
+ * for unit weights); loss[1] <- that loss.  `part` is scratch of
+ * ceil(B/128) * (P + 1) floats.  The reduction order is fixed: repeated calls
+ * give bit-identical gradients. */
+int gpunb_rsmlp_backward(int B, const float *X, const float *T, const float *W, const void *wq,
+                         const float *wf, float *grad, float *loss, float *part, void *stream);
+/* One Adam step on the FP32 master (bias-corrected, step >= 1), then
+ * wq <- bf16(wf). */
+int gpunb_rsmlp_adam(float *wf, float *m1, float *m2, const float *grad, float lr, float beta1,
+                     float beta2, float eps, int step, void *wq, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

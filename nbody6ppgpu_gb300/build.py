@@ -19,7 +19,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIB = PKG / "libgpunb.so"
-SOURCES = ["regf_kernels.cu", "pot_kernels.cu", "order_kernels.cu", "engine.cu", "noalloc.cu"]
+SOURCES = ["regf_kernels.cu", "pot_kernels.cu", "order_kernels.cu", "engine.cu", "noalloc.cu",
+           "rsmlp.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -1,0 +1,96 @@
+"""Neighbour-radius experiment: the plain RS rule against the learned
+predictor with the plain rule as fallback.
+
+    python -m nbody6ppgpu_gb300.rs_experiment --n 16384 --ticks 64 --model king
+
+1. Harvest (features, label) pairs by running the regular-step driver with the
+   plain rule on two seeded clusters (the pairs the integrator itself
+   generates).
+2. Train the MLP on the GPU kernels (Adam, FP32 master, BF16 weights).
+3. Run a third seeded cluster twice from the same state -- plain rule, and
+   predictor + fallback -- and compare list-overflow recomputes after the
+   first block (the first block is identical for both), the membership
+   against the rule's own target, and the regular-call time.
+Prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import dataclasses
+import json
+import math
+import time
+
+import numpy as np
+
+from . import ics
+from .rsharness import Harness
+from .rsmlp import RSMLP
+
+
+def make(model: str, n: int, seed: int, target: float, q: float = 0.5):
+    """Seeded cluster; q < 1/2 scales the virial velocities to virial ratio q
+    (a cold start that collapses)."""
+    if model == "king":
+        c = ics.king(n, seed=seed, nb_target=target)
+    else:
+        c = ics.plummer(n, seed=seed, masses="kroupa", nb_target=target, exact_energy_max=0)
+    if q != 0.5:
+        c = dataclasses.replace(c, v=c.v * math.sqrt(q / 0.5))
+    return c
+
+
+def run(model="king", n=16384, ticks=64, nnbopt=100, nnbmax=200, levels=6, epochs=25,
+        train_seeds=(11, 12), eval_seed=13, q=0.5):
+    t0 = time.perf_counter()
+    X, Y = [], []
+    for s in train_seeds:
+        h = Harness(make(model, n, s, nnbopt, q), nnbopt, nnbmax, harvest=True, levels=levels)
+        h.run(ticks)
+        x, y = h.dataset()
+        h.close()
+        X.append(x)
+        Y.append(y)
+    X = np.concatenate(X)
+    Y = np.concatenate(Y)
+    t_harvest = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mlp = RSMLP(seed=3)
+    losses = mlp.train(X, Y, epochs=epochs)
+    t_train = time.perf_counter() - t0
+    c = make(model, n, eval_seed, nnbopt, q)
+    out = {"model": model, "q": q, "n": n, "ticks": ticks, "nnbopt": nnbopt, "nnbmax": nnbmax,
+           "levels": levels, "train_pairs": int(len(X)), "label_variance": float(Y.var()),
+           "train_mse_first_epoch": losses[0], "train_mse_last_epoch": losses[-1],
+           "harvest_s": t_harvest, "train_s": t_train}
+    for name, pred in (("plain", None), ("predictor", mlp)):
+        h = Harness(c, nnbopt, nnbmax, levels=levels)
+        s = h.run(ticks, predictor=pred).as_dict()
+        h.close()
+        out[name] = {k: s[k] for k in ("first_call_overflows", "overflow_events",
+                                       "overflow_after_predictor", "active",
+                                       "recompute_rate", "mean_count", "count_p99",
+                                       "regf_seconds", "predict_seconds", "predictor_used",
+                                       "predictor_fallback")}
+    p, q = out["plain"]["overflow_events"], out["predictor"]["overflow_events"]
+    out["overflow_recompute_ratio_plain_over_predictor"] = (p / q) if q else (None if p == 0 else float("inf"))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--model", default="king", choices=["king", "plummer"])
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--ticks", type=int, default=64)
+    ap.add_argument("--nnbopt", type=int, default=100)
+    ap.add_argument("--nnbmax", type=int, default=200)
+    ap.add_argument("--levels", type=int, default=6)
+    ap.add_argument("--q", type=float, default=0.5, help="virial ratio of the start")
+    ap.add_argument("--epochs", type=int, default=25)
+    a = ap.parse_args()
+    print(json.dumps(run(a.model, a.n, a.ticks, a.nnbopt, a.nnbmax, a.levels, epochs=a.epochs,
+                         q=a.q)), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,255 @@
+"""Regular-step driver for the neighbour-radius experiments.
+
+Drives libgpunb.so the way NBODY6++'s regular section does (intgrt.F:912-944,
+util_gpu.F:33-116): every tick the whole j-set is sent, the particles whose
+regular step is due form the active block, `gpunb_regf_` returns their
+regular force and neighbour lists, overflowed rows are repaired by the
+overflow rule and the chunk is computed again (one recompute per overflowed
+particle, as the GO TO 550 loop of util_gpu.F:98-101 does), and RS is then
+updated -- by the plain rule (regcor_gpu.F:146-253) or by the learned
+predictor with the plain rule as fallback.  The bodies move under the total
+force (a second regf call with an empty neighbour sphere gives it), with a
+kick-drift-kick leapfrog on the smallest regular step.
+
+Training pairs: the features of a particle at one regular step, and as label
+log(RS_k / RS), RS_k the radius that gives it exactly k neighbours at its next
+regular step under the kernel's membership test (position or predicted
+position inside RS, `label_log_radius`), k the membership the plain rule aims
+at for it (regcor_gpu.F:152-163: NNBOPT-stabilised, tapered outside the
+half-mass radius).  The rule approaches that membership by at
+most 25% in volume per step; the predictor proposes the radius for it
+directly.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import ics, rsrule
+from .gpunb import GpuNb
+from .rsmlp import features
+
+CHUNK = 1024            # maxthr of util_gpu.F:7
+
+
+@dataclass
+class HarnessStats:
+    regular_calls: int = 0
+    active: int = 0
+    first_call_overflows: int = 0    # overflows of the first block (same for every policy)
+    overflow_events: int = 0         # overflowed rows after it (one recompute each)
+    overflow_after_predictor: int = 0  # ... of which the RS came from the predictor
+    recompute_pairs: float = 0.0     # extra pair work of the recomputes
+    pairs: float = 0.0               # pair work of the first evaluations
+    predictor_used: int = 0
+    predictor_fallback: int = 0
+    regf_seconds: float = 0.0
+    predict_seconds: float = 0.0
+    counts: list = field(default_factory=list)
+
+    def as_dict(self):
+        d = dict(self.__dict__)
+        c = np.concatenate(self.counts) if self.counts else np.zeros(0)
+        d.pop("counts")
+        d["mean_count"] = float(c.mean()) if c.size else 0.0
+        d["count_p99"] = float(np.percentile(c, 99)) if c.size else 0.0
+        d["recompute_rate"] = self.overflow_events / max(self.active, 1)
+        return d
+
+
+def initial_rs(x: np.ndarray, nnbopt: int, n: int) -> np.ndarray:
+    """fpoly0.F:50-52: RS = RS0 sqrt(1 + r^2); RS0 from the mean density
+    (a common choice of the input parameter) -- deliberately not adapted to
+    the local density, as at the start of a run."""
+    rs0 = (3.0 * nnbopt / (4.0 * math.pi * n)) ** (1.0 / 3.0)
+    r2 = np.einsum("ij,ij->i", x, x)
+    return rs0 * np.sqrt(1.0 + r2)
+
+
+def label_log_radius(x: np.ndarray, v: np.ndarray, dtr: np.ndarray, idx: np.ndarray,
+                     ks: np.ndarray) -> np.ndarray:
+    """log of the radius R at which particle i's neighbour list holds exactly
+    k_i members besides itself, under the kernel's own membership test
+    min(|dx|^2, |dx + dtr_i dv|^2) < R^2 (gpunb.velocity.cu:172-180): the
+    geometric mean of the k-th and (k+1)-th smallest keys q_j =
+    min(|dx|^2, |dx + dtr_i dv|^2).
+
+    The k+2 smallest keys are all among the k+2 nearest bodies in position or
+    the k+2 nearest in predicted position x + dtr_i v (q_j is at most either
+    distance), so two k-nearest queries per step size give them exactly."""
+    from scipy.spatial import cKDTree
+    out = np.empty(idx.size)
+    tree = cKDTree(x)
+    d_all = dtr[idx]
+    for d in np.unique(d_all):
+        sel = np.nonzero(d_all == d)[0]
+        ii = idx[sel]
+        k = ks[sel]
+        K = int(min(k.max() + 2, x.shape[0]))
+        _, ja = tree.query(x[ii], k=K, workers=-1)
+        xp = x + d * v
+        _, jb = cKDTree(xp).query(xp[ii], k=K, workers=-1)
+        J = np.sort(np.concatenate([ja, jb], axis=1), axis=1)
+        dup = np.zeros(J.shape, dtype=bool)
+        dup[:, 1:] = J[:, 1:] == J[:, :-1]
+        dx = x[J] - x[ii][:, None, :]
+        dp = dx + d * (v[J] - v[ii][:, None, :])
+        q = np.minimum(np.einsum("abk,abk->ab", dx, dx), np.einsum("abk,abk->ab", dp, dp))
+        q[dup] = np.inf
+        q.sort(axis=1)                          # column 0: the body itself (q = 0)
+        rows = np.arange(sel.size)
+        lo = np.maximum(q[rows, k], 1e-300)
+        hi = np.maximum(q[rows, k + 1], lo)
+        out[sel] = 0.25 * (np.log(lo) + np.log(hi))
+    return out
+
+
+class Harness:
+    def __init__(self, cluster: ics.Cluster, nnbopt: int, nnbmax: int, smax: float = 0.125,
+                 levels: int = 4, params: rsrule.RSParams | None = None, rs=None,
+                 harvest: bool = False, rs0_factor: float = 1.0):
+        self.c = cluster
+        self.n = cluster.n
+        self.nnbopt, self.nnbmax = nnbopt, nnbmax
+        self.m = cluster.m.copy()
+        self.x = cluster.x.copy()
+        self.v = cluster.v.copy()
+        self.rs = (rs0_factor * initial_rs(self.x, nnbopt, self.n) if rs is None
+                   else rs.copy())
+        # regular steps: fpoly0.F:55-56, quantised to SMAX / 2^k, k < levels
+        st = ics.regular_step(self.x, smax)
+        k = np.clip(np.ceil(np.log2(smax / st)), 0, levels - 1).astype(int)
+        self.stepr = smax / 2.0 ** k
+        self.dt = smax / 2.0 ** (levels - 1)
+        self.tick = 0
+        self.next_tick = (self.stepr / self.dt).round().astype(int)
+        self.prev_nnb = np.full(self.n, nnbopt, dtype=np.int64)
+        self.src = np.zeros(self.n, dtype=np.int64)      # 1: RS set by the predictor
+        self.p = params or rsrule.RSParams(nnbopt=nnbopt, nnbmax=nnbmax,
+                                           bodym=float(self.m.mean()))
+        self.nb = GpuNb(self.n)
+        self.acc = self._total_force()
+        self.harvest = harvest
+        self.pending = {}
+        self.X, self.Y = [], []
+        self.stats = HarnessStats()
+
+    def close(self):
+        self.nb.close()
+
+    # -- dynamics -------------------------------------------------------------
+    def _total_force(self):
+        self.nb.send(self.m, self.x, self.v)
+        h2 = np.full(self.n, 1e-30)
+        r = self.nb.regf(h2, np.zeros(self.n), self.x, self.v, 2, 1)
+        return r.acc
+
+    def _kdk(self):
+        self.v += 0.5 * self.dt * self.acc
+        self.x += self.dt * self.v
+        self.acc = self._total_force()
+        self.v += 0.5 * self.dt * self.acc
+        self.tick += 1
+
+    # -- the regular block ---------------------------------------------------------
+    def _regf_with_recompute(self, idx):
+        """gpunb_regf_ on the active block in chunks of CHUNK; overflowed rows
+        are shrunk by the overflow rule and their chunk recomputed, one
+        recompute per overflowed row (util_gpu.F:66-101)."""
+        lmax = self.nnbmax + 1
+        t0 = time.perf_counter()
+        self.nb.send(self.m, self.x, self.v)
+        accs, jrks, nnbs, lists = [], [], [], []
+        for s in range(0, idx.size, CHUNK):
+            ch = idx[s:s + CHUNK]
+            res = self.nb.regf(self.rs[ch] ** 2, self.stepr[ch], self.x[ch], self.v[ch], lmax,
+                               self.nnbmax)
+            self.stats.pairs += ch.size * float(self.n)
+            while True:
+                over = res.list[:, 0] < 0
+                nover = int(over.sum())
+                if nover == 0:
+                    break
+                if self.stats.regular_calls == 0:
+                    self.stats.first_call_overflows += nover
+                else:
+                    self.stats.overflow_events += nover
+                    self.stats.overflow_after_predictor += int(self.src[ch[over]].sum())
+                    self.stats.recompute_pairs += nover * ch.size * float(self.n)
+                self.rs[ch[over]] = rsrule.overflow_rs(self.rs[ch[over]], res.list[over, 0],
+                                                       self.p)
+                sub = ch[over]
+                r2 = self.nb.regf(self.rs[sub] ** 2, self.stepr[sub], self.x[sub], self.v[sub],
+                                  lmax, self.nnbmax)
+                res.acc[over] = r2.acc
+                res.jrk[over] = r2.jrk
+                res.pot[over] = r2.pot
+                res.list[over] = r2.list
+            accs.append(res.acc); jrks.append(res.jrk)
+            nnbs.append(res.list[:, 0].copy()); lists.append(res.list)
+        self.stats.regf_seconds += time.perf_counter() - t0
+        self.stats.regular_calls += 1
+        return np.concatenate(accs), np.concatenate(jrks), np.concatenate(nnbs)
+
+    def step(self, predictor=None):
+        """Advance one tick; returns the active block's size."""
+        self._kdk()
+        idx = np.nonzero(self.next_tick <= self.tick)[0]
+        if idx.size == 0:
+            return 0
+        acc, jrk, nnb_raw = self._regf_with_recompute(idx)
+        nnb = np.maximum(nnb_raw - 1, 0)                 # self removed (util_gpu.F:102-111)
+        self.stats.active += idx.size
+        self.stats.counts.append(nnb)
+        if self.harvest:
+            self._harvest(idx)
+        F = features(self.x[idx], self.v[idx], self.m[idx] * self.n, self.rs[idx], nnb, acc,
+                     jrk, self.stepr[idx], self.nnbopt)
+        rs_old = self.rs[idx].copy()
+        plain, target = rsrule.regcor_rs(rs_old, nnb, self.prev_nnb[idx], self.x[idx],
+                                         self.v[idx], self.stepr[idx], self.p,
+                                         return_target=True)
+        plain = np.where(nnb < 2, rsrule.few_nb_rs(rs_old), plain)
+        new = plain
+        self.src[idx] = 0
+        if predictor is not None:
+            t0 = time.perf_counter()
+            y = predictor.predict(F)
+            self.stats.predict_seconds += time.perf_counter() - t0
+            # count implied at the predicted radius (local density unchanged);
+            # outside 0.5-1.5 x the rule's own target the plain rule is used
+            pred_count = (nnb + 1.0) * np.exp(3.0 * y) - 1.0
+            ok = (pred_count >= 0.5 * target) & (pred_count <= 1.5 * target) & np.isfinite(y)
+            new = np.where(ok, rs_old * np.exp(y), plain)
+            self.src[idx] = ok
+            self.stats.predictor_used += int(ok.sum())
+            self.stats.predictor_fallback += int((~ok).sum())
+        if self.harvest:
+            for q, i in enumerate(idx):
+                self.pending[int(i)] = (F[q], rs_old[q], target[q])
+        self.rs[idx] = new
+        self.prev_nnb[idx] = nnb
+        self.next_tick[idx] += (self.stepr[idx] / self.dt).round().astype(int)
+        return idx.size
+
+    def _harvest(self, idx):
+        have = np.array([int(i) for i in idx if int(i) in self.pending], dtype=np.int64)
+        if have.size == 0:
+            return
+        ks = np.array([int(min(max(round(self.pending[i][2]), 1), self.n - 3)) for i in have])
+        logr = label_log_radius(self.x, self.v, self.stepr, have, ks)
+        for q, i in enumerate(have):
+            f, rs_then, _ = self.pending.pop(int(i))
+            self.X.append(f)
+            self.Y.append(logr[q] - math.log(rs_then))
+
+    def run(self, ticks: int, predictor=None):
+        for _ in range(ticks):
+            self.step(predictor)
+        return self.stats
+
+    def dataset(self):
+        return np.array(self.X), np.array(self.Y)
