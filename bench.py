@@ -202,7 +202,7 @@ def run_reference(args, ws, rank):
 
 # --------------------------------------------------------------------------
 def batched_leg(lib, dev, stream, steps: int, warmup: int):
-    """configs[2]: 256 independent Plummer clusters (N log-uniform in
+    """256 independent Plummer clusters (N log-uniform in
     [512, 16384], active fraction log-uniform in [2^-10, 1], neighbour target
     U[50, 150]), every step one batched send + regf in a single persistent
     launch replayed from a CUDA graph, against one send + regf per cluster."""
@@ -270,6 +270,88 @@ def batched_leg(lib, dev, stream, steps: int, warmup: int):
             "speedup_over_sequential": seq_ms / batched_ms}
 
 
+def king1m_leg(n_sm: int, peak_mhz: float):
+    """King W0 = 6, N = 2^20, Kroupa masses with 10% binaries as c.m. bodies,
+    RS for a mean of 100 neighbours, nbmax 1024: the split kernel at
+    ni in {1024, 16384, 262144, N} (host ABI, kernel time from the library's
+    CUDA events), the FP64 kernel at ni = 16384, and the split results against
+    the FP64 ones on that block."""
+    from nbody6ppgpu_gb300 import ics
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    t0 = time.perf_counter()
+    k = ics.king(1 << 20, seed=4, nb_target=100.0)
+    t_ics = time.perf_counter() - t0
+    n = k.n
+    h2 = k.h2()
+    peak = fp32_peak_tflops(n_sm, peak_mhz)
+    blocks = {}
+    ref = None
+    with GpuNb(n) as nb:
+        nb.send(k.m, k.x, k.v)
+        nb.set_timing(True)
+        for ni in (1024, 16384, 262144, n):
+            act = ics.active_set(n, ni, seed=ni)
+            best = None
+            for _ in range(3 if ni < n else 2):
+                r = nb.regf(h2[act], k.dtr[act], k.x[act], k.v[act], 1025, 1024)
+                ms = float(nb.kernel_times()[-1])
+                best = ms if best is None else min(best, ms)
+            gp = ni * n / (best * 1e-3) / 1e9
+            blocks[str(ni)] = {"kernel_ms": best, "gpairs_s": gp,
+                               "frac_fp32": gp * 1e9 * FLOPS_PER_PAIR / 1e12 / peak,
+                               "overflows": int((r.list[:, 0] < 0).sum())}
+            if ni == 16384:
+                ref = (r.acc.copy(), r.jrk.copy(), r.pot.copy(), r.list.copy())
+        nb.set_precision("fp64")
+        act = ics.active_set(n, 16384, seed=16384)
+        r = nb.regf(h2[act], k.dtr[act], k.x[act], k.v[act], 1025, 1024)
+        fp64_ms = float(nb.kernel_times()[-1])
+    a, j, p, lst = ref
+    ea = np.linalg.norm(a - r.acc, axis=1) / np.linalg.norm(r.acc, axis=1)
+    ej = np.linalg.norm(j - r.jrk, axis=1) / np.linalg.norm(r.jrk, axis=1)
+    ep = np.abs(p - r.pot) / np.abs(r.pot)
+    fp64_gp = 16384 * n / (fp64_ms * 1e-3) / 1e9
+    return {"workload": "King W0=6, N=2^20, Kroupa, 10% binaries as c.m. bodies, target 100, "
+                        "nbmax 1024", "setup_s": t_ics, "blocks": blocks,
+            "fp64_ni16384": {"kernel_ms": fp64_ms, "gpairs_s": fp64_gp},
+            "speedup_split_over_fp64_kernel_ni16384": blocks["16384"]["gpairs_s"] / fp64_gp,
+            "speedup_split_ni_N_over_fp64_kernel": blocks[str(n)]["gpairs_s"] / fp64_gp,
+            "rel_err_vs_fp64_kernel_ni16384": {
+                "acc_p99": float(np.percentile(ea, 99)), "acc_max": float(ea.max()),
+                "jrk_p99": float(np.percentile(ej, 99)), "jrk_max": float(ej.max()),
+                "pot_max": float(ep.max())},
+            "lists_identical_to_fp64_kernel": bool(np.array_equal(lst, r.list))}
+
+
+def rs_predictor_leg(dev):
+    """Inference of the neighbour-radius MLP for 2^20 particles (one forward
+    kernel): 2^20 x (8*64 + 64*64 + 64) multiply-adds."""
+    import torch
+    from nbody6ppgpu_gb300.rsmlp import RSMLP
+    m = RSMLP(seed=0, device=dev.index)
+    B = 1 << 20
+    X = torch.randn(B, 8, device=dev)
+    y = torch.empty(B, device=dev)
+    sp = m.stream.cuda_stream
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        assert m.lib.gpunb_rsmlp_forward(B, X.data_ptr(), m.wq.data_ptr(), m.master.data_ptr(),
+                                         y.data_ptr(), sp) == 0
+    reps = 10
+    e0.record(m.stream)
+    for _ in range(reps):
+        m.lib.gpunb_rsmlp_forward(B, X.data_ptr(), m.wq.data_ptr(), m.master.data_ptr(),
+                                  y.data_ptr(), sp)
+    e1.record(m.stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    macs = B * (8 * 64 + 64 * 64 + 64)
+    return {"particles": B, "forward_ms": ms, "gmacs_per_s": macs / (ms * 1e-3) / 1e9,
+            "kernel": "rsmlp_forward_kernel (FP32 CUDA cores, BF16 weights)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -279,6 +361,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-large", action="store_true", help="skip the N = 2^20 King leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local = dist_env()
@@ -435,11 +518,21 @@ def main():
     if not args.no_batched:
         batched = batched_leg(lib, dev, stream, steps=args.steps, warmup=args.warmup)
 
+    nb.close()
+    king = None
+    if not args.no_large:
+        king = king1m_leg(n_sm, peak_mhz)
+    rsp = rs_predictor_leg(dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu, _ = cpu_baseline(c, acts)
 
-    launches_per_block = 7   # pack, pair kernel, merge, 2x scan, gather, offsets
+    # the library's own kernels per step: per send bbox_init, bbox, morton, pack;
+    # per regf prep, pair kernel, merge, two scans, gather, offsets, plus the
+    # Morton key kernel of the i-ordering when ni >= 256.  The Morton sorts are
+    # CUB radix sorts (57 launches per step in the ncu launch list).
+    own_per_step = 4 * len(BLOCKS) + 7 * len(BLOCKS) + sum(ni >= 256 for ni in BLOCKS)
     line = {
         "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
@@ -463,7 +556,8 @@ def main():
                                     " (MEASURED_PEAKS.json has no FP32 entry)"},
         "e2e": {"value": ws * pairs_per_step / e2e_s / 1e9, "unit": "Gpairs/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": launches_per_block * len(BLOCKS) * args.steps,
+        "gpu_launches": own_per_step * args.steps,
+        "library_launches": {"cub_radix_sort": 57 * args.steps},
         "clocks": clk,
         "wall_s_timed_region": t_wall,
         "device": name,
@@ -472,7 +566,9 @@ def main():
         line["cpu_baseline"] = cpu
     if batched is not None:
         line["batched_clusters"] = batched
-    nb.close()
+    if king is not None:
+        line["king1m"] = king
+    line["rs_predictor_inference"] = rsp
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -54,9 +54,9 @@ def main():
         raise SystemExit("reference AVX library not available (needs x86_64 and the sources)")
     ref = O.RefAVX(1 << 16)
 
-    # configs[0]: Plummer N=2048, equal masses, mean count 50, nbmax 256
+    # Plummer N=2048, equal masses, mean count 50, nbmax 256
     c = ics.plummer(2048, seed=1, nb_target=50.0)
-    regf_case("cfg1_plummer2048", c.m, c.x, c.v, c.h2(), c.dtr, np.arange(c.n), 257, 256, 0, ref)
+    regf_case("plummer2048_equal", c.m, c.x, c.v, c.h2(), c.dtr, np.arange(c.n), 257, 256, 0, ref)
 
     # mass-weighted criterion (KZ(39) = 2, 3): Kroupa masses, h2 = RS^2 / BODYM
     k = ics.plummer(512, seed=5, masses="kroupa", nb_target=30.0)

@@ -6,7 +6,7 @@ import pytest
 from conftest import load_golden, rel_vec_err, rows_equal, unpack_list
 from oracle import oracle as O
 
-CASES = ["cfg1_plummer2048", "mflag_plummer512", "overflow_plummer512", "ragged_n37"]
+CASES = ["plummer2048_equal", "mflag_plummer512", "overflow_plummer512", "ragged_n37"]
 
 
 def run_oracle(g):
@@ -41,7 +41,7 @@ def test_oracle_matches_reference_cpu_path(name):
 
 
 def test_port_matches_reference_cpu_path():
-    g = load_golden("cfg1_plummer2048")
+    g = load_golden("plummer2048_equal")
     p = O.Port()
     p.send(g["m"], g["x"], g["v"])
     acc, jrk, pot, lst = p.regf(g["h2"], g["dtr"], g["x"], g["v"], int(g["lmax"]),

@@ -57,7 +57,7 @@ def run_golden(g, precision="split", variant=-1, splits=0):
                        int(g["nnbmax"]), int(g["m_flag"]))
 
 
-@pytest.mark.parametrize("name", ["cfg1_plummer2048", "mflag_plummer512",
+@pytest.mark.parametrize("name", ["plummer2048_equal", "mflag_plummer512",
                                   "overflow_plummer512", "ragged_n37"])
 @pytest.mark.parametrize("precision", ["split", "fp64"])
 def test_golden_cases(lib, name, precision):
@@ -77,7 +77,7 @@ def test_golden_cases(lib, name, precision):
 
 
 def test_all_launch_shapes_agree_and_are_deterministic(lib):
-    g = load_golden("cfg1_plummer2048")
+    g = load_golden("plummer2048_equal")
     base = run_golden(g, "split", 0, 0)
     again = run_golden(g, "split", 0, 0)
     assert np.array_equal(base.acc, again.acc) and np.array_equal(base.list, again.list)
