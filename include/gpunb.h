@@ -92,6 +92,16 @@ void gpunb_set_launch(int variant, int splits);
 int gpunb_num_variants(void);
 int gpunb_variant_info(int variant, int *ipt, int *warps_i, int *warps_j);
 
+/* How gpunb_send_/gpunb_regf_ move the caller's host arrays (no reference
+ * counterpart).  mode 1 (the default where supported): copy straight from and
+ * to the caller's pageable arrays and let the device write the LISTGP rows,
+ * which needs a device that reads pageable memory coherently through the
+ * host's page tables (Grace + Blackwell over NVLink-C2C); the environment
+ * variable GPUNB_HOST_DIRECT=0 turns it off at start-up.  mode 0: stage
+ * through pinned buffers and scatter the rows on the host.  Returns the mode
+ * in effect, or -1 without a device.  Results are identical in both modes. */
+int gpunb_set_host_path(int mode);
+
 /* Autotuner: time every shape for (nj, ni) on the current j-set with
  * synthetic i-particles drawn from it, keep the fastest, and cache it per
  * (nj bucket, ni bucket).  Returns the chosen variant; *splits, *ms out. */

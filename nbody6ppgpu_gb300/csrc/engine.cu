@@ -222,6 +222,12 @@ struct Engine {
   int last_variant = -1, last_splits = 0, last_gx = 0;
   std::map<long long, TuneEntry> tune;
   int autotune_on = 0;
+  // host arrays of the gpunb_* calls: 1 = copied straight from/to the
+  // caller's (pageable) arrays and list rows written by the device, which
+  // needs coherent access to pageable memory through the host's page tables
+  // (Grace + GB300 over NVLink-C2C); 0 = staged through pinned buffers
+  int host_direct = 0;
+  int host_direct_supported = 0;
   // profile counters (GPUNB_profile)
   double time_send = 0, time_grav = 0, time_reduce = 0, time_out = 0;
   long long num_inter = 0;
@@ -265,6 +271,16 @@ static bool devinit(int irank) {
   gethostname(host, sizeof(host) - 1);
   fprintf(stderr, "# GPU initialization - rank: %d; HOST %s; NGPU 1; device: %d %s\n", irank,
           host, dev, prop.name);
+  int pageable = 0, host_tables = 0;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                             dev) != cudaSuccess) {
+    cudaGetLastError();
+    pageable = host_tables = 0;
+  }
+  g.host_direct_supported = (pageable && host_tables) ? 1 : 0;
+  g.host_direct = g.host_direct_supported;
+  if (const char *p = getenv("GPUNB_HOST_DIRECT")) g.host_direct &= (atoi(p) != 0);
   g.devinit = true;
   if (const char *p = getenv("GPUNB_TUNE_CACHE")) gpunb_tune_load(p);
   if (const char *p = getenv("GPUNB_AUTOTUNE")) g.autotune_on = atoi(p);
@@ -381,11 +397,12 @@ static int plan_splits(int variant, int ni, int ntile, bool mflag) {
   return (int)s;
 }
 
-// Shapes measured on GB300 (N = 65536 Plummer, all shapes and split counts):
-// 4 warps along i with 128-bit j loads for blocks of 512 and more, one warp
-// of 32 i-particles with the j tile split over 8 warps below.
+// Shapes measured on GB300 (N = 65536 Plummer and N = 2^20 King, all shapes
+// and split counts): 4 warps along i reading 8 j per step (two 128-bit loads
+// per field, one warp vote per 8 j) for blocks of 512 and more, one warp of
+// 32 i-particles with the j tile split over 8 warps below.
 static void heuristic_plan(int ni, int ntile, bool mflag, int &variant, int &splits) {
-  variant = (ni >= 512) ? 4 : 2;
+  variant = (ni >= 512) ? 6 : 2;
   splits = plan_splits(variant, ni, ntile, mflag);
 }
 
@@ -559,18 +576,28 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   cudaStream_t st = g.stream;
   const bool mflag = m_flag != 0;
 
-  // stage inputs: h2 | dtr | x | v
+  // inputs: h2 | dtr | x | v
   const size_t in_doubles = (size_t)8 * ni;
-  if (!g.hin.ensure(in_doubles * sizeof(double)) || !g.iraw.ensure(in_doubles * sizeof(double)))
-    return;
-  double *hin = g.hin.as<double>();
-  hcopy(hin, h2, (size_t)ni * sizeof(double));
-  hcopy(hin + ni, dtr, (size_t)ni * sizeof(double));
-  hcopy(hin + 2 * (size_t)ni, xi, (size_t)ni * 3 * sizeof(double));
-  hcopy(hin + 5 * (size_t)ni, vi, (size_t)ni * 3 * sizeof(double));
+  if (!g.iraw.ensure(in_doubles * sizeof(double))) return;
   double *din = g.iraw.as<double>();
   CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
-  CUDA_OR(cudaMemcpyAsync(din, hin, in_doubles * sizeof(double), cudaMemcpyHostToDevice, st), );
+  if (g.host_direct) {
+    CUDA_OR(cudaMemcpyAsync(din, h2, (size_t)ni * sizeof(double), cudaMemcpyHostToDevice, st), );
+    CUDA_OR(cudaMemcpyAsync(din + ni, dtr, (size_t)ni * sizeof(double), cudaMemcpyHostToDevice,
+                            st), );
+    CUDA_OR(cudaMemcpyAsync(din + 2 * (size_t)ni, xi, (size_t)ni * 3 * sizeof(double),
+                            cudaMemcpyHostToDevice, st), );
+    CUDA_OR(cudaMemcpyAsync(din + 5 * (size_t)ni, vi, (size_t)ni * 3 * sizeof(double),
+                            cudaMemcpyHostToDevice, st), );
+  } else {
+    if (!g.hin.ensure(in_doubles * sizeof(double))) return;
+    double *hin = g.hin.as<double>();
+    hcopy(hin, h2, (size_t)ni * sizeof(double));
+    hcopy(hin + ni, dtr, (size_t)ni * sizeof(double));
+    hcopy(hin + 2 * (size_t)ni, xi, (size_t)ni * 3 * sizeof(double));
+    hcopy(hin + 5 * (size_t)ni, vi, (size_t)ni * 3 * sizeof(double));
+    CUDA_OR(cudaMemcpyAsync(din, hin, in_doubles * sizeof(double), cudaMemcpyHostToDevice, st), );
+  }
   ISet is;
   is.h2 = din;
   is.dtr = din + ni;
@@ -610,6 +637,23 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
                          : ((ni + regf_variant(variant).itile() - 1) / regf_variant(variant).itile()) *
                                regf_variant(variant).itile();
   if (finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, 0, st) != GPUNB_OK) return;
+  if (g.host_direct) {
+    // results straight into the caller's arrays; the device writes the rows
+    CUDA_OR(launch_list_rows(o.dense, o.off, o.btot, o.nnb, ni, lmax, list, st), );
+    CUDA_OR(cudaMemcpyAsync(acc, o.acc, (size_t)ni * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                            st), );
+    CUDA_OR(cudaMemcpyAsync(jrk, o.jrk, (size_t)ni * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                            st), );
+    CUDA_OR(cudaMemcpyAsync(pot, o.pot, (size_t)ni * sizeof(double), cudaMemcpyDeviceToHost, st), );
+    if (!g.hout.ensure(sizeof(int))) return;
+    int *h_err = g.hout.as<int>();
+    CUDA_OR(cudaMemcpyAsync(h_err, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
+    CUDA_OR(cudaStreamSynchronize(st), );
+    const double t_grav = wtime();
+    g.time_grav += t_grav - t_begin;
+    check_device_error(*h_err);
+    return;
+  }
   const size_t out_bytes = (size_t)7 * ni * sizeof(double) + (size_t)ni * sizeof(int);
   if (!g.hout.ensure(out_bytes + 2 * sizeof(int))) return;
   char *hob = g.hout.as<char>();
@@ -759,14 +803,22 @@ void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
   const double t0 = wtime();
   g.isend++;
   cudaStream_t st = g.stream;
-  double *h = g.hj.as<double>();
-  hcopy(h, mj, (size_t)n * sizeof(double));
-  hcopy(h + n, xj, (size_t)n * 3 * sizeof(double));
-  hcopy(h + 4 * (size_t)n, vj, (size_t)n * 3 * sizeof(double));
   CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
-  if (n > 0)
+  if (n > 0 && g.host_direct) {
+    double *d = g.jraw.as<double>();
+    CUDA_OR(cudaMemcpyAsync(d, mj, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st), );
+    CUDA_OR(cudaMemcpyAsync(d + n, xj, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                            st), );
+    CUDA_OR(cudaMemcpyAsync(d + 4 * (size_t)n, vj, (size_t)n * 3 * sizeof(double),
+                            cudaMemcpyHostToDevice, st), );
+  } else if (n > 0) {
+    double *h = g.hj.as<double>();
+    hcopy(h, mj, (size_t)n * sizeof(double));
+    hcopy(h + n, xj, (size_t)n * 3 * sizeof(double));
+    hcopy(h + 4 * (size_t)n, vj, (size_t)n * 3 * sizeof(double));
     CUDA_OR(cudaMemcpyAsync(g.jraw.p, h, (size_t)n * 7 * sizeof(double), cudaMemcpyHostToDevice,
                             st), );
+  }
   if (send_common(n, st) != GPUNB_OK) return;
   int herr = 0;
   CUDA_OR(cudaMemcpyAsync(&herr, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
@@ -869,6 +921,13 @@ int gpunb_variant_info(int variant, int *ipt, int *warps_i, int *warps_j) {
   if (warps_i) *warps_i = d.wi;
   if (warps_j) *warps_j = d.wj;
   return 0;
+}
+
+int gpunb_set_host_path(int mode) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!devinit(0)) return -1;
+  g.host_direct = (mode != 0) && g.host_direct_supported;
+  return g.host_direct;
 }
 
 void gpunb_set_timing(int flag) {

@@ -11,6 +11,7 @@ namespace gpunb {
 struct VariantDesc {
   int ipt, wi, wj;                       // i per thread, warps along i, warps along j
   int jv;                                // j read per shared-memory load (2 or 4)
+  int minb;                              // minimum resident blocks (register cap)
   int threads() const { return 32 * wi * wj; }
   int itile() const { return 32 * ipt * wi; }
 };
@@ -45,6 +46,11 @@ int list_scan_blocks(int ni);
 cudaError_t launch_list_scan(const int *rowlen, int ni, int *off, int *btot, cudaStream_t st);
 cudaError_t launch_list_gather(int *rows, int cap, const int *rowlen, const int *off,
                                const int *btot, int ni, int *dense, cudaStream_t st);
+// rows[i * lmax] = nnb[i], rows[i * lmax + 1 ..] = the i-th compacted sublist
+// (offsets as left by launch_list_scan: in-block off + block base boff);
+// rows may be host memory the device reaches coherently
+cudaError_t launch_list_rows(const int *dense, const int *off, const int *boff, const int *nnb,
+                             int ni, int lmax, int *rows, cudaStream_t st);
 cudaError_t launch_list_finalize_offsets(int *off, const int *btot, int ni, cudaStream_t st);
 
 // spatial (Morton) ordering

@@ -66,8 +66,14 @@ __device__ __forceinline__ unsigned long long spread3(unsigned int v) {
   return x;
 }
 
-// 48-bit Morton key (16 bits per axis inside the bounding box) and identity
-// values for the sort.
+// Morton keys: MORTON_BITS per axis inside the bounding box.  10 bits (a
+// 1024^3 grid) keep a tile of 128 bodies compact even in a 2^20-body core,
+// and the 30-bit key sorts in four 8-bit radix passes instead of six.
+constexpr int MORTON_BITS = 10;
+constexpr int KEY_BITS = 3 * MORTON_BITS;
+constexpr float MORTON_MAX = (float)((1 << MORTON_BITS) - 1);
+
+// Morton key and identity values for the sort.
 __global__ void morton_kernel(const double *__restrict__ x, int n, const int *__restrict__ bb,
                               unsigned long long *__restrict__ key, int *__restrict__ val) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -77,9 +83,9 @@ __global__ void morton_kernel(const double *__restrict__ x, int n, const int *__
   for (int c = 0; c < 3; ++c) {
     const float lo = ord2f(bb[c]), hi = ord2f(bb[3 + c]);
     const float span = hi - lo;
-    const float s = span > 0.f ? 65535.0f / span : 0.f;
+    const float s = span > 0.f ? MORTON_MAX / span : 0.f;
     float u = ((float)x[3 * i + c] - lo) * s;
-    u = fminf(fmaxf(u, 0.f), 65535.f);
+    u = fminf(fmaxf(u, 0.f), MORTON_MAX);
     q[c] = (unsigned int)u;
   }
   key[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
@@ -97,7 +103,7 @@ __device__ __forceinline__ int owner_of(const int *__restrict__ off, int nset, i
   return lo;
 }
 
-// Batched sets: key = (set index << 48) | Morton key, so that one stable sort
+// Batched sets: key = (set index << KEY_BITS) | Morton key, so that one stable sort
 // groups the bodies by set and orders each set along the curve.
 __global__ void morton_batch_kernel(const double *__restrict__ x, int n, const int *__restrict__ bb,
                                     const int *__restrict__ off, int nset,
@@ -109,13 +115,13 @@ __global__ void morton_batch_kernel(const double *__restrict__ x, int n, const i
   for (int c = 0; c < 3; ++c) {
     const float lo = ord2f(bb[c]), hi = ord2f(bb[3 + c]);
     const float span = hi - lo;
-    const float s = span > 0.f ? 65535.0f / span : 0.f;
+    const float s = span > 0.f ? MORTON_MAX / span : 0.f;
     float u = ((float)x[3 * i + c] - lo) * s;
-    u = fminf(fmaxf(u, 0.f), 65535.f);
+    u = fminf(fmaxf(u, 0.f), MORTON_MAX);
     q[c] = (unsigned int)u;
   }
   const unsigned long long set = (unsigned long long)owner_of(off, nset, i);
-  key[i] = (set << 48) | spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+  key[i] = (set << KEY_BITS) | spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
   val[i] = i;
 }
 
@@ -139,8 +145,8 @@ cudaError_t launch_order_batch(const double *x, int n, const int *bb, const int 
   morton_batch_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, n, bb, off, nset, keys, vals_alt);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  int end_bit = 48;
-  while ((1ll << (end_bit - 48)) < nset) ++end_bit;
+  int end_bit = KEY_BITS;
+  while ((1ll << (end_bit - KEY_BITS)) < nset) ++end_bit;
   size_t tb = temp_bytes;
   e = cub::DeviceRadixSort::SortPairs(temp, tb, keys, keys_alt, vals_alt, sorted, n, 0, end_bit,
                                       st);
@@ -150,8 +156,8 @@ cudaError_t launch_order_batch(const double *x, int n, const int *bb, const int 
 }
 
 size_t order_batch_temp_bytes(int n, int nset) {
-  int end_bit = 48;
-  while ((1ll << (end_bit - 48)) < nset) ++end_bit;
+  int end_bit = KEY_BITS;
+  while ((1ll << (end_bit - KEY_BITS)) < nset) ++end_bit;
   size_t tb = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tb, (const unsigned long long *)nullptr,
                                   (unsigned long long *)nullptr, (const int *)nullptr,
@@ -163,7 +169,7 @@ size_t order_temp_bytes(int n) {
   size_t tb = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tb, (const unsigned long long *)nullptr,
                                   (unsigned long long *)nullptr, (const int *)nullptr,
-                                  (int *)nullptr, n, 0, 48);
+                                  (int *)nullptr, n, 0, KEY_BITS);
   return tb;
 }
 
@@ -185,7 +191,8 @@ cudaError_t launch_order(const double *x, int n, const int *bb, unsigned long lo
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   size_t tb = temp_bytes;
-  return cub::DeviceRadixSort::SortPairs(temp, tb, keys, keys_alt, vals_alt, perm, n, 0, 48, st);
+  return cub::DeviceRadixSort::SortPairs(temp, tb, keys, keys_alt, vals_alt, perm, n, 0, KEY_BITS,
+                                         st);
 }
 
 }  // namespace gpunb

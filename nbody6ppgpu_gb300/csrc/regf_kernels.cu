@@ -198,61 +198,112 @@ __device__ __forceinline__ void record_neighbour(const RegfOut &out, int i, int 
   if (slot < out.cap) out.rows[(size_t)i * out.cap + slot] = j;
 }
 
-// Two j (one f32x2 lane pair) against one i: the whole per-pair computation.
+// Two j (one f32x2 lane pair) against one i.  The per-pair computation is
+// split in three so that the kernel can run the geometry of several lane
+// pairs, take one warp vote for the rare neighbour-candidate branch, and then
+// accumulate: the dependent chains of the lane pairs interleave instead of
+// being cut apart by a branch after every pair.
 struct JPair {
   f2 v[NFIELD];   // indexed by JField
 };
 
-template <bool MFLAG>
-__device__ __forceinline__ void pair2(const IState &I, float H, const JPair &p, f2 (&q)[NQ],
-                                      int jg0, int jbase, const JSet &js, const ISet &is,
-                                      const RegfOut &out) {
+struct PairGeo {
+  f2 dx, dy, dz, dvx, dvy, dvz, mn, r2, rv, z;
+};
+
+__device__ __forceinline__ void pair_geo(const IState &I, const JPair &p, PairGeo &g) {
   // double-single coordinate difference: (hi_j - hi_i) + (lo_j - lo_i)
-  const f2 dx = add2(add2(p.v[F_XH], I.nxh), add2(p.v[F_XL], I.nxl));
-  const f2 dy = add2(add2(p.v[F_YH], I.nyh), add2(p.v[F_YL], I.nyl));
-  const f2 dz = add2(add2(p.v[F_ZH], I.nzh), add2(p.v[F_ZL], I.nzl));
-  const f2 dvx = add2(p.v[F_VX], I.nvx);
-  const f2 dvy = add2(p.v[F_VY], I.nvy);
-  const f2 dvz = add2(p.v[F_VZ], I.nvz);
-  const f2 mn = p.v[F_MN];
-  const f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-  const f2 rv = fma2(dz, dvz, fma2(dy, dvy, mul2(dx, dvx)));
+  g.dx = add2(add2(p.v[F_XH], I.nxh), add2(p.v[F_XL], I.nxl));
+  g.dy = add2(add2(p.v[F_YH], I.nyh), add2(p.v[F_YL], I.nyl));
+  g.dz = add2(add2(p.v[F_ZH], I.nzh), add2(p.v[F_ZL], I.nzl));
+  g.dvx = add2(p.v[F_VX], I.nvx);
+  g.dvy = add2(p.v[F_VY], I.nvy);
+  g.dvz = add2(p.v[F_VZ], I.nvz);
+  g.mn = p.v[F_MN];
+  g.r2 = fma2(g.dz, g.dz, fma2(g.dy, g.dy, mul2(g.dx, g.dx)));
+  g.rv = fma2(g.dz, g.dvz, fma2(g.dy, g.dvy, mul2(g.dx, g.dvx)));
   // rsqrt estimate + one Newton step, scaled: z = y0 (x y0^2 - 3) = -2/r
-  const f2 y0 = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-  f2 z = mul2(y0, fma2(mul2(r2, y0), y0, mk2(-3.0f)));
-  const bool c0 = r2.x < H, c1 = r2.y < H;
-  if (__any_sync(0xffffffffu, c0 | c1)) {
-    // perm maps a tile slot to the index into the sent arrays; padding slots
-    // hold -1 and never qualify.  Ids are reported relative to the owning
-    // j-set (jbase), in the caller's numbering.
-    if (c0) {
-      const int jo = js.perm[jg0];
-      if (jo >= 0 &&
-          decide_pair<MFLAG>(I, is, js, jo, dx.x, dy.x, dz.x, dvx.x, dvy.x, dvz.x, r2.x, mn.x)) {
-        record_neighbour(out, I.i, jo - jbase);
-        z.x = 0.f;
-      }
-    }
-    if (c1) {
-      const int jo = js.perm[jg0 + 1];
-      if (jo >= 0 &&
-          decide_pair<MFLAG>(I, is, js, jo, dx.y, dy.y, dz.y, dvx.y, dvy.y, dvz.y, r2.y, mn.y)) {
-        record_neighbour(out, I.i, jo - jbase);
-        z.y = 0.f;
-      }
+  const f2 y0 = make_float2(rsqrtf(g.r2.x), rsqrtf(g.r2.y));
+  g.z = mul2(y0, fma2(mul2(g.r2, y0), y0, mk2(-3.0f)));
+}
+
+__device__ __forceinline__ bool pair_maybe(const PairGeo &g, float H) {
+  return (g.r2.x < H) | (g.r2.y < H);
+}
+
+// Candidates of one lane pair (rare path): decide, record, and drop the
+// neighbours from the sums.  perm maps a tile slot to the index into the sent
+// arrays; padding slots hold -1 and never qualify.  Ids are reported relative
+// to the owning j-set (jbase), in the caller's numbering.
+template <bool MFLAG>
+__device__ __forceinline__ void pair_candidates(const IState &I, float H, PairGeo &g, int jg0,
+                                                int jbase, const JSet &js, const ISet &is,
+                                                const RegfOut &out) {
+  if (g.r2.x < H) {
+    const int jo = js.perm[jg0];
+    if (jo >= 0 && decide_pair<MFLAG>(I, is, js, jo, g.dx.x, g.dy.x, g.dz.x, g.dvx.x, g.dvy.x,
+                                      g.dvz.x, g.r2.x, g.mn.x)) {
+      record_neighbour(out, I.i, jo - jbase);
+      g.z.x = 0.f;
     }
   }
-  const f2 mr = mul2(mn, z);            // m/r
-  const f2 z2 = mul2(z, z);             // 4/r^2
+  if (g.r2.y < H) {
+    const int jo = js.perm[jg0 + 1];
+    if (jo >= 0 && decide_pair<MFLAG>(I, is, js, jo, g.dx.y, g.dy.y, g.dz.y, g.dvx.y, g.dvy.y,
+                                      g.dvz.y, g.r2.y, g.mn.y)) {
+      record_neighbour(out, I.i, jo - jbase);
+      g.z.y = 0.f;
+    }
+  }
+}
+
+__device__ __forceinline__ void pair_acc(const PairGeo &g, f2 (&q)[NQ]) {
+  const f2 mr = mul2(g.mn, g.z);        // m/r
+  const f2 z2 = mul2(g.z, g.z);         // 4/r^2
   const f2 mr3 = mul2(mr, z2);          // 4 m/r^3
   q[6] = add2(q[6], mr);
-  q[0] = fma2(mr3, dx, q[0]);
-  q[1] = fma2(mr3, dy, q[1]);
-  q[2] = fma2(mr3, dz, q[2]);
-  const f2 al = mul2(mul2(rv, z2), mk2(-0.75f));   // -3 (r.v)/r^2
-  q[3] = fma2(mr3, fma2(al, dx, dvx), q[3]);
-  q[4] = fma2(mr3, fma2(al, dy, dvy), q[4]);
-  q[5] = fma2(mr3, fma2(al, dz, dvz), q[5]);
+  q[0] = fma2(mr3, g.dx, q[0]);
+  q[1] = fma2(mr3, g.dy, q[1]);
+  q[2] = fma2(mr3, g.dz, q[2]);
+  const f2 al = mul2(mul2(g.rv, z2), mk2(-0.75f));   // -3 (r.v)/r^2
+  q[3] = fma2(mr3, fma2(al, g.dx, g.dvx), q[3]);
+  q[4] = fma2(mr3, fma2(al, g.dy, g.dvy), q[4]);
+  q[5] = fma2(mr3, fma2(al, g.dz, g.dvz), q[5]);
+}
+
+// Four j (two lane pairs) against one i, one warp vote for both.
+template <bool MFLAG>
+__device__ __forceinline__ void pair4(const IState &I, float H, const JPair &p0, const JPair &p1,
+                                      f2 (&q)[NQ], int jg0, int jbase, const JSet &js,
+                                      const ISet &is, const RegfOut &out) {
+  PairGeo g0, g1;
+  pair_geo(I, p0, g0);
+  pair_geo(I, p1, g1);
+  if (__any_sync(0xffffffffu, pair_maybe(g0, H) | pair_maybe(g1, H))) {
+    pair_candidates<MFLAG>(I, H, g0, jg0, jbase, js, is, out);
+    pair_candidates<MFLAG>(I, H, g1, jg0 + 2, jbase, js, is, out);
+  }
+  pair_acc(g0, q);
+  pair_acc(g1, q);
+}
+
+// Eight j (four lane pairs) against one i, one warp vote for all.
+template <bool MFLAG>
+__device__ __forceinline__ void pair8(const IState &I, float H, const JPair (&p)[4], f2 (&q)[NQ],
+                                      int jg0, int jbase, const JSet &js, const ISet &is,
+                                      const RegfOut &out) {
+  PairGeo g[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) pair_geo(I, p[u], g[u]);
+  const bool any = pair_maybe(g[0], H) | pair_maybe(g[1], H) | pair_maybe(g[2], H) |
+                   pair_maybe(g[3], H);
+  if (__any_sync(0xffffffffu, any)) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      pair_candidates<MFLAG>(I, H, g[u], jg0 + 2 * u, jbase, js, is, out);
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) pair_acc(g[u], q);
 }
 
 // ---------------------------------------------------------------------------
@@ -277,14 +328,15 @@ struct RegfWork {
   int n_items;
 };
 
-template <int IPT, int WI, int WJ, int JV, bool MFLAG>
-__global__ void __launch_bounds__(32 * WI * WJ)
+template <int IPT, int WI, int WJ, int JV, bool MFLAG, int MINB>
+__global__ void __launch_bounds__(32 * WI * WJ, MINB)
     regf_ds_kernel(const JSet js, const ISet is, const RegfOut out, const RegfWork w) {
   constexpr int NT = 32 * WI * WJ;
   constexpr int NW = NT / 32;
   constexpr int ITILE = 32 * IPT * WI;
   constexpr int JW = JT / WJ;
-  static_assert(JW % JV == 0 && (JV == 2 || JV == 4), "j per warp must be a multiple of JV");
+  static_assert(JW % JV == 0 && JW % 4 == 0 && (JV == 2 || JV == 4 || JV == 8),
+                "j per warp must be a multiple of JV and of 4");
   extern __shared__ __align__(128) float smem[];
   float *ring = smem;                                   // NSTAGE * TILE_FLOATS
   float *ffs = smem + NSTAGE * TILE_FLOATS;             // [2][NQ][IPT][NT] float-float
@@ -365,26 +417,38 @@ __global__ void __launch_bounds__(32 * WI * WJ)
         const float base = I[k].dv * (I[k].va + vmax);
         const float b = MFLAG ? fmaf(I[k].s, smax, base) : I[k].s + base;
         const float H = (I[k].s < 0.f) ? -1.0f : b * b;
-        if (JV == 2) {
-#pragma unroll 2
-          for (int jj = jbeg; jj < jbeg + JW; jj += 2) {
-            JPair p;
+        if (JV == 8) {
+          for (int jj = jbeg; jj < jbeg + JW; jj += 8) {
+            JPair p[4];
 #pragma unroll
-            for (int f = 0; f < NFIELD; ++f) p.v[f] = *(const f2 *)(T + f * JT + jj);
-            pair2<MFLAG>(I[k], H, p, q[k], (t0 + t) * JT + jj, jbase, js, is, out);
+            for (int f = 0; f < NFIELD; ++f) {
+              const float4 u = *(const float4 *)(T + f * JT + jj);
+              const float4 w4 = *(const float4 *)(T + f * JT + jj + 4);
+              p[0].v[f] = make_float2(u.x, u.y);
+              p[1].v[f] = make_float2(u.z, u.w);
+              p[2].v[f] = make_float2(w4.x, w4.y);
+              p[3].v[f] = make_float2(w4.z, w4.w);
+            }
+            pair8<MFLAG>(I[k], H, p, q[k], (t0 + t) * JT + jj, jbase, js, is, out);
           }
-        } else {
-          for (int jj = jbeg; jj < jbeg + JW; jj += 4) {
-            JPair p0, p1;
+        } else
+        for (int jj = jbeg; jj < jbeg + JW; jj += 4) {
+          JPair p0, p1;
+          if (JV == 2) {
+#pragma unroll
+            for (int f = 0; f < NFIELD; ++f) {
+              p0.v[f] = *(const f2 *)(T + f * JT + jj);
+              p1.v[f] = *(const f2 *)(T + f * JT + jj + 2);
+            }
+          } else {
 #pragma unroll
             for (int f = 0; f < NFIELD; ++f) {
               const float4 u = *(const float4 *)(T + f * JT + jj);
               p0.v[f] = make_float2(u.x, u.y);
               p1.v[f] = make_float2(u.z, u.w);
             }
-            pair2<MFLAG>(I[k], H, p0, q[k], (t0 + t) * JT + jj, jbase, js, is, out);
-            pair2<MFLAG>(I[k], H, p1, q[k], (t0 + t) * JT + jj + 2, jbase, js, is, out);
           }
+          pair4<MFLAG>(I[k], H, p0, p1, q[k], (t0 + t) * JT + jj, jbase, js, is, out);
         }
       }
       // fold the tile's FP32 chunk sums into the float-float accumulators
@@ -769,8 +833,13 @@ __global__ void list_finalize_offsets_kernel(int *off, const int *btot, int ni, 
   if (i == 0) off[ni] = btot[nb];
 }
 
-static const VariantDesc kVariants[] = {{2, 4, 1, 2}, {2, 2, 2, 2}, {1, 1, 8, 2}, {1, 4, 1, 2},
-                                        {1, 4, 1, 4}, {1, 8, 1, 2}};
+// ipt, warps along i, warps along j, j per load, minimum resident blocks per
+// SM (the register cap, 65536 / (threads x blocks) per thread, set to what
+// each shape reaches unconstrained: a tighter cap, e.g. 80 registers for six
+// blocks of variant 4, spills and measured slower)
+static const VariantDesc kVariants[] = {{2, 4, 1, 2, 3}, {2, 2, 2, 2, 3}, {1, 1, 8, 2, 2},
+                                        {1, 4, 1, 2, 5}, {1, 4, 1, 4, 5}, {1, 8, 1, 2, 2},
+                                        {1, 4, 1, 8, 4}};
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 
 int regf_num_variants() { return kNumVariants; }
@@ -783,14 +852,18 @@ size_t regf_ds_smem(int v) {
 
 typedef void (*regf_fn)(JSet, ISet, RegfOut, RegfWork);
 static regf_fn regf_kernel_ptr(int v, bool mflag) {
+#define GPUNB_RK(a, b, c, d, e) \
+  (mflag ? regf_ds_kernel<a, b, c, d, true, e> : regf_ds_kernel<a, b, c, d, false, e>)
   switch (v) {
-    case 0: return mflag ? regf_ds_kernel<2, 4, 1, 2, true> : regf_ds_kernel<2, 4, 1, 2, false>;
-    case 1: return mflag ? regf_ds_kernel<2, 2, 2, 2, true> : regf_ds_kernel<2, 2, 2, 2, false>;
-    case 2: return mflag ? regf_ds_kernel<1, 1, 8, 2, true> : regf_ds_kernel<1, 1, 8, 2, false>;
-    case 3: return mflag ? regf_ds_kernel<1, 4, 1, 2, true> : regf_ds_kernel<1, 4, 1, 2, false>;
-    case 4: return mflag ? regf_ds_kernel<1, 4, 1, 4, true> : regf_ds_kernel<1, 4, 1, 4, false>;
-    default: return mflag ? regf_ds_kernel<1, 8, 1, 2, true> : regf_ds_kernel<1, 8, 1, 2, false>;
+    case 0: return GPUNB_RK(2, 4, 1, 2, 3);
+    case 1: return GPUNB_RK(2, 2, 2, 2, 3);
+    case 2: return GPUNB_RK(1, 1, 8, 2, 2);
+    case 3: return GPUNB_RK(1, 4, 1, 2, 5);
+    case 4: return GPUNB_RK(1, 4, 1, 4, 5);
+    case 5: return GPUNB_RK(1, 8, 1, 2, 2);
+    default: return GPUNB_RK(1, 4, 1, 8, 4);
   }
+#undef GPUNB_RK
 }
 
 int regf_ds_blocks_per_sm(int v, bool mflag) {
@@ -844,7 +917,9 @@ cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const IS
 cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *perm,
                               const int *cnt, int nnbmax, double *acc, double *jrk, double *pot,
                               int *nnb, int *rowlen, cudaStream_t st) {
-  if (S >= 32)
+  // many splits of a small block: a block per i-slot (threads over splits);
+  // otherwise a thread per i-slot, whose reads are coalesced across the warp
+  if (S >= 32 && ni < 8192)
     regf_merge_wide_kernel<<<ni, MERGE_THREADS, 0, st>>>(part, S, ni, ni_pad, perm, cnt, nnbmax,
                                                          acc, jrk, pot, nnb, rowlen);
   else
@@ -882,6 +957,36 @@ cudaError_t launch_list_gather(int *rows, int cap, const int *rowlen, const int 
                                const int *btot, int ni, int *dense, cudaStream_t st) {
   list_gather_kernel<<<(ni + GATHER_WARPS - 1) / GATHER_WARPS, 32 * GATHER_WARPS, 0, st>>>(
       rows, cap, rowlen, off, btot, ni, dense);
+  return cudaGetLastError();
+}
+
+// Host-visible rows (the gpunb_regf_ LISTGP layout) written by the device:
+// one warp per row, row[0] = the signed count, row[1..count] = the ids of the
+// compacted list (row i starts at off[i] + boff[i / SCAN_ITEMS], the scan's
+// in-block offset plus its block's base).  `rows` is the caller's host array, reached through the
+// coherent host-memory path (the caller checks that the device may access
+// pageable memory through the host's page tables before using this).
+__global__ void list_rows_kernel(const int *__restrict__ dense, const int *__restrict__ off,
+                                 const int *__restrict__ boff, const int *__restrict__ nnb, int ni,
+                                 int lmax, int *__restrict__ rows) {
+  const int lane = threadIdx.x & 31;
+  const int i = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (i >= ni) return;
+  const int c = nnb[i];
+  int *row = rows + (size_t)i * lmax;
+  if (lane == 0) row[0] = c;
+  if (c > 0) {
+    const int *src = dense + off[i] + boff[i / SCAN_ITEMS];
+    for (int u = lane; u < c; u += 32) row[1 + u] = src[u];
+  }
+}
+
+cudaError_t launch_list_rows(const int *dense, const int *off, const int *boff, const int *nnb,
+                             int ni, int lmax, int *rows, cudaStream_t st) {
+  if (ni <= 0) return cudaSuccess;
+  const int threads = 256;
+  const long long blocks = ((long long)ni * 32 + threads - 1) / threads;
+  list_rows_kernel<<<(unsigned)blocks, threads, 0, st>>>(dense, off, boff, nnb, ni, lmax, rows);
   return cudaGetLastError();
 }
 

@@ -71,6 +71,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "gpunb_tune_load": ([C.c_char_p], C.c_int),
         "gpunb_tune_save": ([C.c_char_p], C.c_int),
         "gpunb_set_timing": ([C.c_int], None),
+        "gpunb_set_host_path": ([C.c_int], C.c_int),
         "gpunb_kernel_times": ([_P(C.c_float), C.c_int], C.c_int),
         "gpunb_last_kernel_ms": ([], C.c_float),
         "gpunb_last_launch": ([ip, ip, ip], None),
@@ -184,6 +185,12 @@ class GpuNb:
         v, s, g = C.c_int(), C.c_int(), C.c_int()
         self.lib.gpunb_last_launch(C.byref(v), C.byref(s), C.byref(g))
         return v.value, s.value, g.value
+
+    def set_host_path(self, direct: bool) -> int:
+        """1: copy straight from/to the caller's arrays, rows written by the
+        device (where the device reads pageable memory coherently); 0: staged
+        through pinned buffers.  Returns the mode in effect."""
+        return self.lib.gpunb_set_host_path(1 if direct else 0)
 
     def set_timing(self, on: bool) -> None:
         self.lib.gpunb_set_timing(1 if on else 0)

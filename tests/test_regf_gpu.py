@@ -202,3 +202,29 @@ def test_gpupot_coincident_and_large(lib):
     o = np.array([O.pot_fp64(m, x, int(i) + 1, 1)[0] for i in samp])
     assert (np.abs(p[samp] - o) / o).max() < 1e-6
     assert np.isfinite(p[10]) and np.isfinite(p[11])
+
+
+def test_host_paths_identical(lib, plummer64k):
+    """Direct host arrays (device writes the rows) and pinned staging give the
+    same bytes, including overflow rows and blocks above the host-scatter
+    threshold."""
+    c = plummer64k
+    g = load_golden("overflow_plummer512")
+    ii = g["ii"]
+    act = ics.active_set(c.n, 16384, seed=3)
+    h2 = c.h2()
+    cases = [(g["m"], g["x"], g["v"], g["h2"], g["dtr"], g["x"][ii], g["v"][ii],
+              int(g["lmax"]), int(g["nnbmax"])),
+             (c.m, c.x, c.v, h2[act], c.dtr[act], c.x[act], c.v[act], 257, 256)]
+    with GpuNb(c.n) as nb:
+        for m, x, v, hh, dtr, xi, vi, lmax, nnbmax in cases:
+            out = []
+            for mode in (1, 0):
+                nb.set_host_path(bool(mode))
+                nb.send(m, x, v)
+                out.append(nb.regf(hh, dtr, xi, vi, lmax, nnbmax))
+            nb.set_host_path(True)
+            a, b = out
+            assert np.array_equal(a.list, b.list)
+            assert np.array_equal(a.acc, b.acc) and np.array_equal(a.jrk, b.jrk)
+            assert np.array_equal(a.pot, b.pot)
