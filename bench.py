@@ -531,7 +531,7 @@ def main():
     # the library's own kernels per step: per send bbox_init, bbox, morton, pack;
     # per regf prep, pair kernel, merge, two scans, gather, offsets, plus the
     # Morton key kernel of the i-ordering when ni >= 256.  The Morton sorts are
-    # CUB radix sorts (57 launches per step in the ncu launch list).
+    # CUB radix sorts (43 launches per step in the ncu launch list).
     own_per_step = 4 * len(BLOCKS) + 7 * len(BLOCKS) + sum(ni >= 256 for ni in BLOCKS)
     line = {
         "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": ws,
@@ -557,7 +557,7 @@ def main():
         "e2e": {"value": ws * pairs_per_step / e2e_s / 1e9, "unit": "Gpairs/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": own_per_step * args.steps,
-        "library_launches": {"cub_radix_sort": 57 * args.steps},
+        "library_launches": {"cub_radix_sort": 43 * args.steps},
         "clocks": clk,
         "wall_s_timed_region": t_wall,
         "device": name,
