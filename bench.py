@@ -323,6 +323,63 @@ def king1m_leg(n_sm: int, peak_mhz: float):
             "lists_identical_to_fp64_kernel": bool(np.array_equal(lst, r.list))}
 
 
+def irregular_leg(c, h2, lists_src, cpu: bool):
+    """Irregular (neighbour) force through the irr_simd_* ABI (the drop-in
+    for src/Main/irr.avx.cpp): the bench's Plummer N = 65536 with the
+    neighbour lists of its ni = 65536 regular block (the particle itself
+    removed), predictor state from that block's regular force, blocks of
+    1024, 16384 and 65536 particles at a common time.  Unit: listed pairs."""
+    from nbody6ppgpu_gb300.irr import IrrSimd
+    n = c.n
+    lmax = lists_src.shape[1]
+    lists = np.zeros_like(lists_src)
+    for i in range(n):
+        cnt = max(int(lists_src[i, 0]), 0)
+        ids = lists_src[i, 1:1 + cnt]
+        ids = ids[ids != i]
+        lists[i, 0] = len(ids)
+        lists[i, 1:1 + len(ids)] = ids
+    rng = np.random.default_rng(7)
+    f = rng.normal(0.0, 0.5, (n, 3))
+    fdot = rng.normal(0.0, 0.5, (n, 3))
+    ti = 1.0
+    t0 = ti - rng.uniform(0.0, 2e-3, n)
+    out = {"workload": "Plummer N=65536 (the bench cluster), lists of its regular block, "
+                       "host ABI (irr_simd_firr_vec_)", "blocks": {}}
+    with IrrSimd(n, lmax) as irr:
+        irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
+        irr.set_lists(lists)
+        for ni in (1024, 16384, n):
+            act = rng.permutation(n)[:ni]
+            pairs = int(lists[act, 0].sum())
+            irr.firr(ti, act)
+            best = 1e9
+            for _ in range(5):
+                t = time.perf_counter()
+                a, j, nid = irr.firr(ti, act)
+                best = min(best, time.perf_counter() - t)
+            out["blocks"][str(ni)] = {"pairs": pairs, "ms": best * 1e3,
+                                      "gpairs_s": pairs / best / 1e9}
+    if cpu:
+        from oracle import oracle as O
+        act = rng.permutation(n)[:16384]
+        O.irr_fp64(c.x, c.v, f, fdot, c.m, t0, lists, ti, act)
+        t = time.perf_counter()
+        oa, oj, on = O.irr_fp64(c.x, c.v, f, fdot, c.m, t0, lists, ti, act)
+        dt = time.perf_counter() - t
+        with IrrSimd(n, lmax) as irr:
+            irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
+            irr.set_lists(lists)
+            a, j, nid = irr.firr(ti, act)
+        ok = np.linalg.norm(oa, axis=1) > 0
+        ea = np.linalg.norm(a[ok] - oa[ok], axis=1) / np.linalg.norm(oa[ok], axis=1)
+        out["cpu_fp64_oracle"] = {"gpairs_s": int(lists[act, 0].sum()) / dt / 1e9,
+                                  "ni": 16384, "cores": O.num_threads()}
+        out["max_rel_err_vs_fp64_oracle"] = float(ea.max())
+        out["nnbid_identical"] = bool(np.array_equal(nid, on))
+    return out
+
+
 def rs_predictor_leg(dev):
     """Inference of the neighbour-radius MLP for 2^20 particles (one forward
     kernel): 2^20 x (8*64 + 64*64 + 64) multiply-adds."""
@@ -362,6 +419,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-large", action="store_true", help="skip the N = 2^20 King leg")
+    ap.add_argument("--no-irregular", action="store_true", help="skip the irregular-force leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local = dist_env()
@@ -519,6 +577,11 @@ def main():
         batched = batched_leg(lib, dev, stream, steps=args.steps, warmup=args.warmup)
 
     nb.close()
+    irr = None
+    if not args.no_irregular:
+        lists_by_particle = np.zeros_like(outs[65536].list)
+        lists_by_particle[acts[65536]] = outs[65536].list
+        irr = irregular_leg(c, h2, lists_by_particle, cpu=(rank == 0 and not args.no_cpu_baseline))
     king = None
     if not args.no_large:
         king = king1m_leg(n_sm, peak_mhz)
@@ -568,6 +631,8 @@ def main():
         line["batched_clusters"] = batched
     if king is not None:
         line["king1m"] = king
+    if irr is not None:
+        line["irregular"] = irr
     line["rs_predictor_inference"] = rsp
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -50,6 +50,10 @@ static void fail(int code, const char *fmt, ...) {
   if (g_abort_on_error) abort();
 }
 
+// errors raised by the other translation units of the library (irregular
+// force): same record, same abort policy
+void report_failure(int code, const char *msg) { fail(code, "%s", msg); }
+
 #define CUDA_OR(call, ret)                                                          \
   do {                                                                              \
     cudaError_t e_ = (call);                                                        \

@@ -1,0 +1,127 @@
+"""Python binding of the GPU irregular-force library (include/irr.h), the
+drop-in for NBODY6++'s SIMD library src/Main/irr.avx.cpp.
+
+    with IrrSimd(nmax, lmax) as irr:
+        irr.set_jp(x0, v0, f, fdot, m, t0)        # all particles (or a subset)
+        irr.set_lists(lists)                      # rows: count, 0-based ids
+        acc, jrk, nnbid = irr.firr(ti, active)    # 0-based active indices
+
+The calls go through the reference's own Fortran-style entry points
+(1-based addresses and ids), one particle per set call, as the Fortran
+integrator makes them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .gpunb import GpunbError, _check, load
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+
+
+def _dp(a):
+    return a.ctypes.data_as(_D)
+
+
+def _bind(lib):
+    for name, args, res in [
+        ("irr_simd_open_", [_I, _I, _I], None),
+        ("irr_simd_close_", [_I], None),
+        ("irr_simd_profile_", [_I], None),
+        ("irr_simd_set_jp_", [_I, _D, _D, _D, _D, _D, _D], None),
+        ("irr_simd_set_list_", [_I, _I], None),
+        ("irr_simd_firr_vec_", [_D, _I, _I, _D, _D, _I], None),
+        ("irr_set_host_path", [C.c_int], C.c_int),
+    ]:
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+
+
+class IrrSimd:
+    """One open irregular-force library (the process-wide state of the C ABI)."""
+
+    def __init__(self, nmax: int, lmax: int, rank: int = 0):
+        self.lib = load()
+        _bind(self.lib)
+        self.nmax, self.lmax = nmax, lmax
+        self.lib.irr_simd_open_(C.byref(C.c_int(nmax)), C.byref(C.c_int(lmax)),
+                                C.byref(C.c_int(rank)))
+        _check(self.lib)
+
+    def close(self) -> None:
+        self.lib.irr_simd_close_(C.byref(C.c_int(0)))
+        _check(self.lib)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_host_path(self, direct: bool) -> int:
+        return self.lib.irr_set_host_path(1 if direct else 0)
+
+    def set_jp(self, x0, v0, f, fdot, m, t0, idx=None) -> None:
+        """irr_simd_set_jp_ for the particles idx (0-based; default all):
+        position, velocity, F (force/2), FDOT (derivative/6), mass, time."""
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        v0 = np.ascontiguousarray(v0, dtype=np.float64)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        fdot = np.ascontiguousarray(fdot, dtype=np.float64)
+        m = np.ascontiguousarray(m, dtype=np.float64)
+        t0 = np.ascontiguousarray(t0, dtype=np.float64)
+        idx = range(len(m)) if idx is None else idx
+        fn = self.lib.irr_simd_set_jp_
+        a = C.c_int(0)
+        mm = C.c_double(0.0)
+        tt = C.c_double(0.0)
+        for i in idx:
+            i = int(i)
+            a.value = i + 1
+            mm.value = float(m[i])
+            tt.value = float(t0[i])
+            fn(C.byref(a), _dp(x0[i]), _dp(v0[i]), _dp(f[i]), _dp(fdot[i]), C.byref(mm),
+               C.byref(tt))
+        _check(self.lib)
+
+    def set_lists(self, lists, idx=None) -> None:
+        """irr_simd_set_list_ for the rows idx (default all) of lists[n][lmax]
+        (count, then 0-based ids), passed as Fortran LIST rows."""
+        lists = np.asarray(lists, dtype=np.int32)
+        idx = range(lists.shape[0]) if idx is None else idx
+        fn = self.lib.irr_simd_set_list_
+        a = C.c_int(0)
+        for i in idx:
+            i = int(i)
+            row = lists[i]
+            c = int(row[0])
+            buf = np.empty(1 + c, dtype=np.int32)
+            buf[0] = c
+            buf[1:] = row[1:1 + c] + 1
+            a.value = i + 1
+            fn(C.byref(a), buf.ctypes.data_as(_I))
+        _check(self.lib)
+
+    def firr(self, ti: float, active) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """Irregular force, its derivative and the nearest neighbour (1-based,
+        0 for an empty list) of the 0-based particles `active` at time ti."""
+        addr = np.ascontiguousarray(np.asarray(active) + 1, dtype=np.int32)
+        ni = addr.shape[0]
+        acc = np.zeros((max(ni, 1), 3))
+        jrk = np.zeros((max(ni, 1), 3))
+        nid = np.zeros(max(ni, 1), dtype=np.int32)
+        self.lib.irr_simd_firr_vec_(C.byref(C.c_double(ti)), C.byref(C.c_int(ni)),
+                                    addr.ctypes.data_as(_I), _dp(acc), _dp(jrk),
+                                    nid.ctypes.data_as(_I))
+        _check(self.lib)
+        return acc[:ni], jrk[:ni], nid[:ni]
+
+    def profile(self) -> None:
+        self.lib.irr_simd_profile_(C.byref(C.c_int(0)))
+
+
+__all__ = ["IrrSimd", "GpunbError"]

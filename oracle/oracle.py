@@ -8,6 +8,8 @@ module, as the checker or the timed CPU baseline; the product never imports it.
     Port            portable FP32 restatement of src/Main/reg.avx.cpp / pot.avx.cpp
     RefAVX          the reference's own reg.avx.cpp / pot.avx.cpp compiled from
                     its sources into oracle/_ref (x86_64 hosts only)
+    irr_fp64(...)   FP64 irregular force of src/Main/irr.avx.cpp (irr_fp64.c)
+    RefIrrAVX       the reference's own irr.avx.cpp compiled into oracle/_ref
 """
 from __future__ import annotations
 
@@ -39,7 +41,8 @@ def lib() -> C.CDLL:
     global _lib
     if _lib is None:
         path = HERE / "liboracle.so"
-        srcs = [HERE / "oracle_fp64.c", HERE / "port_fp32.c", HERE / "Makefile"]
+        srcs = [HERE / "oracle_fp64.c", HERE / "port_fp32.c", HERE / "irr_fp64.c",
+                HERE / "Makefile"]
         if not path.exists() or any(s.stat().st_mtime > path.stat().st_mtime for s in srcs):
             build()
         _lib = C.CDLL(str(path))
@@ -51,6 +54,8 @@ def lib() -> C.CDLL:
                                         _I, C.c_int]
         _lib.port_pot_fp32.argtypes = [C.c_int, C.c_int, C.c_int, _D, _D, _D]
         _lib.oracle_num_threads.restype = C.c_int
+        _lib.oracle_irr_fp64.argtypes = [C.c_int, _D, _D, _D, _D, _D, _D, C.c_int, _I, C.c_double,
+                                         C.c_int, _I, _D, _D, _I]
     return _lib
 
 
@@ -184,3 +189,72 @@ class RefAVX:
         a = [C.c_int(0), C.c_int(istart), C.c_int(ni), C.c_int(n)]
         self.potlib.gpupot_(*[C.byref(v) for v in a], _dp(mp), _dp(xp), _dp(pot))
         return pot[istart - 1:istart - 1 + ni]
+
+
+def irr_fp64(x0, v0, a2, j6, m, t0, lists, ti, addr):
+    """FP64 irregular force (irr.avx.cpp semantics) of the particles addr
+    (0-based) at time ti; lists[n][lmax]: count then 0-based ids.
+    Returns acc [ni, 3], jrk [ni, 3], nnbid [ni] (1-based, 0 if no list)."""
+    m = _c(m); n = m.shape[0]
+    x0 = _c(x0, (n, 3)); v0 = _c(v0, (n, 3)); a2 = _c(a2, (n, 3)); j6 = _c(j6, (n, 3))
+    t0 = _c(t0)
+    lists = np.ascontiguousarray(lists, dtype=np.int32)
+    addr = np.ascontiguousarray(addr, dtype=np.int32)
+    ni = addr.shape[0]
+    acc = np.empty((ni, 3)); jrk = np.empty((ni, 3)); nid = np.empty(ni, dtype=np.int32)
+    lib().oracle_irr_fp64(n, _dp(x0), _dp(v0), _dp(a2), _dp(j6), _dp(m), _dp(t0),
+                          lists.shape[1], lists.ctypes.data_as(_I), float(ti), ni,
+                          addr.ctypes.data_as(_I), _dp(acc), _dp(jrk), nid.ctypes.data_as(_I))
+    return acc, jrk, nid
+
+
+class RefIrrAVX:
+    """The reference's src/Main/irr.avx.cpp built into oracle/_ref (x86_64
+    only), driven through its own Fortran-style entry points (1-based
+    addresses and ids)."""
+
+    PATH = HERE / "_ref" / "libref_irr_avx.so"
+
+    @classmethod
+    def available(cls) -> bool:
+        return cls.PATH.exists()
+
+    def __init__(self, nmax: int, lmax: int):
+        self.lib = C.CDLL(str(self.PATH))
+        for name in ("irr_simd_open_", "irr_simd_close_", "irr_simd_set_jp_",
+                     "irr_simd_set_list_", "irr_simd_firr_vec_"):
+            getattr(self.lib, name).restype = None
+        self.nmax, self.lmax = nmax, lmax
+        self.lib.irr_simd_open_(C.byref(C.c_int(nmax)), C.byref(C.c_int(lmax)),
+                                C.byref(C.c_int(0)))
+
+    def close(self):
+        self.lib.irr_simd_close_(C.byref(C.c_int(0)))
+
+    def set_jp(self, x0, v0, a2, j6, m, t0):
+        n = len(m)
+        for i in range(n):
+            xs = [np.ascontiguousarray(a[i], dtype=np.float64) for a in (x0, v0, a2, j6)]
+            self.lib.irr_simd_set_jp_(C.byref(C.c_int(i + 1)), *[_dp(a) for a in xs],
+                                      C.byref(C.c_double(m[i])), C.byref(C.c_double(t0[i])))
+
+    def set_lists(self, lists):
+        """lists[n][lmax] with 0-based ids; passed as the Fortran LIST rows
+        (count, then 1-based ids)."""
+        for i in range(lists.shape[0]):
+            row = np.ascontiguousarray(lists[i], dtype=np.int32).copy()
+            c = int(row[0])
+            row[1:1 + c] += 1
+            # the library reads whole groups of 8 ids
+            buf = np.zeros(1 + 8 * ((c + 7) // 8 + 1), dtype=np.int32)
+            buf[:1 + c] = row[:1 + c]
+            self.lib.irr_simd_set_list_(C.byref(C.c_int(i + 1)), buf.ctypes.data_as(_I))
+
+    def firr(self, ti, addr):
+        a = np.ascontiguousarray(np.asarray(addr) + 1, dtype=np.int32)
+        ni = a.shape[0]
+        acc = np.empty((ni, 3)); jrk = np.empty((ni, 3)); nid = np.empty(ni, dtype=np.int32)
+        self.lib.irr_simd_firr_vec_(C.byref(C.c_double(ti)), C.byref(C.c_int(ni)),
+                                    a.ctypes.data_as(_I), _dp(acc), _dp(jrk),
+                                    nid.ctypes.data_as(_I))
+        return acc, jrk, nid

@@ -1,10 +1,10 @@
 """Generate the golden fixtures that pin the CPU oracle to the reference.
 
-Runs, in this (x86_64) container, the reference's own CPU regular-force and
-potential code (src/Main/reg.avx.cpp, src/Main/pot.avx.cpp, compiled from the
-reference sources by `make -C oracle ref` into oracle/_ref) and the FP64
-oracle on seeded inputs, and stores inputs and both outputs in
-tests/golden/*.npz.  The tests then check the oracle against these files on
+Runs, in this (x86_64) container, the reference's own CPU regular-force,
+potential and irregular-force code (src/Main/reg.avx.cpp, pot.avx.cpp,
+irr.avx.cpp, compiled from the reference sources by `make -C oracle ref` into
+oracle/_ref) and the FP64 oracles on seeded inputs, and stores inputs and
+both outputs in tests/golden/*.npz.  The tests then check the oracle against these files on
 any host, without the reference present.
 
     python tests/golden/make_golden.py
@@ -83,6 +83,43 @@ def main():
                         ref_sub=ref.pot(pm, px, 100, 50), fp64_sub=O.pot_fp64(pm, px, 100, 50))
     ref.close()
     print("pot: written")
+
+    # irregular force (irr.avx.cpp): neighbour lists of the regular path with
+    # the particle itself removed, predictor state from the full force
+    irr_case("irr_plummer2048", c, seed=21, ti=0.25, empty=())
+    irr_case("irr_ragged_n37", r, seed=22, ti=1.5, empty=(0, 7, 30))
+
+
+def irr_case(name, c, seed, ti, empty):
+    n = c.n
+    rng = np.random.default_rng(seed)
+    lmax = 257
+    _, _, _, lst = O.regf_fp64(c.m, c.x, c.v, c.h2(), c.dtr, c.x, c.v, lmax, lmax - 1)
+    lists = np.zeros((n, lmax), dtype=np.int32)
+    for i in range(n):
+        ids = lst[i, 1:1 + max(lst[i, 0], 0)]
+        ids = ids[ids != i]
+        if i in empty:
+            ids = ids[:0]
+        lists[i, 0] = len(ids)
+        lists[i, 1:1 + len(ids)] = ids
+    acc, jrk, _, _ = O.regf_fp64(c.m, c.x, c.v, np.full(n, 1e-30), np.zeros(n), c.x, c.v,
+                                 2, 1)
+    f = 0.5 * acc
+    fdot = jrk / 6.0
+    t0 = ti - rng.uniform(0.0, 0.01, n)
+    active = rng.permutation(n)[: max(1, (2 * n) // 3)]
+    refi = O.RefIrrAVX(n, lmax)
+    refi.set_jp(c.x, c.v, f, fdot, c.m, t0)
+    refi.set_lists(lists)
+    ra, rj, rn = refi.firr(ti, active)
+    refi.close()
+    oa, oj, on = O.irr_fp64(c.x, c.v, f, fdot, c.m, t0, lists, ti, active)
+    np.savez_compressed(OUT / f"{name}.npz", x0=c.x, v0=c.v, f=f, fdot=fdot, m=c.m, t0=t0,
+                        lists=lists, ti=ti, active=active, ref_acc=ra, ref_jrk=rj, ref_nnbid=rn,
+                        fp64_acc=oa, fp64_jrk=oj, fp64_nnbid=on)
+    print(f"{name}: ni={len(active)} n={n} nearest-neighbour ids identical ref/fp64:",
+          int(np.sum(rn == on)), "/", len(rn))
 
 
 if __name__ == "__main__":

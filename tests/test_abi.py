@@ -1,4 +1,4 @@
-"""The C-ABI library: builds, loads, exports every symbol include/gpunb.h
+"""The C-ABI library: builds, loads, exports every symbol include/*.h
 declares, and refuses to run without a GPU (no CPU fallback)."""
 import ctypes
 import re
@@ -9,19 +9,23 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
-HEADER = ROOT / "include" / "gpunb.h"
+HEADERS = sorted((ROOT / "include").glob("*.h"))
 
 
 def declared_symbols():
-    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", text, flags=re.M)
-    return sorted(set(n for n in names if n.startswith(("gpunb", "gpupot"))))
+    names = []
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", text, flags=re.M)
+    return sorted(set(n for n in names if n.startswith(("gpunb", "gpupot", "irr_"))))
 
 
 def test_header_declares_reference_abi():
     names = declared_symbols()
     for ref in ["gpunb_devinit_", "gpunb_open_", "gpunb_close_", "gpunb_send_", "gpunb_regf_",
-                "gpunb_profile_", "gpupot_"]:
+                "gpunb_profile_", "gpupot_", "irr_simd_open_", "irr_simd_close_",
+                "irr_simd_profile_", "irr_simd_set_jp_", "irr_simd_set_list_",
+                "irr_simd_firr_vec_"]:
         assert ref in names
 
 
