@@ -389,25 +389,37 @@ static long long tune_key(int nj, int ni, int mflag, int prec) {
 // j-splits for a persistent launch: about 32 work items per resident block,
 // so that the last round of items leaves little of the machine idle, with
 // at least 2 tiles per item.
+// j-splits: about 64 work items per resident block (the dynamic queue then
+// balances the blocks to within one short item), at least one tile per item.
 static int plan_splits(int variant, int ni, int ntile, bool mflag) {
   const VariantDesc d = regf_variant(variant);
   const int gx = (ni + d.itile() - 1) / d.itile();
   const int bps = regf_ds_blocks_per_sm(variant, mflag);
-  const long long want = 32ll * g.n_sm * bps;
+  const long long want = 64ll * g.n_sm * bps;
   long long s = (want + gx - 1) / gx;
-  const int smax = std::max(1, ntile / 2);
+  const int smax = std::max(1, ntile);
   if (s > smax) s = smax;
   if (s < 1) s = 1;
   return (int)s;
 }
 
-// Shapes measured on GB300 (N = 65536 Plummer and N = 2^20 King, all shapes
-// and split counts): 4 warps along i reading 8 j per step (two 128-bit loads
-// per field, one warp vote per 8 j) for blocks of 512 and more, one warp of
-// 32 i-particles with the j tile split over 8 warps below.
+// Shapes measured on GB300 (autotuner sweeps, N = 65536 Plummer and N = 2^20
+// King): below 512 i-particles one warp of 32 i with the j tile split over 8
+// warps (variant 2); otherwise 4 warps x 32 i, reading 8 j per warp vote
+// (variant 6, 4 blocks per SM) when the items are long (4 tiles or more),
+// and 4 j per vote (variant 4, 5 blocks per SM) when they are short.
 static void heuristic_plan(int ni, int ntile, bool mflag, int &variant, int &splits) {
-  variant = (ni >= 512) ? 6 : 2;
+  if (ni < 512) {
+    variant = 2;
+    splits = plan_splits(variant, ni, ntile, mflag);
+    return;
+  }
+  variant = 6;
   splits = plan_splits(variant, ni, ntile, mflag);
+  if ((long long)ntile < 4ll * splits) {
+    variant = 4;
+    splits = plan_splits(variant, ni, ntile, mflag);
+  }
 }
 
 static void fp64_plan(int ni, int ntile64, int &gx, int &splits) {

@@ -777,6 +777,64 @@ __global__ void __launch_bounds__(SCAN_THREADS) list_scan_totals_kernel(int *bto
 constexpr int GATHER_WARPS = 8;
 constexpr int GATHER_SMEM_IDS = 1024;
 
+// Bitonic sort of 32*E ints held by one warp, element u = lane*E + r in
+// v[r]: exchanges at distance >= E between lanes (shuffles), below E inside
+// a lane.  Ascending.
+template <int E>
+__device__ __forceinline__ void warp_bitonic_sort(int (&v)[E], int lane) {
+  constexpr int P2 = 32 * E;
+#pragma unroll
+  for (int k = 2; k <= P2; k <<= 1) {
+#pragma unroll
+    for (int jd = k >> 1; jd > 0; jd >>= 1) {
+      if (jd >= E) {
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+          const int u = lane * E + r;
+          const int other = __shfl_xor_sync(0xffffffffu, v[r], jd / E);
+          const bool keep_min = ((u & jd) == 0) == ((u & k) == 0);
+          v[r] = keep_min ? min(v[r], other) : max(v[r], other);
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+          const int p = r ^ jd;
+          if (p > r) {
+            const int u = lane * E + r;
+            const bool up = (u & k) == 0;
+            const int x = v[r], y = v[p];
+            if ((x > y) == up) {
+              v[r] = y;
+              v[p] = x;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+template <int E>
+__device__ __forceinline__ void gather_row_regs(const int *__restrict__ row, int n, int lane,
+                                                int *__restrict__ out) {
+  int v[E];
+#pragma unroll
+  for (int r = 0; r < E; ++r) {
+    const int u = lane * E + r;
+    v[r] = (u < n) ? row[u] : INT_MAX;
+  }
+  warp_bitonic_sort<E>(v, lane);
+#pragma unroll
+  for (int r = 0; r < E; ++r) {
+    const int u = lane * E + r;
+    if (u < n) out[u] = v[r];
+  }
+}
+
+// Row i (its accepted neighbours, appended in any order by the pair kernel)
+// -> ascending, into the compacted list at off[i] + boff[i / SCAN_ITEMS].
+// Rows of up to 256 ids are sorted in registers, up to GATHER_SMEM_IDS in
+// shared memory, longer ones in place (odd-even transposition).
 __global__ void __launch_bounds__(32 * GATHER_WARPS) list_gather_kernel(
     int *__restrict__ rows, int cap, const int *__restrict__ len, const int *__restrict__ off,
     const int *__restrict__ boff, int ni, int *__restrict__ dense) {
@@ -787,6 +845,11 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS) list_gather_kernel(
   const int n = len[i];
   if (n == 0) return;
   int *row = rows + (size_t)i * cap;
+  const int o = off[i] + boff[i / SCAN_ITEMS];
+  if (n <= 32) { gather_row_regs<1>(row, n, lane, dense + o); return; }
+  if (n <= 64) { gather_row_regs<2>(row, n, lane, dense + o); return; }
+  if (n <= 128) { gather_row_regs<4>(row, n, lane, dense + o); return; }
+  if (n <= 256) { gather_row_regs<8>(row, n, lane, dense + o); return; }
   const bool in_smem = n <= GATHER_SMEM_IDS;
   int *a = in_smem ? buf[warp] : row;
   int p2 = 1;
@@ -819,7 +882,6 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS) list_gather_kernel(
       __syncwarp();
     }
   }
-  const int o = off[i] + boff[i / SCAN_ITEMS];
   for (int u = lane; u < n; u += 32) dense[o + u] = a[u];
 }
 
