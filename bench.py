@@ -360,6 +360,20 @@ def irregular_leg(c, h2, lists_src, cpu: bool):
                 best = min(best, time.perf_counter() - t)
             out["blocks"][str(ni)] = {"pairs": pairs, "ms": best * 1e3,
                                       "gpairs_s": pairs / best / 1e9}
+        # predict-and-send from the stored state vs gpunb_send_ of host arrays
+        from nbody6ppgpu_gb300.gpunb import GpuNb
+        from nbody6ppgpu_gb300.irr import send_predicted
+        with GpuNb(n) as nb:
+            tp, ts = [], []
+            for _ in range(6):
+                t = time.perf_counter()
+                xp, vp = send_predicted(ti, c.m)
+                tp.append(time.perf_counter() - t)
+                t = time.perf_counter()
+                nb.send(c.m, xp, vp)
+                ts.append(time.perf_counter() - t)
+        out["predict_send_ms"] = 1e3 * min(tp[1:])
+        out["send_host_arrays_ms"] = 1e3 * min(ts[1:])
     if cpu:
         from oracle import oracle as O
         act = rng.permutation(n)[:16384]

@@ -169,6 +169,19 @@ void gpunb_set_graphs(int flag);
 int gpupot_device_noalloc(int istart, int ni, int n, const double *m, const double *x,
                           double *pot, void *stream);
 
+/* Predict-and-send (no reference counterpart; replaces the host prediction
+ * of src/Main/xbpredall.f:16-27 followed by GPUNB_SEND at intgrt.F:916-918).
+ * Predicts bodies *ifirst .. *ntot (1-based) to *time from the state stored
+ * with irr_simd_set_jp_ (include/irr.h: X0, X0DOT, F, FDOT, T0), returns
+ * X and XDOT of those bodies in x[ntot-ifirst+1][3], xdot[...] (the values
+ * xbpredall would compute, for the caller's other uses) and uploads them with
+ * the masses body[ntot-ifirst+1] as the regular-force j-set, as
+ * gpunb_send_(NN, BODY(IFIRST), X(1,IFIRST), XDOT(1,IFIRST)) would: the j-set
+ * never crosses to the host and back.  Needs irr_simd_open_ with nmax >= ntot
+ * and gpunb_open_.  KS components (KSRES2 in xbpredall) stay with the caller. */
+void gpunb_send_predicted_(int *ifirst, int *ntot, double *time, double body[], double x[][3],
+                           double xdot[][3]);
+
 /* ---- Learned neighbour-radius predictor (no reference counterpart) --------
  * An 8 -> 64 -> 64 -> 1 GELU MLP that proposes each active particle's next
  * RS in place of the plain rule of src/Main/regcor_gpu.F:146-253; the caller

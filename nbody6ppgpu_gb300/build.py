@@ -49,7 +49,7 @@ def _stale() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*")) + [ROOT / "include" / "gpunb.h", Path(__file__)]
+    deps = list(CSRC.glob("*")) + list((ROOT / "include").glob("*.h")) + [Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps if p.exists())
 
 

@@ -167,6 +167,22 @@ __global__ void irr_put_rows_kernel(int k, const int *__restrict__ idx,
   for (int u = lane; u < len && u < lmax; u += 32) d[u] = s[u];
 }
 
+// Predicted positions and velocities of particles a0 .. a0+n-1 at ti, in the
+// arrays of a j-set upload (xbpredall.f:16-27: X = ((FDOT S + F) S + X0DOT) S
+// + X0, XDOT = (1.5 FDOT S + F) 2 S + X0DOT, with F and FDOT as stored).
+__global__ void irr_predict_all_kernel(const double *__restrict__ rec, int a0, int n, double ti,
+                                       double *__restrict__ x, double *__restrict__ v) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double xp[3], vp[3], m;
+  predict(rec + (size_t)(a0 + k) * REC, ti, xp, vp, m);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    x[3 * (size_t)k + c] = xp[c];
+    v[3 * (size_t)k + c] = vp[c];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host
 
@@ -229,7 +245,7 @@ struct State {
   std::vector<unsigned> seen;    // epoch stamps for de-duplication
   unsigned epoch = 0;
   std::vector<int> uniq;
-  DevBuf rec_d, list_d, addr_d, out_d, nid_d, idx_d, stage_d, off_d, err_d;
+  DevBuf rec_d, list_d, addr_d, out_d, nid_d, idx_d, stage_d, off_d, err_d, pm_d, px_d, pv_d;
   PinBuf stage_h, idx_h, off_h, err_h;
   double time_grav = 0.0;
   unsigned long long num_inter = 0, num_fcall = 0, num_steps = 0;
@@ -265,7 +281,7 @@ static double wtime() {
 
 static void release_all() {
   for (DevBuf *b : {&S.rec_d, &S.list_d, &S.addr_d, &S.out_d, &S.nid_d, &S.idx_d, &S.stage_d,
-                    &S.off_d, &S.err_d})
+                    &S.off_d, &S.err_d, &S.pm_d, &S.px_d, &S.pv_d})
     b->release();
   for (PinBuf *b : {&S.stage_h, &S.idx_h, &S.off_h, &S.err_h}) b->release();
   S.rec_h.clear();
@@ -584,6 +600,48 @@ static void firr_vec(double ti, int ni, const int *addr, double (*acc)[3], doubl
   S.time_grav += wtime() - t0;
 }
 
+static void send_predicted(int ifirst, int ntot, double ti, const double *body, double (*x)[3],
+                           double (*xdot)[3]) {
+  std::lock_guard<std::mutex> lk(S.mu);
+  if (!S.open) {
+    failf(GPUNB_E_NOT_OPEN, "gpunb_send_predicted_ needs the particle state of irr_simd_open_ "
+                            "and irr_simd_set_jp_");
+    return;
+  }
+  const int n = ntot - ifirst + 1;
+  if (ifirst < 1 || n < 0 || ntot > S.nmax) {
+    failf(GPUNB_E_ARG, "gpunb_send_predicted_: bodies %d..%d outside [1, %d]", ifirst, ntot,
+          S.nmax);
+    return;
+  }
+  cudaStream_t st = S.st;
+  if (!upload()) return;
+  if (!S.pm_d.ensure((size_t)std::max(n, 1) * sizeof(double)) ||
+      !S.px_d.ensure((size_t)std::max(n, 1) * 3 * sizeof(double)) ||
+      !S.pv_d.ensure((size_t)std::max(n, 1) * 3 * sizeof(double))) {
+    failf(GPUNB_E_ALLOC, "gpunb_send_predicted_: device allocation failed");
+    return;
+  }
+  if (n > 0) {
+    IRR_CUDA(cudaMemcpyAsync(S.pm_d.p, body, (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
+                             st), );
+    irr_predict_all_kernel<<<(n + 255) / 256, 256, 0, st>>>(S.rec_d.as<double>(), ifirst - 1, n,
+                                                           ti, S.px_d.as<double>(),
+                                                           S.pv_d.as<double>());
+    IRR_CUDA(cudaGetLastError(), );
+  }
+  if (gpunb_send_device(n, S.pm_d.as<double>(), S.px_d.as<double>(), S.pv_d.as<double>(), st) !=
+      GPUNB_OK)
+    return;   // the engine has recorded the reason
+  if (n > 0) {
+    IRR_CUDA(cudaMemcpyAsync(&x[0][0], S.px_d.p, (size_t)n * 3 * sizeof(double),
+                             cudaMemcpyDeviceToHost, st), );
+    IRR_CUDA(cudaMemcpyAsync(&xdot[0][0], S.pv_d.p, (size_t)n * 3 * sizeof(double),
+                             cudaMemcpyDeviceToHost, st), );
+  }
+  IRR_CUDA(cudaStreamSynchronize(st), );
+}
+
 }  // namespace irr
 }  // namespace gpunb
 
@@ -609,6 +667,11 @@ void irr_simd_set_list_(int *addr, int *nblist) { set_list(*addr, nblist); }
 void irr_simd_firr_vec_(double *ti, int *ni, int addr[], double acc[][3], double jrk[][3],
                         int nnbid[]) {
   firr_vec(*ti, *ni, addr, acc, jrk, nnbid);
+}
+
+void gpunb_send_predicted_(int *ifirst, int *ntot, double *time, double body[], double x[][3],
+                           double xdot[][3]) {
+  send_predicted(*ifirst, *ntot, *time, body, x, xdot);
 }
 
 int irr_set_host_path(int mode) {

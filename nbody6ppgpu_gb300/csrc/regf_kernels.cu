@@ -16,14 +16,38 @@
 #include <cfloat>
 #include <climits>
 
+// A tile is "near" an i-particle, and its pairs take the double-single
+// coordinate path, when |O - x_i|^2 < GPUNB_NEAR_K2 R^2.  With K = 2 every
+// pair of a far tile is at least R away, so the tile-relative rounding
+// (2^-22 (R + |dx|) per axis) stays within 2^-21 |dx|.  Measured against the
+// FP64 kernel (Plummer 65536 and King 2^20, ni = 16384): force and jerk
+// errors equal to the all-double-single kernel's to two digits, while
+// K = 0 (every tile relative) doubled the jerk's 99th percentile; the pair
+// kernel gains 7% (N = 65536) to 13% (N = 2^20) over K = infinity.
+#ifndef GPUNB_NEAR_K2
+#define GPUNB_NEAR_K2 4.0f
+#endif
+
 namespace gpunb {
 
 // ---------------------------------------------------------------------------
-// j packing: FP64 (as sent) -> split-precision SoA tiles + tile metadata.
+// j packing: FP64 (as sent) -> tile-relative FP32 SoA tiles + tile metadata.
 // One block of JT threads per tile.  Replaces the host-side Jparticle packing
-// of gpunb.velocity.cu:716-727 (which also drops positions to plain FP32).
+// of gpunb.velocity.cu:716-727 (which drops positions to plain FP32).
 // Tile slot p holds body perm[p] (identity when perm is null; perm[p] = -1
 // marks a padding slot).
+
+// block-wide max / min of one double (JT threads), result in every thread
+__device__ __forceinline__ double block_max(double a, double *s) {
+  for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = a;
+  __syncthreads();
+  double r = s[0];
+  for (int w = 1; w < JT / 32; ++w) r = fmax(r, s[w]);
+  return r;
+}
+
 __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restrict__ m,
                                                          const double *__restrict__ x,
                                                          const double *__restrict__ v, int nj,
@@ -31,51 +55,77 @@ __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restric
                                                          float *__restrict__ tiles, int *err) {
   const int t = blockIdx.x, l = threadIdx.x, p = t * JT + l;
   float *T = tiles + (size_t)t * TILE_FLOATS;
-  double vabs = 0.0, mj = 0.0;
-  int real = 0;
+  __shared__ double s_red[JT / 32];
   const int j = perm ? perm[p] : (p < nj ? p : -1);   // -1: padding slot
+  double xj[3] = {0.0, 0.0, 0.0}, vj[3] = {0.0, 0.0, 0.0}, mj = 0.0;
   if (j >= 0) {
-    const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
-    const double v0 = v[3 * j], v1 = v[3 * j + 1], v2 = v[3 * j + 2];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      xj[c] = x[3 * j + c];
+      vj[c] = v[3 * j + c];
+    }
     mj = m[j];
-    if (isnan(x0) || isnan(x1) || isnan(x2) || isnan(v0) || isnan(v1) || isnan(v2) || isnan(mj))
+    if (isnan(xj[0]) || isnan(xj[1]) || isnan(xj[2]) || isnan(vj[0]) || isnan(vj[1]) ||
+        isnan(vj[2]) || isnan(mj))
       raise_error(err, GPUNB_E_NAN);
-    float h, lo;
-    ds_split(x0, h, lo); T[F_XH * JT + l] = h; T[F_XL * JT + l] = lo;
-    ds_split(x1, h, lo); T[F_YH * JT + l] = h; T[F_YL * JT + l] = lo;
-    ds_split(x2, h, lo); T[F_ZH * JT + l] = h; T[F_ZL * JT + l] = lo;
-    T[F_VX * JT + l] = (float)v0;
-    T[F_VY * JT + l] = (float)v1;
-    T[F_VZ * JT + l] = (float)v2;
+  }
+  // tile centre: midpoint of the real bodies' bounding box
+  double o[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double hi = block_max(j >= 0 ? xj[c] : -INFINITY, s_red);
+    const double lo = -block_max(j >= 0 ? -xj[c] : -INFINITY, s_red);
+    o[c] = (hi >= lo) ? 0.5 * lo + 0.5 * hi : 0.0;   // no real body: O = 0
+    if (isnan(o[c])) o[c] = 0.0;
+  }
+  double r2 = 0.0;
+  if (j >= 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double d = xj[c] - o[c];
+      r2 += d * d;
+      T[(F_XR + c) * JT + l] = (float)d;
+      float h, lo;
+      ds_split(xj[c], h, lo);
+      T[(F_XH + c) * JT + l] = h;
+      T[(F_XL + c) * JT + l] = lo;
+    }
+    T[F_VX * JT + l] = (float)vj[0];
+    T[F_VY * JT + l] = (float)vj[1];
+    T[F_VZ * JT + l] = (float)vj[2];
     T[F_MN * JT + l] = (float)(-0.5 * mj);
-    vabs = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
-    real = 1;
   } else {
     // padding body: massless and far away, never a neighbour candidate
+    T[F_XR * JT + l] = 1.0e15f;
+    T[F_YR * JT + l] = 1.0e15f;
+    T[F_ZR * JT + l] = 1.0e15f;
     T[F_XH * JT + l] = 1.0e15f; T[F_XL * JT + l] = 0.f;
     T[F_YH * JT + l] = 1.0e15f; T[F_YL * JT + l] = 0.f;
     T[F_ZH * JT + l] = 1.0e15f; T[F_ZL * JT + l] = 0.f;
     T[F_VX * JT + l] = 0.f; T[F_VY * JT + l] = 0.f; T[F_VZ * JT + l] = 0.f;
     T[F_MN * JT + l] = -0.f;
   }
-  // tile maxima of |v| and m (block reduction), rounded up when narrowed
-  __shared__ double s_v[JT / 32], s_m[JT / 32];
-  __shared__ int s_n[JT / 32];
-  for (int o = 16; o > 0; o >>= 1) {
-    vabs = fmax(vabs, __shfl_xor_sync(0xffffffffu, vabs, o));
-    mj = fmax(mj, __shfl_xor_sync(0xffffffffu, mj, o));
-    real += __shfl_xor_sync(0xffffffffu, real, o);
-  }
-  if ((l & 31) == 0) { s_v[l >> 5] = vabs; s_m[l >> 5] = mj; s_n[l >> 5] = real; }
-  __syncthreads();
+  // tile maxima of |v|, m and |x - O|, rounded up when narrowed; body count
+  const double vm = block_max(j >= 0 ? sqrt(vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2]) : 0.0,
+                              s_red);
+  const double mm = block_max(mj, s_red);
+  const double rad = block_max(sqrt(r2), s_red);
+  const double nr = block_max(j >= 0 ? (double)(l + 1) : 0.0, s_red);   // slots fill from 0
   if (l == 0) {
-    double vm = 0.0, mm = 0.0;
-    int nr = 0;
-    for (int w = 0; w < JT / 32; ++w) { vm = fmax(vm, s_v[w]); mm = fmax(mm, s_m[w]); nr += s_n[w]; }
-    T[NFIELD * JT + 0] = (float)(vm * (1.0 + 0x1p-20));
-    T[NFIELD * JT + 1] = (float)(sqrt(fmax(mm, 0.0)) * (1.0 + 0x1p-20));
-    T[NFIELD * JT + 2] = (float)nr;
-    T[NFIELD * JT + 3] = 0.f;
+    float *M = T + NFIELD * JT;
+    M[M_VMAX] = (float)(vm * (1.0 + 0x1p-20));
+    M[M_SMAX] = (float)(sqrt(fmax(mm, 0.0)) * (1.0 + 0x1p-20));
+    M[M_COUNT] = (float)nr;
+    M[M_RAD] = (float)(rad * (1.0 + 0x1p-20));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float h, lo;
+      ds_split(o[c], h, lo);
+      M[M_OH + c] = h;
+      M[M_OL + c] = lo;
+    }
+    M[M_OH + 3] = 0.f;
+    M[M_OL + 3] = 0.f;
   }
 }
 
@@ -106,7 +156,7 @@ __device__ __forceinline__ bool nb_test_fp64(const ISet &is, int i, const JSet &
 // ---------------------------------------------------------------------------
 // Per-i register state of the split-precision kernel.
 struct IState {
-  f2 nxh, nyh, nzh, nxl, nyl, nzl;  // -(hi, lo) of the position, duplicated
+  float nxh, nyh, nzh, nxl, nyl, nzl;  // -(hi, lo) of the position
   f2 nvx, nvy, nvz;                 // -velocity, duplicated
   float s;                          // sqrt(h2) * (1 + 2^-12)  (filter radius)
   float dv;                         // |dtr| * (1 + 2^-12)
@@ -150,13 +200,13 @@ __device__ __forceinline__ void load_istate(IState &I, const float4 *__restrict_
   if (valid) {
     const float4 *r = rec + 4 * (size_t)slot;
     const float4 a = r[0], b = r[1], c = r[2], d = r[3];
-    I.nxh = mk2(a.x); I.nyh = mk2(a.y); I.nzh = mk2(a.z);
-    I.nxl = mk2(a.w); I.nyl = mk2(b.x); I.nzl = mk2(b.y);
+    I.nxh = a.x; I.nyh = a.y; I.nzh = a.z;
+    I.nxl = a.w; I.nyl = b.x; I.nzl = b.y;
     I.nvx = mk2(b.z); I.nvy = mk2(b.w); I.nvz = mk2(c.x);
     I.s = c.y; I.dv = c.z; I.va = c.w;
     I.h2f = d.x; I.dtrf = d.y; I.i = __float_as_int(d.z);
   } else {
-    I.nxh = I.nyh = I.nzh = I.nxl = I.nyl = I.nzl = mk2(0.f);
+    I.nxh = I.nyh = I.nzh = I.nxl = I.nyl = I.nzl = 0.f;
     I.nvx = I.nvy = I.nvz = mk2(0.f);
     I.s = -1.f; I.dv = 0.f; I.va = 0.f; I.h2f = -1.f; I.dtrf = 0.f; I.i = -1;
   }
@@ -174,11 +224,14 @@ __device__ __noinline__ bool decide_pair_fp64(const ISet &is, int i, const JSet 
 // the FP32 value lies inside a conservative error band around the criterion.
 // The band bounds the FP32 rounding of the coordinate and velocity
 // differences, of h2 and of the products by 2^-14 of the magnitudes involved
-// (|dv| bounded by its L1 norm).
+// (|dv| bounded by its L1 norm), plus 2^-18 R (r + w) for the tile-relative
+// coordinates (their error is below 2^-23 (R + r) per component; R = tile
+// radius).
 template <bool MFLAG>
 __device__ __forceinline__ bool decide_pair(const IState &I, const ISet &is, const JSet &js,
                                             int jg, float dx, float dy, float dz, float dvx,
-                                            float dvy, float dvz, float r2, float mneg_half) {
+                                            float dvy, float dvz, float r2, float mneg_half,
+                                            float R) {
   const float px = fmaf(I.dtrf, dvx, dx);
   const float py = fmaf(I.dtrf, dvy, dy);
   const float pz = fmaf(I.dtrf, dvz, dz);
@@ -188,7 +241,7 @@ __device__ __forceinline__ bool decide_pair(const IState &I, const ISet &is, con
   bool in = r2min < crit;
   const float dv1 = fabsf(dvx) + fabsf(dvy) + fabsf(dvz);
   const float w = 2.0f * fabsf(I.dtrf) * (I.va + dv1);
-  const float band = 0x1p-14f * (fabsf(crit) + r2 + w * w);
+  const float band = 0x1p-14f * (fabsf(crit) + r2 + w * w) + 0x1p-18f * R * (sqrtf(r2) + w);
   if (fabsf(r2min - crit) <= band) in = decide_pair_fp64<MFLAG>(is, I.i, js, jg);
   return in;
 }
@@ -211,11 +264,29 @@ struct PairGeo {
   f2 dx, dy, dz, dvx, dvy, dvz, mn, r2, rv, z;
 };
 
-__device__ __forceinline__ void pair_geo(const IState &I, const JPair &p, PairGeo &g) {
-  // double-single coordinate difference: (hi_j - hi_i) + (lo_j - lo_i)
-  g.dx = add2(add2(p.v[F_XH], I.nxh), add2(p.v[F_XL], I.nxl));
-  g.dy = add2(add2(p.v[F_YH], I.nyh), add2(p.v[F_YL], I.nyl));
-  g.dz = add2(add2(p.v[F_ZH], I.nzh), add2(p.v[F_ZL], I.nzl));
+// Per (i, tile): the offset O - x_i of the tile centre from the i-particle
+// (double-single difference rounded to FP32, duplicated for the lane pairs),
+// the candidate bound H on r^2 and the tile radius R.
+struct TileCtx {
+  f2 ox, oy, oz;
+  f2 nxh, nyh, nzh, nxl, nyl, nzl;   // -(hi, lo) of x_i, for near tiles
+  float H, R;
+};
+
+template <bool REL>
+__device__ __forceinline__ void pair_geo(const IState &I, const TileCtx &C, const JPair &p,
+                                         PairGeo &g) {
+  if (REL) {
+    // from the tile-relative position: (x_j - O) + (O - x_i)
+    g.dx = add2(p.v[F_XR], C.ox);
+    g.dy = add2(p.v[F_YR], C.oy);
+    g.dz = add2(p.v[F_ZR], C.oz);
+  } else {
+    // double-single difference: (hi_j - hi_i) + (lo_j - lo_i)
+    g.dx = add2(add2(p.v[F_XH], C.nxh), add2(p.v[F_XL], C.nxl));
+    g.dy = add2(add2(p.v[F_YH], C.nyh), add2(p.v[F_YL], C.nyl));
+    g.dz = add2(add2(p.v[F_ZH], C.nzh), add2(p.v[F_ZL], C.nzl));
+  }
   g.dvx = add2(p.v[F_VX], I.nvx);
   g.dvy = add2(p.v[F_VY], I.nvy);
   g.dvz = add2(p.v[F_VZ], I.nvz);
@@ -236,13 +307,14 @@ __device__ __forceinline__ bool pair_maybe(const PairGeo &g, float H) {
 // arrays; padding slots hold -1 and never qualify.  Ids are reported relative
 // to the owning j-set (jbase), in the caller's numbering.
 template <bool MFLAG>
-__device__ __forceinline__ void pair_candidates(const IState &I, float H, PairGeo &g, int jg0,
-                                                int jbase, const JSet &js, const ISet &is,
-                                                const RegfOut &out) {
+__device__ __forceinline__ void pair_candidates(const IState &I, const TileCtx &C, PairGeo &g,
+                                                int jg0, int jbase, const JSet &js,
+                                                const ISet &is, const RegfOut &out) {
+  const float H = C.H;
   if (g.r2.x < H) {
     const int jo = js.perm[jg0];
     if (jo >= 0 && decide_pair<MFLAG>(I, is, js, jo, g.dx.x, g.dy.x, g.dz.x, g.dvx.x, g.dvy.x,
-                                      g.dvz.x, g.r2.x, g.mn.x)) {
+                                      g.dvz.x, g.r2.x, g.mn.x, C.R)) {
       record_neighbour(out, I.i, jo - jbase);
       g.z.x = 0.f;
     }
@@ -250,7 +322,7 @@ __device__ __forceinline__ void pair_candidates(const IState &I, float H, PairGe
   if (g.r2.y < H) {
     const int jo = js.perm[jg0 + 1];
     if (jo >= 0 && decide_pair<MFLAG>(I, is, js, jo, g.dx.y, g.dy.y, g.dz.y, g.dvx.y, g.dvy.y,
-                                      g.dvz.y, g.r2.y, g.mn.y)) {
+                                      g.dvz.y, g.r2.y, g.mn.y, C.R)) {
       record_neighbour(out, I.i, jo - jbase);
       g.z.y = 0.f;
     }
@@ -272,38 +344,85 @@ __device__ __forceinline__ void pair_acc(const PairGeo &g, f2 (&q)[NQ]) {
 }
 
 // Four j (two lane pairs) against one i, one warp vote for both.
-template <bool MFLAG>
-__device__ __forceinline__ void pair4(const IState &I, float H, const JPair &p0, const JPair &p1,
-                                      f2 (&q)[NQ], int jg0, int jbase, const JSet &js,
-                                      const ISet &is, const RegfOut &out) {
+template <bool MFLAG, bool REL>
+__device__ __forceinline__ void pair4(const IState &I, const TileCtx &C, const JPair &p0,
+                                      const JPair &p1, f2 (&q)[NQ], int jg0, int jbase,
+                                      const JSet &js, const ISet &is, const RegfOut &out) {
   PairGeo g0, g1;
-  pair_geo(I, p0, g0);
-  pair_geo(I, p1, g1);
-  if (__any_sync(0xffffffffu, pair_maybe(g0, H) | pair_maybe(g1, H))) {
-    pair_candidates<MFLAG>(I, H, g0, jg0, jbase, js, is, out);
-    pair_candidates<MFLAG>(I, H, g1, jg0 + 2, jbase, js, is, out);
+  pair_geo<REL>(I, C, p0, g0);
+  pair_geo<REL>(I, C, p1, g1);
+  if (__any_sync(0xffffffffu, pair_maybe(g0, C.H) | pair_maybe(g1, C.H))) {
+    pair_candidates<MFLAG>(I, C, g0, jg0, jbase, js, is, out);
+    pair_candidates<MFLAG>(I, C, g1, jg0 + 2, jbase, js, is, out);
   }
   pair_acc(g0, q);
   pair_acc(g1, q);
 }
 
 // Eight j (four lane pairs) against one i, one warp vote for all.
-template <bool MFLAG>
-__device__ __forceinline__ void pair8(const IState &I, float H, const JPair (&p)[4], f2 (&q)[NQ],
-                                      int jg0, int jbase, const JSet &js, const ISet &is,
-                                      const RegfOut &out) {
+template <bool MFLAG, bool REL>
+__device__ __forceinline__ void pair8(const IState &I, const TileCtx &C, const JPair (&p)[4],
+                                      f2 (&q)[NQ], int jg0, int jbase, const JSet &js,
+                                      const ISet &is, const RegfOut &out) {
   PairGeo g[4];
 #pragma unroll
-  for (int u = 0; u < 4; ++u) pair_geo(I, p[u], g[u]);
+  for (int u = 0; u < 4; ++u) pair_geo<REL>(I, C, p[u], g[u]);
+  const float H = C.H;
   const bool any = pair_maybe(g[0], H) | pair_maybe(g[1], H) | pair_maybe(g[2], H) |
                    pair_maybe(g[3], H);
   if (__any_sync(0xffffffffu, any)) {
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      pair_candidates<MFLAG>(I, H, g[u], jg0 + 2 * u, jbase, js, is, out);
+      pair_candidates<MFLAG>(I, C, g[u], jg0 + 2 * u, jbase, js, is, out);
   }
 #pragma unroll
   for (int u = 0; u < 4; ++u) pair_acc(g[u], q);
+}
+
+// One warp's share [jbeg, jbeg + JW) of a tile against one i: the fields the
+// path needs, JV j per shared-memory load, one warp vote per 4 (JV <= 4) or
+// 8 j (JV = 8).
+template <bool MFLAG, bool REL, int JV, int JW>
+__device__ __forceinline__ void tile_pairs(const IState &I, const TileCtx &C,
+                                           const float *__restrict__ T, int jbeg, f2 (&q)[NQ],
+                                           int jg_tile, int jbase, const JSet &js,
+                                           const ISet &is, const RegfOut &out) {
+  constexpr int F0 = REL ? 0 : F_VX;
+  constexpr int F1 = REL ? NFIELD_REL : NFIELD;
+  if (JV == 8) {
+    for (int jj = jbeg; jj < jbeg + JW; jj += 8) {
+      JPair p[4];
+#pragma unroll
+      for (int f = F0; f < F1; ++f) {
+        const float4 u = *(const float4 *)(T + f * JT + jj);
+        const float4 w4 = *(const float4 *)(T + f * JT + jj + 4);
+        p[0].v[f] = make_float2(u.x, u.y);
+        p[1].v[f] = make_float2(u.z, u.w);
+        p[2].v[f] = make_float2(w4.x, w4.y);
+        p[3].v[f] = make_float2(w4.z, w4.w);
+      }
+      pair8<MFLAG, REL>(I, C, p, q, jg_tile + jj, jbase, js, is, out);
+    }
+  } else {
+    for (int jj = jbeg; jj < jbeg + JW; jj += 4) {
+      JPair p0, p1;
+      if (JV == 2) {
+#pragma unroll
+        for (int f = F0; f < F1; ++f) {
+          p0.v[f] = *(const f2 *)(T + f * JT + jj);
+          p1.v[f] = *(const f2 *)(T + f * JT + jj + 2);
+        }
+      } else {
+#pragma unroll
+        for (int f = F0; f < F1; ++f) {
+          const float4 u = *(const float4 *)(T + f * JT + jj);
+          p0.v[f] = make_float2(u.x, u.y);
+          p1.v[f] = make_float2(u.z, u.w);
+        }
+      }
+      pair4<MFLAG, REL>(I, C, p0, p1, q, jg_tile + jj, jbase, js, is, out);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -409,46 +528,35 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
       if (!mbar_wait_bounded(&bar[st], par)) s_abort = 1;
       if (*(volatile int *)&s_abort) break;
       const float *T = ring + st * TILE_FLOATS;
-      const float vmax = T[NFIELD * JT + 0];
-      const float smax = T[NFIELD * JT + 1];
+      const float *M = T + NFIELD * JT;
+      const float vmax = M[M_VMAX], smax = M[M_SMAX], rad = M[M_RAD];
+      const float ohx = M[M_OH], ohy = M[M_OH + 1], ohz = M[M_OH + 2];
+      const float olx = M[M_OL], oly = M[M_OL + 1], olz = M[M_OL + 2];
       const int jbeg = wj * JW;
 #pragma unroll
       for (int k = 0; k < IPT; ++k) {
+        TileCtx C;
+        // O - x_i from the double-single parts, rounded once to FP32
+        C.ox = mk2(__fadd_rn(__fadd_rn(ohx, I[k].nxh), __fadd_rn(olx, I[k].nxl)));
+        C.oy = mk2(__fadd_rn(__fadd_rn(ohy, I[k].nyh), __fadd_rn(oly, I[k].nyl)));
+        C.oz = mk2(__fadd_rn(__fadd_rn(ohz, I[k].nzh), __fadd_rn(olz, I[k].nzl)));
         const float base = I[k].dv * (I[k].va + vmax);
-        const float b = MFLAG ? fmaf(I[k].s, smax, base) : I[k].s + base;
-        const float H = (I[k].s < 0.f) ? -1.0f : b * b;
-        if (JV == 8) {
-          for (int jj = jbeg; jj < jbeg + JW; jj += 8) {
-            JPair p[4];
-#pragma unroll
-            for (int f = 0; f < NFIELD; ++f) {
-              const float4 u = *(const float4 *)(T + f * JT + jj);
-              const float4 w4 = *(const float4 *)(T + f * JT + jj + 4);
-              p[0].v[f] = make_float2(u.x, u.y);
-              p[1].v[f] = make_float2(u.z, u.w);
-              p[2].v[f] = make_float2(w4.x, w4.y);
-              p[3].v[f] = make_float2(w4.z, w4.w);
-            }
-            pair8<MFLAG>(I[k], H, p, q[k], (t0 + t) * JT + jj, jbase, js, is, out);
-          }
-        } else
-        for (int jj = jbeg; jj < jbeg + JW; jj += 4) {
-          JPair p0, p1;
-          if (JV == 2) {
-#pragma unroll
-            for (int f = 0; f < NFIELD; ++f) {
-              p0.v[f] = *(const f2 *)(T + f * JT + jj);
-              p1.v[f] = *(const f2 *)(T + f * JT + jj + 2);
-            }
-          } else {
-#pragma unroll
-            for (int f = 0; f < NFIELD; ++f) {
-              const float4 u = *(const float4 *)(T + f * JT + jj);
-              p0.v[f] = make_float2(u.x, u.y);
-              p1.v[f] = make_float2(u.z, u.w);
-            }
-          }
-          pair4<MFLAG>(I[k], H, p0, p1, q[k], (t0 + t) * JT + jj, jbase, js, is, out);
+        float b = MFLAG ? fmaf(I[k].s, smax, base) : I[k].s + base;
+        b = fmaf(rad, 0x1p-20f, b);   // the tile-relative rounding, 2^-22 (R + r) per axis
+        C.H = (I[k].s < 0.f) ? -1.0f : b * b;
+        C.R = rad;
+        // near tiles (|O - x_i| < 2R for a lane of the warp) take the
+        // double-single path, the others the tile-relative one
+        const float o2 = C.ox.x * C.ox.x + C.oy.x * C.oy.x + C.oz.x * C.oz.x;
+        const bool near = (I[k].s >= 0.f) && (o2 < GPUNB_NEAR_K2 * rad * rad);
+        if (__any_sync(0xffffffffu, near)) {
+          C.nxh = mk2(I[k].nxh); C.nyh = mk2(I[k].nyh); C.nzh = mk2(I[k].nzh);
+          C.nxl = mk2(I[k].nxl); C.nyl = mk2(I[k].nyl); C.nzl = mk2(I[k].nzl);
+          tile_pairs<MFLAG, false, JV, JW>(I[k], C, T, jbeg, q[k], (t0 + t) * JT, jbase, js, is,
+                                           out);
+        } else {
+          tile_pairs<MFLAG, true, JV, JW>(I[k], C, T, jbeg, q[k], (t0 + t) * JT, jbase, js, is,
+                                          out);
         }
       }
       // fold the tile's FP32 chunk sums into the float-float accumulators

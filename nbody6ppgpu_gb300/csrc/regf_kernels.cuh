@@ -8,17 +8,38 @@
 namespace gpunb {
 
 // ---------------------------------------------------------------------------
-// j-tile layout (split precision).  JT bodies per tile, SoA fields, then one
-// float4 of tile metadata.  One tile is one 16-byte-aligned bulk copy.
+// j-tile layout.  JT bodies per tile (consecutive along the Morton curve),
+// SoA fields, then three float4 of tile metadata.  One tile is one
+// 16-byte-aligned bulk copy.  Positions are held twice:
+//   * relative to the tile's centre O (the midpoint of its bounding box) as
+//     single FP32 values.  A thread forms, once per tile, the offset
+//     o = O - x_i of its i-particle in double-single arithmetic rounded to
+//     FP32, and per pair dx = (x_j - O) + o: one addition per component.
+//     The rounding of x_j - O is at most 2^-24 of the tile radius R, so dx
+//     carries an absolute error below 2^-22 (R + |dx|) per component, within
+//     2^-21 |dx| for the tiles this path is used for (|o| >= 2R);
+//   * as double-single hi/lo pairs, for the tiles near the warp's i-particles
+//     (|o| < 2R for one of them): dx = (hi_j - hi_i) + (lo_j - lo_i), three
+//     additions per component, error 2^-23 |dx|.
 constexpr int JT = 128;
-enum JField { F_XH = 0, F_YH, F_ZH, F_XL, F_YL, F_ZL, F_VX, F_VY, F_VZ, F_MN, NFIELD };
-constexpr int TILE_FLOATS = NFIELD * JT + 4;
+enum JField {
+  F_XR = 0, F_YR, F_ZR, F_VX, F_VY, F_VZ, F_MN,   // far tiles read these 7
+  F_XH, F_YH, F_ZH, F_XL, F_YL, F_ZL,             // near tiles: velocity, mass and these
+  NFIELD
+};
+constexpr int NFIELD_REL = F_MN + 1;
+constexpr int TILE_META = 12;
+constexpr int TILE_FLOATS = NFIELD * JT + TILE_META;
 constexpr int TILE_BYTES = TILE_FLOATS * 4;
 static_assert(TILE_BYTES % 16 == 0, "tile must be a multiple of 16 bytes");
 // F_MN holds -m/2: the force loop forms -2/r in its Newton step, so that
 // (-m/2)*(-2/r) = m/r needs no negation.
-// metadata: [0] = max |v_j| over the tile (rounded up), [1] = sqrt(max m_j)
-// (rounded up), [2] = number of real bodies in the tile, [3] unused.
+// metadata (float offsets from NFIELD*JT):
+//   [0] max |v_j| over the tile (rounded up)   [1] sqrt(max m_j) (rounded up)
+//   [2] number of real bodies                  [3] tile radius R (rounded up)
+//   [4..6] hi parts of O (x, y, z)              [7] unused
+//   [8..10] lo parts of O                       [11] unused
+enum TileMeta { M_VMAX = 0, M_SMAX, M_COUNT, M_RAD, M_OH = 4, M_OL = 8 };
 
 // FP64 j tile for the plain FP64 kernel (three bulk copies per tile).
 constexpr int JT64 = 64;

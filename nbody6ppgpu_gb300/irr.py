@@ -124,4 +124,25 @@ class IrrSimd:
         self.lib.irr_simd_profile_(C.byref(C.c_int(0)))
 
 
-__all__ = ["IrrSimd", "GpunbError"]
+__all__ = ["IrrSimd", "GpunbError", "send_predicted"]
+
+
+def send_predicted(time: float, body, ifirst: int = 1, ntot: int | None = None):
+    """gpunb_send_predicted_: predict bodies ifirst..ntot (1-based) to `time`
+    from the state stored with IrrSimd.set_jp and upload them as the
+    regular-force j-set (needs an open GpuNb and an open IrrSimd).  Returns
+    the predicted X and XDOT of those bodies."""
+    lib = load()
+    fn = lib.gpunb_send_predicted_
+    fn.argtypes = [_I, _I, _D, _D, _D, _D]
+    fn.restype = None
+    body = np.ascontiguousarray(body, dtype=np.float64)
+    if ntot is None:
+        ntot = ifirst + len(body) - 1
+    n = ntot - ifirst + 1
+    x = np.zeros((max(n, 1), 3))
+    xd = np.zeros((max(n, 1), 3))
+    fn(C.byref(C.c_int(ifirst)), C.byref(C.c_int(ntot)), C.byref(C.c_double(time)), _dp(body),
+       _dp(x), _dp(xd))
+    _check(lib)
+    return x[:n], xd[:n]

@@ -163,3 +163,32 @@ def test_device_resident_entry_point():
     st.synchronize()
     _check_fp64(A.cpu().numpy(), J.cpu().numpy(), NID.cpu().numpy(), g["fp64_acc"],
                 g["fp64_jrk"], g["fp64_nnbid"])
+
+
+def test_send_predicted_equals_host_prediction_then_send():
+    """gpunb_send_predicted_ returns the xbpredall.f prediction and leaves the
+    library in the state gpunb_send_ of those arrays would: the next regular
+    force is the same, bit for bit."""
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    from nbody6ppgpu_gb300.irr import send_predicted
+    g = load_golden("irr_plummer2048")
+    n = len(g["m"])
+    ti = float(g["ti"])
+    x0, v0, f, fdot, m, t0 = (g[k] for k in ("x0", "v0", "f", "fdot", "m", "t0"))
+    s = (ti - t0)[:, None]
+    X = ((fdot * s + f) * s + v0) * s + x0          # xbpredall.f:21-26
+    XD = (fdot * 1.5 * s + f) * 2.0 * s + v0
+    ifirst = 5                                        # bodies 1-4 stand for KS components
+    sl = slice(ifirst - 1, n)
+    act = np.arange(0, n - ifirst + 1, 7)
+    h2 = np.full(act.size, 0.01)
+    dtr = np.full(act.size, 1e-3)
+    with _irr(g), GpuNb(n) as nb:
+        xp, vp = send_predicted(ti, m[sl], ifirst, n)
+        np.testing.assert_allclose(xp, X[sl], rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(vp, XD[sl], rtol=1e-13, atol=1e-15)
+        r1 = nb.regf(h2, dtr, xp[act], vp[act], 129, 128)
+        nb.send(m[sl], xp, vp)
+        r2 = nb.regf(h2, dtr, xp[act], vp[act], 129, 128)
+    for a, b in ((r1.acc, r2.acc), (r1.jrk, r2.jrk), (r1.pot, r2.pot), (r1.list, r2.list)):
+        assert np.array_equal(a, b)
