@@ -5,8 +5,10 @@ predictor with the plain rule as fallback.
 
 1. Harvest (features, label) pairs by running the regular-step driver with the
    plain rule on two seeded clusters (the pairs the integrator itself
-   generates).
-2. Train the MLP on the GPU kernels (Adam, FP32 master, BF16 weights).
+   generates); train the MLP on the GPU kernels (Adam, FP32 master, BF16
+   weights).
+2. Harvest again on the same seeds with the predictor in the loop, and refit
+   on all pairs (rounds = 2, the default).
 3. Run a third seeded cluster twice from the same state -- plain rule, and
    predictor + fallback -- and compare list-overflow recomputes after the
    first block (the first block is identical for both), the membership
@@ -41,25 +43,33 @@ def make(model: str, n: int, seed: int, target: float, q: float = 0.5):
 
 
 def run(model="king", n=16384, ticks=64, nnbopt=100, nnbmax=200, levels=6, epochs=25,
-        train_seeds=(11, 12), eval_seed=13, q=0.5):
-    t0 = time.perf_counter()
+        train_seeds=(11, 12), eval_seed=13, q=0.5, rounds=2):
+    """rounds > 1: after the first fit, harvest again on the training seeds
+    with the predictor in the loop (the states it leads to), add those pairs
+    and refit -- the usual remedy for the shift between the plain rule's
+    states and the predictor's."""
+    t_harvest = t_train = 0.0
     X, Y = [], []
-    for s in train_seeds:
-        h = Harness(make(model, n, s, nnbopt, q), nnbopt, nnbmax, harvest=True, levels=levels)
-        h.run(ticks)
-        x, y = h.dataset()
-        h.close()
-        X.append(x)
-        Y.append(y)
+    mlp = None
+    for rnd in range(rounds):
+        t0 = time.perf_counter()
+        for s in train_seeds:
+            h = Harness(make(model, n, s, nnbopt, q), nnbopt, nnbmax, harvest=True, levels=levels)
+            h.run(ticks, predictor=mlp)
+            x, y = h.dataset()
+            h.close()
+            X.append(x)
+            Y.append(y)
+        t_harvest += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        mlp = RSMLP(seed=3)
+        losses = mlp.train(np.concatenate(X), np.concatenate(Y), epochs=epochs)
+        t_train += time.perf_counter() - t0
     X = np.concatenate(X)
     Y = np.concatenate(Y)
-    t_harvest = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    mlp = RSMLP(seed=3)
-    losses = mlp.train(X, Y, epochs=epochs)
-    t_train = time.perf_counter() - t0
     c = make(model, n, eval_seed, nnbopt, q)
-    out = {"model": model, "q": q, "n": n, "ticks": ticks, "nnbopt": nnbopt, "nnbmax": nnbmax,
+    out = {"model": model, "q": q, "n": n, "ticks": ticks, "rounds": rounds, "nnbopt": nnbopt,
+           "nnbmax": nnbmax,
            "levels": levels, "train_pairs": int(len(X)), "label_variance": float(Y.var()),
            "train_mse_first_epoch": losses[0], "train_mse_last_epoch": losses[-1],
            "harvest_s": t_harvest, "train_s": t_train}
@@ -87,9 +97,11 @@ def main():
     ap.add_argument("--levels", type=int, default=6)
     ap.add_argument("--q", type=float, default=0.5, help="virial ratio of the start")
     ap.add_argument("--epochs", type=int, default=25)
+    ap.add_argument("--rounds", type=int, default=2,
+                    help="harvest rounds (later ones with the predictor in the loop)")
     a = ap.parse_args()
     print(json.dumps(run(a.model, a.n, a.ticks, a.nnbopt, a.nnbmax, a.levels, epochs=a.epochs,
-                         q=a.q)), flush=True)
+                         q=a.q, rounds=a.rounds)), flush=True)
 
 
 if __name__ == "__main__":

@@ -146,7 +146,7 @@ def test_predictor_cuts_overflow_recomputes():
     pytest.importorskip("scipy")
     from nbody6ppgpu_gb300.rs_experiment import run
     r = run(model="king", n=8192, ticks=256, nnbopt=100, nnbmax=200, levels=6, epochs=25,
-            q=0.1)
+            rounds=1, q=0.1)
     plain, pred = r["plain"], r["predictor"]
     assert plain["overflow_events"] >= 200            # the regime does overflow
     assert pred["overflow_events"] * 3 <= plain["overflow_events"]
