@@ -538,6 +538,14 @@ def main():
     peak_mhz = clk.get("sm_max_mhz") or 2070.0
     peak = fp32_peak_tflops(n_sm, peak_mhz)
     load_mhz = clk.get("sm_mhz") or peak_mhz
+    # measured FP32 throughput of this device (packed FMA chains, the pair
+    # loop's instruction), after the timed region
+    import ctypes as _C
+    lib.gpunb_fp32_peak.argtypes = [_C.POINTER(_C.c_float), _C.POINTER(_C.c_float)]
+    lib.gpunb_fp32_peak.restype = _C.c_int
+    _tf, _ms = _C.c_float(0), _C.c_float(0)
+    peak_meas = float(_tf.value) if lib.gpunb_fp32_peak(_C.byref(_tf), _C.byref(_ms)) == 0 \
+        else None
 
     # ---- accuracy of the split kernel against the FP64 kernel ------------
     nb.set_precision("split")
@@ -626,6 +634,8 @@ def main():
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved_tflops / peak,
                      "frac_at_load_clock": achieved_tflops / fp32_peak_tflops(n_sm, load_mhz),
+                     "peak_measured_fp32": peak_meas,
+                     "frac_of_measured_fp32": (achieved_tflops / peak_meas) if peak_meas else None,
                      "traffic": read_traffic(),
                      "kernel": "regf_ds_kernel (ni=65536 block)",
                      "kernel_ms": k_ms, "flops_per_pair": FLOPS_PER_PAIR,

@@ -169,6 +169,12 @@ void gpunb_set_graphs(int flag);
 int gpupot_device_noalloc(int istart, int ni, int n, const double *m, const double *x,
                           double *pot, void *stream);
 
+/* Measured FP32 throughput of this device (no reference counterpart): a
+ * kernel of independent packed f32x2 FMA chains, the instruction of the pair
+ * loop; *tflops = achieved FP32 TFLOP/s, *ms = its duration.  The roofline
+ * denominator of the regular-force kernel. */
+int gpunb_fp32_peak(float *tflops, float *ms);
+
 /* Predict-and-send (no reference counterpart; replaces the host prediction
  * of src/Main/xbpredall.f:16-27 followed by GPUNB_SEND at intgrt.F:916-918).
  * Predicts bodies *ifirst .. *ntot (1-based) to *time from the state stored

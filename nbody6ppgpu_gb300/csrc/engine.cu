@@ -405,21 +405,12 @@ static int plan_splits(int variant, int ni, int ntile, bool mflag) {
 
 // Shapes measured on GB300 (autotuner sweeps, N = 65536 Plummer and N = 2^20
 // King): below 512 i-particles one warp of 32 i with the j tile split over 8
-// warps (variant 2); otherwise 4 warps x 32 i, reading 8 j per warp vote
-// (variant 6, 4 blocks per SM) when the items are long (4 tiles or more),
-// and 4 j per vote (variant 4, 5 blocks per SM) when they are short.
+// warps (variant 2); up to 8191 4 warps x 32 i reading 4 j per warp vote
+// (variant 4, 5 blocks per SM); from 8192 on 8 j per vote (variant 6, 4
+// blocks per SM).
 static void heuristic_plan(int ni, int ntile, bool mflag, int &variant, int &splits) {
-  if (ni < 512) {
-    variant = 2;
-    splits = plan_splits(variant, ni, ntile, mflag);
-    return;
-  }
-  variant = 6;
+  variant = ni < 512 ? 2 : (ni < 8192 ? 4 : 6);
   splits = plan_splits(variant, ni, ntile, mflag);
-  if ((long long)ntile < 4ll * splits) {
-    variant = 4;
-    splits = plan_splits(variant, ni, ntile, mflag);
-  }
 }
 
 static void fp64_plan(int ni, int ntile64, int &gx, int &splits) {

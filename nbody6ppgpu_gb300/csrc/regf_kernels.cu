@@ -5,9 +5,11 @@
 // the host prefix sum / merge of gpunb.velocity.cu:793-878.
 //
 // Pipeline for one gpunb_regf_ call (all on one stream):
-//   regf_ds_kernel<...>   pair loop, grid (i-tiles x j-splits), partial sums
-//   regf_merge_kernel     FP64 sum of the j-split partials in fixed order,
-//                         neighbour count -> in-band overflow flag
+//   regf_prep_kernel      FP32 i-records in Morton processing order
+//   regf_ds_kernel<...>   persistent pair loop over (i-tile, j-split) work
+//                         items from a device queue, partial sums per split
+//   regf_merge_(wide_)kernel  FP64 sum of the j-split partials in fixed
+//                         order, neighbour count -> in-band overflow flag
 //   list_scan_*           exclusive scan of accepted row lengths
 //   list_gather_kernel    per-row sort (ascending j) + compaction
 #include "regf_kernels.cuh"

@@ -7,8 +7,8 @@ predictor with the plain rule as fallback.
    plain rule on two seeded clusters (the pairs the integrator itself
    generates); train the MLP on the GPU kernels (Adam, FP32 master, BF16
    weights).
-2. Harvest again on the same seeds with the predictor in the loop, and refit
-   on all pairs (rounds = 2, the default).
+2. Optionally (rounds = 2) harvest again on the same seeds with the
+   predictor in the loop, and refit on all pairs.
 3. Run a third seeded cluster twice from the same state -- plain rule, and
    predictor + fallback -- and compare list-overflow recomputes after the
    first block (the first block is identical for both), the membership
@@ -43,7 +43,7 @@ def make(model: str, n: int, seed: int, target: float, q: float = 0.5):
 
 
 def run(model="king", n=16384, ticks=64, nnbopt=100, nnbmax=200, levels=6, epochs=25,
-        train_seeds=(11, 12), eval_seed=13, q=0.5, rounds=2):
+        train_seeds=(11, 12), eval_seed=13, q=0.5, rounds=1):
     """rounds > 1: after the first fit, harvest again on the training seeds
     with the predictor in the loop (the states it leads to), add those pairs
     and refit -- the usual remedy for the shift between the plain rule's
@@ -97,7 +97,7 @@ def main():
     ap.add_argument("--levels", type=int, default=6)
     ap.add_argument("--q", type=float, default=0.5, help="virial ratio of the start")
     ap.add_argument("--epochs", type=int, default=25)
-    ap.add_argument("--rounds", type=int, default=2,
+    ap.add_argument("--rounds", type=int, default=1,
                     help="harvest rounds (later ones with the predictor in the loop)")
     a = ap.parse_args()
     print(json.dumps(run(a.model, a.n, a.ticks, a.nnbopt, a.nnbmax, a.levels, epochs=a.epochs,
