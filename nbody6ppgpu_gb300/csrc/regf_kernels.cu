@@ -39,15 +39,24 @@ namespace gpunb {
 // Tile slot p holds body perm[p] (identity when perm is null; perm[p] = -1
 // marks a padding slot).
 
-// block-wide max / min of one double (JT threads), result in every thread
-__device__ __forceinline__ double block_max(double a, double *s) {
-  for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+// block-wide maxima of NV doubles (JT threads), results in every thread
+template <int NV>
+__device__ __forceinline__ void block_max(double (&a)[NV], double (*s)[NV]) {
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    for (int o = 16; o > 0; o >>= 1) a[q] = fmax(a[q], __shfl_xor_sync(0xffffffffu, a[q], o));
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) s[threadIdx.x >> 5][q] = a[q];
+  }
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = a;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    double r = s[0][q];
+    for (int w = 1; w < JT / 32; ++w) r = fmax(r, s[w][q]);
+    a[q] = r;
+  }
   __syncthreads();
-  double r = s[0];
-  for (int w = 1; w < JT / 32; ++w) r = fmax(r, s[w]);
-  return r;
 }
 
 __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restrict__ m,
@@ -57,7 +66,8 @@ __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restric
                                                          float *__restrict__ tiles, int *err) {
   const int t = blockIdx.x, l = threadIdx.x, p = t * JT + l;
   float *T = tiles + (size_t)t * TILE_FLOATS;
-  __shared__ double s_red[JT / 32];
+  __shared__ double s_red6[JT / 32][6];
+  __shared__ double s_red4[JT / 32][4];
   const int j = perm ? perm[p] : (p < nj ? p : -1);   // -1: padding slot
   double xj[3] = {0.0, 0.0, 0.0}, vj[3] = {0.0, 0.0, 0.0}, mj = 0.0;
   if (j >= 0) {
@@ -72,11 +82,17 @@ __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restric
       raise_error(err, GPUNB_E_NAN);
   }
   // tile centre: midpoint of the real bodies' bounding box
+  double bb[6];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    bb[c] = j >= 0 ? xj[c] : -INFINITY;        // max
+    bb[3 + c] = j >= 0 ? -xj[c] : -INFINITY;   // -min
+  }
+  block_max<6>(bb, s_red6);
   double o[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const double hi = block_max(j >= 0 ? xj[c] : -INFINITY, s_red);
-    const double lo = -block_max(j >= 0 ? -xj[c] : -INFINITY, s_red);
+    const double hi = bb[c], lo = -bb[3 + c];
     o[c] = (hi >= lo) ? 0.5 * lo + 0.5 * hi : 0.0;   // no real body: O = 0
     if (isnan(o[c])) o[c] = 0.0;
   }
@@ -108,11 +124,10 @@ __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restric
     T[F_MN * JT + l] = -0.f;
   }
   // tile maxima of |v|, m and |x - O|, rounded up when narrowed; body count
-  const double vm = block_max(j >= 0 ? sqrt(vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2]) : 0.0,
-                              s_red);
-  const double mm = block_max(mj, s_red);
-  const double rad = block_max(sqrt(r2), s_red);
-  const double nr = block_max(j >= 0 ? (double)(l + 1) : 0.0, s_red);   // slots fill from 0
+  double mx[4] = {j >= 0 ? sqrt(vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2]) : 0.0, mj,
+                  sqrt(r2), j >= 0 ? (double)(l + 1) : 0.0};   // real slots fill from 0
+  block_max<4>(mx, s_red4);
+  const double vm = mx[0], mm = mx[1], rad = mx[2], nr = mx[3];
   if (l == 0) {
     float *M = T + NFIELD * JT;
     M[M_VMAX] = (float)(vm * (1.0 + 0x1p-20));
@@ -766,22 +781,42 @@ __global__ void __launch_bounds__(MERGE_THREADS)
   }
 }
 
-__global__ void regf_merge_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
-                                  const int *__restrict__ perm, const int *__restrict__ cnt,
-                                  int nnbmax, double *__restrict__ acc, double *__restrict__ jrk,
-                                  double *__restrict__ pot, int *__restrict__ nnb,
-                                  int *__restrict__ rowlen) {
-  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-  if (slot >= ni) return;
+// Large blocks: a block of MERGE_KW warps per 32 consecutive slots, lane =
+// slot, warp w summing the splits w, w + MERGE_KW, ... in order (reads
+// coalesced across the warp), then the MERGE_KW partial sums of a slot added
+// in warp order: the same FP64 order in every run, with MERGE_KW times the
+// memory parallelism of a thread per slot.
+constexpr int MERGE_KW = 8;
+__global__ void __launch_bounds__(32 * MERGE_KW)
+    regf_merge_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
+                      const int *__restrict__ perm, const int *__restrict__ cnt, int nnbmax,
+                      double *__restrict__ acc, double *__restrict__ jrk, double *__restrict__ pot,
+                      int *__restrict__ nnb, int *__restrict__ rowlen) {
+  __shared__ double sh[MERGE_KW][NQ][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int slot = blockIdx.x * 32 + lane;
   double s[NQ];
 #pragma unroll
   for (int c = 0; c < NQ; ++c) s[c] = 0.0;
-  for (int k = 0; k < S; ++k) {
-    const double *p = part + (size_t)k * NQ * ni_pad + slot;
+  if (slot < ni) {
+    for (int k = w; k < S; k += MERGE_KW) {
+      const double *p = part + (size_t)k * NQ * ni_pad + slot;
 #pragma unroll
-    for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * ni_pad];
+      for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * ni_pad];
+    }
   }
-  merge_store(s, perm ? perm[slot] : slot, cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
+#pragma unroll
+  for (int c = 0; c < NQ; ++c) sh[w][c][lane] = s[c];
+  __syncthreads();
+  if (w == 0 && slot < ni) {
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) {
+      double t = sh[0][c][lane];
+      for (int u = 1; u < MERGE_KW; ++u) t += sh[u][c][lane];
+      s[c] = t;
+    }
+    merge_store(s, perm ? perm[slot] : slot, cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
+  }
 }
 
 // Batched clusters: one block per i-tile; the tile's splits are the partial
@@ -1095,8 +1130,9 @@ cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, con
     regf_merge_wide_kernel<<<ni, MERGE_THREADS, 0, st>>>(part, S, ni, ni_pad, perm, cnt, nnbmax,
                                                          acc, jrk, pot, nnb, rowlen);
   else
-    regf_merge_kernel<<<(ni + 255) / 256, 256, 0, st>>>(part, S, ni, ni_pad, perm, cnt, nnbmax,
-                                                        acc, jrk, pot, nnb, rowlen);
+    regf_merge_kernel<<<(ni + 31) / 32, 32 * MERGE_KW, 0, st>>>(part, S, ni, ni_pad, perm, cnt,
+                                                                nnbmax, acc, jrk, pot, nnb,
+                                                                rowlen);
   return cudaGetLastError();
 }
 
