@@ -394,6 +394,31 @@ def irregular_leg(c, h2, lists_src, cpu: bool):
     return out
 
 
+def potential_leg(c, cpu: bool):
+    """gpupot_ (the energy check's potential, gpupot.gpu.cu:61-127) over all
+    bodies of the bench cluster, host ABI, against the FP32 port on the host
+    cores and the FP64 oracle on a sample."""
+    from nbody6ppgpu_gb300.gpunb import gpupot
+    n = c.n
+    gpupot(c.m, c.x)
+    best = 1e9
+    for _ in range(5):
+        t = time.perf_counter()
+        p = gpupot(c.m, c.x)
+        best = min(best, time.perf_counter() - t)
+    out = {"workload": "Plummer N=65536 (the bench cluster), all bodies, host ABI",
+           "ms": best * 1e3, "gpairs_s": n * n / best / 1e9}
+    if cpu:
+        from oracle import oracle as O
+        t = time.perf_counter()
+        O.Port.pot(c.m, c.x)
+        dt = time.perf_counter() - t
+        out["cpu_port_gpairs_s"] = n * n / dt / 1e9
+        ref = O.pot_fp64(c.m, c.x, 1, 2048)
+        out["max_rel_err_vs_fp64_oracle"] = float(np.max(np.abs(p[:2048] - ref) / ref))
+    return out
+
+
 def rs_predictor_leg(dev):
     """Inference of the neighbour-radius MLP for 2^20 particles (one forward
     kernel): 2^20 x (8*64 + 64*64 + 64) multiply-adds."""
@@ -604,6 +629,7 @@ def main():
         lists_by_particle = np.zeros_like(outs[65536].list)
         lists_by_particle[acts[65536]] = outs[65536].list
         irr = irregular_leg(c, h2, lists_by_particle, cpu=(rank == 0 and not args.no_cpu_baseline))
+    pot = potential_leg(c, cpu=(rank == 0 and not args.no_cpu_baseline))
     king = None
     if not args.no_large:
         king = king1m_leg(n_sm, peak_mhz)
@@ -657,6 +683,7 @@ def main():
         line["king1m"] = king
     if irr is not None:
         line["irregular"] = irr
+    line["potential"] = pot
     line["rs_predictor_inference"] = rsp
     if rank == 0:
         print(json.dumps(line), flush=True)
