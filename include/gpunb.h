@@ -215,6 +215,33 @@ int gpunb_rsmlp_backward(int B, const float *X, const float *T, const float *W, 
 int gpunb_rsmlp_adam(float *wf, float *m1, float *m2, const float *grad, float lr, float beta1,
                      float beta2, float eps, int step, void *wq, void *stream);
 
+/* RS update of an active block on the device (no reference counterpart: the
+ * reference runs src/Main/regcor_gpu.F:120-253 on the host, one particle at a
+ * time).  Plain rule as regcor_gpu.F (with the few-member rule of
+ * fpoly0.F:153-158 for counts below 2 when few_nb_rule), and, when wq is not
+ * NULL, the MLP proposal from the 8 features of each particle normalised by
+ * norm[0..7] (mean) and norm[8..15] (spread), taken where the count it implies
+ * at the current density stays within 0.5-1.5 x the rule's target.  Inputs per
+ * active particle i < ni: x, v ([ni][3]), m_scaled (mass x N), rs, nnb (count,
+ * self excluded), nnb0 (previous count), acc, jrk ([ni][3], regular force and
+ * derivative; only read with wq), dtr.  Outputs rs_new[ni], and when not NULL
+ * target[ni] (the rule's membership target) and used[ni] (1: MLP value).
+ * All pointers are device memory (p is a host struct). */
+typedef struct {
+  int nnbopt, nnbmax;       /* NNBOPT, NNBMAX */
+  int nb_flag;              /* 1: KZ(39) = 0 or 2 (distances from the density centre) */
+  int few_nb_rule;          /* 1: counts below 2 take 1.5 RS (fpoly0.F:153-158) */
+  double rscale, rc, rsfac; /* RSCALE, RC, RSFAC */
+  double bodym;             /* mean mass */
+  double rdens[3];          /* density centre RDENS */
+} gpunb_rs_params;
+int gpunb_rs_update_device(int ni, const gpunb_rs_params *p, const double *x, const double *v,
+                           const double *m_scaled, const double *rs, const int *nnb,
+                           const int *nnb0, const double *acc, const double *jrk,
+                           const double *dtr, const void *wq, const float *wf,
+                           const float *norm, double *rs_new, double *target, int *used,
+                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif

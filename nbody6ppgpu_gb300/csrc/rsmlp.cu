@@ -61,16 +61,7 @@ __device__ void stage_params(MlpSmem &s, const __nv_bfloat16 *__restrict__ wq,
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(MLP_THREADS)
-    rsmlp_forward_kernel(int B, const float *__restrict__ X, const __nv_bfloat16 *__restrict__ wq,
-                         const float *__restrict__ wf, float *__restrict__ y) {
-  __shared__ MlpSmem s;
-  stage_params(s, wq, wf);
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  float x[MLP_IN];
-#pragma unroll
-  for (int f = 0; f < MLP_IN; ++f) x[f] = X[(size_t)b * MLP_IN + f];
+__device__ __forceinline__ float mlp_eval(const MlpSmem &s, const float (&x)[MLP_IN]) {
   float h1[MLP_H];
 #pragma unroll
   for (int o = 0; o < MLP_H; ++o) {
@@ -86,7 +77,131 @@ __global__ void __launch_bounds__(MLP_THREADS)
     for (int k = 0; k < MLP_H; ++k) a = fmaf(s.w2[o * MLP_H + k], h1[k], a);
     out = fmaf(s.w3[o], gelu(a), out);
   }
-  y[b] = out;
+  return out;
+}
+
+__global__ void __launch_bounds__(MLP_THREADS)
+    rsmlp_forward_kernel(int B, const float *__restrict__ X, const __nv_bfloat16 *__restrict__ wq,
+                         const float *__restrict__ wf, float *__restrict__ y) {
+  __shared__ MlpSmem s;
+  stage_params(s, wq, wf);
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  float x[MLP_IN];
+#pragma unroll
+  for (int f = 0; f < MLP_IN; ++f) x[f] = X[(size_t)b * MLP_IN + f];
+  y[b] = mlp_eval(s, x);
+}
+
+// ---------------------------------------------------------------------------
+// RS update of an active block on the device: the plain rule of
+// src/Main/regcor_gpu.F:120-253 (NNBOPT stabilisation, NBAVE cap, taper,
+// inertial and radial-velocity factors, RSFAC limit, second-order cube root,
+// shell square root, inward reduction; the zero-neighbour branch :120-143),
+// optionally the few-member rule of fpoly0.F:153-158, and -- with weights --
+// the learned proposal: features, MLP, and the plain rule as fallback when the
+// count it implies at the current density leaves 0.5-1.5 x the rule's target.
+__device__ void rs_plain(const gpunb_rs_params &p, double rs, int nnb, int nnb0,
+                         const double *x, const double *v, double dtr, double &out,
+                         double &target) {
+  const double znbmin = fmax(0.01 * p.nnbmax, 1.0);
+  const double d0 = x[0] - p.rdens[0], d1 = x[1] - p.rdens[1], d2 = x[2] - p.rdens[2];
+  double ri2, rh2;
+  if (p.nb_flag) {
+    ri2 = d0 * d0 + d1 * d1 + d2 * d2;
+    rh2 = p.rscale * p.rscale;
+  } else {
+    ri2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+    rh2 = 9.0 * p.rscale * p.rscale;
+  }
+  const double rc2 = p.rc * p.rc;
+  if (nnb == 0) {
+    const double rdot = x[0] * v[0] + x[1] * v[1] + x[2] * v[2];
+    out = rdot > 0.0 ? fmax(0.75 * rs, 0.1 * p.rscale) : 1.1 * rs;
+    target = (double)p.nnbopt;
+    return;
+  }
+  const double n = (double)nnb;
+  const double fac = 1.0 + 0.1 * ((double)p.nnbopt - n) / n;
+  double a3 = n * fac;
+  const double nbave =
+      (double)min(p.nnbopt + 150, max(p.nnbmax - 50, (int)znbmin));
+  a3 = fmin(a3, 0.9 * nbave);
+  const long long nbp = (long long)a3;
+  if (p.nb_flag)
+    a3 = ri2 > rh2 ? a3 * fmax(p.rscale / sqrt(ri2), 0.1) : fmax(a3, znbmin);
+  else
+    a3 = fmax(a3, znbmin);
+  target = a3;
+  double a4 = a3 / n;
+  if ((a3 - (double)nnb0) * (a3 - n) < 0.0) a4 = sqrt(a4);
+  const double ridot = d0 * v[0] + d1 * v[1] + d2 * v[2];
+  if (p.nb_flag && ri2 > rc2 && ri2 < 100.0 * rh2) a4 = a4 * (1.0 + ridot * dtr / ri2);
+  const double a5 = fmin(p.rsfac * dtr, 0.25);
+  a4 = a4 - 1.0;
+  a4 = a4 > a5 ? a5 : fmax(a4, -a5);
+  const double a3v = a4 / 3.0;
+  double a1 = 1.0 + a3v - a3v * a3v;
+  if (n < znbmin && (double)nbp > znbmin && a1 < 1.0) a1 = 1.05;
+  const bool change = fabs(a1 - 1.0) > 0.003;
+  const bool shell = rs * rs > ri2 && rs * rs < 2.0 * ri2 && n > 5.0;
+  if (change && shell) a1 = sqrt(fmax(a1, 0.0));
+  double nw = change ? a1 * rs : rs;
+  if (n > nbave && ridot < 0.0) nw = nw * (1.0 - (n - nbave) / (3.0 * n));
+  out = nw;
+}
+
+__global__ void __launch_bounds__(MLP_THREADS)
+    rs_update_kernel(int ni, gpunb_rs_params p, const double *__restrict__ x,
+                     const double *__restrict__ v, const double *__restrict__ m_scaled,
+                     const double *__restrict__ rs, const int *__restrict__ nnb,
+                     const int *__restrict__ nnb0, const double *__restrict__ acc,
+                     const double *__restrict__ jrk, const double *__restrict__ dtr,
+                     const __nv_bfloat16 *__restrict__ wq, const float *__restrict__ wf,
+                     const float *__restrict__ norm, double *__restrict__ rs_new,
+                     double *__restrict__ target, int *__restrict__ used) {
+  __shared__ MlpSmem s;
+  if (wq) stage_params(s, wq, wf);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ni) return;
+  const double *xi = x + 3 * (size_t)i, *vi = v + 3 * (size_t)i;
+  const int n = nnb[i];
+  const double r0 = rs[i];
+  double plain, tgt;
+  rs_plain(p, r0, n, nnb0[i], xi, vi, dtr[i], plain, tgt);
+  if (p.few_nb_rule && n < 2) plain = 1.5 * r0;
+  double nw = plain;
+  int u = 0;
+  if (wq) {
+    // features (rsmlp.py): log distance to the centre, log local density,
+    // count / NNBOPT, log |F_reg|, log |jerk|, log regular step, log mass N,
+    // log RS; normalised with the training set's mean and spread
+    const double e0 = xi[0] - p.rdens[0], e1 = xi[1] - p.rdens[1], e2 = xi[2] - p.rdens[2];
+    const double nn = (double)max(n, 0);
+    const double *a = acc + 3 * (size_t)i, *j = jrk + 3 * (size_t)i;
+    const double f[MLP_IN] = {
+        log(sqrt(e0 * e0 + e1 * e1 + e2 * e2) + 1e-6),
+        log((nn + 1.0) / (4.0 / 3.0 * 3.141592653589793 * r0 * r0 * r0)),
+        nn / (double)p.nnbopt,
+        log(sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) + 1e-30),
+        log(sqrt(j[0] * j[0] + j[1] * j[1] + j[2] * j[2]) + 1e-30),
+        log(fmax(dtr[i], 1e-12)),
+        log(fmax(m_scaled[i], 1e-12)),
+        log(r0)};
+    float xf[MLP_IN];
+#pragma unroll
+    for (int q = 0; q < MLP_IN; ++q)
+      xf[q] = (float)((f[q] - (double)norm[q]) / (double)norm[MLP_IN + q]);
+    const float y = mlp_eval(s, xf);
+    const double pc = (nn + 1.0) * exp(3.0 * (double)y) - 1.0;
+    if (isfinite(y) && pc >= 0.5 * tgt && pc <= 1.5 * tgt) {
+      nw = r0 * exp((double)y);
+      u = 1;
+    }
+  }
+  rs_new[i] = nw;
+  if (target) target[i] = tgt;
+  if (used) used[i] = u;
 }
 
 // Backward pass of the mean of w_b (y_b - t_b)^2 over the batch.  Each block
@@ -270,6 +385,22 @@ int gpunb_rsmlp_adam(float *wf, float *m1, float *m2, const float *grad, float l
   const float bc1 = 1.f - powf(beta1, (float)step), bc2 = 1.f - powf(beta2, (float)step);
   rsmlp_adam_kernel<<<(MLP_P + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
       wf, m1, m2, grad, lr, beta1, beta2, eps, bc1, bc2, (__nv_bfloat16 *)wq);
+  return cudaGetLastError() == cudaSuccess ? GPUNB_OK : GPUNB_E_CUDA;
+}
+
+int gpunb_rs_update_device(int ni, const gpunb_rs_params *p, const double *x, const double *v,
+                           const double *m_scaled, const double *rs, const int *nnb,
+                           const int *nnb0, const double *acc, const double *jrk,
+                           const double *dtr, const void *wq, const float *wf,
+                           const float *norm, double *rs_new, double *target, int *used,
+                           void *stream) {
+  if (ni < 0 || !p) return GPUNB_E_ARG;
+  if (ni == 0) return GPUNB_OK;
+  if (wq && (!wf || !norm || !acc || !jrk || !m_scaled)) return GPUNB_E_ARG;
+  rs_update_kernel<<<(ni + MLP_THREADS - 1) / MLP_THREADS, MLP_THREADS, 0,
+                     (cudaStream_t)stream>>>(ni, *p, x, v, m_scaled, rs, nnb, nnb0, acc, jrk, dtr,
+                                             (const __nv_bfloat16 *)wq, wf, norm, rs_new, target,
+                                             used);
   return cudaGetLastError() == cudaSuccess ? GPUNB_OK : GPUNB_E_CUDA;
 }
 

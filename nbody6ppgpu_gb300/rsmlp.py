@@ -192,3 +192,51 @@ class RSMLP:
 
     def params(self):
         return self.master.cpu().numpy().copy(), self.wq.float().cpu().numpy().copy()
+
+
+class RSParamsC(C.Structure):
+    """gpunb_rs_params (include/gpunb.h)."""
+    _fields_ = [("nnbopt", C.c_int), ("nnbmax", C.c_int), ("nb_flag", C.c_int),
+                ("few_nb_rule", C.c_int), ("rscale", C.c_double), ("rc", C.c_double),
+                ("rsfac", C.c_double), ("bodym", C.c_double), ("rdens", C.c_double * 3)]
+
+
+def rs_update_device(p, x, v, m_scaled, rs, nnb, nnb0, acc, jrk, dtr, mlp: "RSMLP | None" = None,
+                     few_nb_rule: bool = True, device: int = 0):
+    """gpunb_rs_update_device on host arrays (copied to the device and back):
+    the plain RS rule of `rsrule.regcor_rs` (with the few-member rule when
+    few_nb_rule) and, with `mlp`, the learned proposal and its fallback, in
+    one kernel.  p: rsrule.RSParams.  Returns (rs_new, target, used)."""
+    import torch
+    lib = load()
+    fn = lib.gpunb_rs_update_device
+    fn.argtypes = [C.c_int, C.POINTER(RSParamsC)] + [C.c_void_p] * 15
+    fn.restype = C.c_int
+    dev = torch.device("cuda", device)
+    ni = len(rs)
+
+    def d(a, dt=torch.float64):
+        return torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+
+    cp = RSParamsC(int(p.nnbopt), int(p.nnbmax), int(p.nb_flag), int(few_nb_rule),
+                   float(p.rscale), float(p.rc), float(p.rsfac), float(p.bodym),
+                   (C.c_double * 3)(0.0, 0.0, 0.0))
+    X, V, M, R = d(x), d(v), d(m_scaled), d(rs)
+    NB, NB0 = d(nnb, torch.int32), d(nnb0, torch.int32)
+    A, J, DT = d(acc), d(jrk), d(dtr)
+    out = torch.empty(ni, dtype=torch.float64, device=dev)
+    tgt = torch.empty_like(out)
+    used = torch.empty(ni, dtype=torch.int32, device=dev)
+    if mlp is not None:
+        norm = d(np.concatenate([mlp.mu, mlp.sd]).astype(np.float32), torch.float32)
+        wq, wf, nm = mlp.wq.data_ptr(), mlp.master.data_ptr(), norm.data_ptr()
+    else:
+        wq = wf = nm = None
+    torch.cuda.synchronize()
+    rc = fn(ni, C.byref(cp), X.data_ptr(), V.data_ptr(), M.data_ptr(), R.data_ptr(),
+            NB.data_ptr(), NB0.data_ptr(), A.data_ptr(), J.data_ptr(), DT.data_ptr(), wq, wf, nm,
+            out.data_ptr(), tgt.data_ptr(), used.data_ptr(), None)
+    if rc != 0:
+        raise RuntimeError(f"gpunb_rs_update_device failed ({rc})")
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), tgt.cpu().numpy(), used.cpu().numpy()

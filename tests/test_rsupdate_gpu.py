@@ -1,0 +1,69 @@
+"""The RS update on the device (gpunb_rs_update_device): the plain rule
+against rsrule.regcor_rs (itself checked against hand-worked cases of the
+Fortran), and the fused MLP proposal against the host path of the driver
+(features -> forward kernel -> band check -> fallback)."""
+import numpy as np
+import pytest
+
+from nbody6ppgpu_gb300 import rsrule
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0, 0.8, (n, 3)) * rng.choice([0.1, 1.0, 5.0], (n, 1))
+    v = rng.normal(0, 0.5, (n, 3))
+    nnb = rng.integers(0, 260, n)
+    nnb[:20] = 0                       # zero-neighbour branch
+    nnb[20:40] = 1                     # few-member rule
+    nnb0 = np.clip(nnb + rng.integers(-30, 30, n), 0, None)
+    rs = np.exp(rng.uniform(np.log(0.02), np.log(0.5), n))
+    r = np.linalg.norm(x, axis=1)
+    rs[40:80] = r[40:80] * rng.uniform(1.05, 1.35, 40)   # RS^2 in (r^2, 2 r^2): shell rule
+    dtr = rng.choice([0.0039, 0.0156, 0.0625, 0.125], n)
+    acc = rng.normal(0, 1, (n, 3))
+    jrk = rng.normal(0, 3, (n, 3))
+    m_scaled = rng.uniform(0.1, 20, n)
+    return x, v, m_scaled, rs, nnb, nnb0, acc, jrk, dtr
+
+
+@pytest.mark.parametrize("nb_flag", [1, 0])
+def test_plain_rule_matches_host(nb_flag):
+    pytest.importorskip("torch")
+    from nbody6ppgpu_gb300.rsmlp import rs_update_device
+    p = rsrule.RSParams(nnbopt=100, nnbmax=200, nb_flag=nb_flag, bodym=1e-4)
+    x, v, m, rs, nnb, nnb0, acc, jrk, dtr = _inputs(5000, 1 + nb_flag)
+    host, tgt = rsrule.regcor_rs(rs, nnb, nnb0, x, v, dtr, p, return_target=True)
+    got, gtgt, used = rs_update_device(p, x, v, m, rs, nnb, nnb0, acc, jrk, dtr,
+                                       few_nb_rule=False)
+    np.testing.assert_allclose(got, host, rtol=1e-13)
+    np.testing.assert_allclose(gtgt, tgt, rtol=1e-13)
+    assert not used.any()
+    few, _, _ = rs_update_device(p, x, v, m, rs, nnb, nnb0, acc, jrk, dtr, few_nb_rule=True)
+    want = np.where(nnb < 2, rsrule.few_nb_rs(rs), host)
+    np.testing.assert_allclose(few, want, rtol=1e-13)
+
+
+def test_fused_predictor_matches_host_path():
+    pytest.importorskip("torch")
+    from nbody6ppgpu_gb300.rsmlp import RSMLP, features, rs_update_device
+    p = rsrule.RSParams(nnbopt=100, nnbmax=200, bodym=1e-4)
+    x, v, m, rs, nnb, nnb0, acc, jrk, dtr = _inputs(4000, 7)
+    F = features(x, v, m, rs, nnb, acc, jrk, dtr, p.nnbopt)
+    mlp = RSMLP(seed=5)
+    rng = np.random.default_rng(3)
+    T = 0.2 * np.tanh(F[:, 1] - F[:, 1].mean()) + 0.05 * rng.normal(size=len(F))
+    mlp.train(F, T, epochs=3)                       # any fitted network will do
+    plain, tgt = rsrule.regcor_rs(rs, nnb, nnb0, x, v, dtr, p, return_target=True)
+    plain = np.where(nnb < 2, rsrule.few_nb_rs(rs), plain)
+    y = mlp.predict(F)
+    pc = (np.maximum(nnb, 0) + 1.0) * np.exp(3.0 * y.astype(np.float64)) - 1.0
+    ok = (pc >= 0.5 * tgt) & (pc <= 1.5 * tgt) & np.isfinite(y)
+    want = np.where(ok, rs * np.exp(y.astype(np.float64)), plain)
+    got, gtgt, used = rs_update_device(p, x, v, m, rs, nnb, nnb0, acc, jrk, dtr, mlp=mlp)
+    edge = (np.abs(pc - 0.5 * tgt) < 1e-4 * tgt) | (np.abs(pc - 1.5 * tgt) < 1e-4 * tgt)
+    assert np.array_equal(used.astype(bool)[~edge], ok[~edge])
+    assert ok.sum() > 100 and (~ok).sum() > 100       # both branches exercised
+    sel = ~edge
+    np.testing.assert_allclose(got[sel], want[sel], rtol=2e-5)
