@@ -1,0 +1,113 @@
+"""Size-independent properties of the regular force at the full size of the
+King W0=6, N = 2^20 workload, where the CPU oracle would take minutes:
+
+  * parity with the plain FP64 kernel on the same block (lists identical,
+    force and potential within the split-precision tolerance);
+  * mass scaling: doubling every mass doubles acc, jerk and pot bit for bit
+    (powers of two are exact in every FP32/FP64 operation) and keeps the lists;
+  * time reversal with dtr = 0: v -> -v leaves acc, pot and the lists
+    unchanged bit for bit and negates the jerk bit for bit;
+  * translation: shifting every body by the same vector keeps the lists and the
+    force within 1e-6 (only the rounding of the coordinates changes);
+  * permutation of the j-set: the lists map through the permutation.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_vec_err
+
+pytestmark = pytest.mark.gpu
+
+NI = 16384
+LMAX, NNBMAX = 1025, 1024
+
+
+@pytest.fixture(scope="module")
+def king():
+    from nbody6ppgpu_gb300 import ics
+    c = ics.king(1 << 20, seed=4, nb_target=100.0)
+    act = ics.active_set(c.n, NI, seed=NI)
+    return c, act
+
+
+def _regf(nb, c, act, m=None, x=None, v=None, dtr=None, h2=None):
+    m = c.m if m is None else m
+    x = c.x if x is None else x
+    v = c.v if v is None else v
+    dtr = c.dtr[act] if dtr is None else dtr
+    h2 = c.h2()[act] if h2 is None else h2
+    nb.send(m, x, v)
+    return nb.regf(h2, dtr, x[act], v[act], LMAX, NNBMAX)
+
+
+def test_full_size_parity_with_fp64_kernel(king):
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    c, act = king
+    with GpuNb(c.n) as nb:
+        r = _regf(nb, c, act)
+        nb.set_precision("fp64")
+        r64 = _regf(nb, c, act)
+    assert np.array_equal(r.list, r64.list)
+    ea = rel_vec_err(r.acc, r64.acc)
+    ej = rel_vec_err(r.jrk, r64.jrk)
+    ep = np.abs(r.pot - r64.pot) / np.abs(r64.pot)
+    assert np.percentile(ea, 99) < 1e-6 and ea.max() < 1e-5
+    assert np.percentile(ej, 99) < 1e-6 and ej.max() < 1e-5
+    assert ep.max() < 1e-6
+
+
+def test_mass_scaling_is_exact(king):
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    c, act = king
+    with GpuNb(c.n) as nb:
+        r1 = _regf(nb, c, act)
+        r2 = _regf(nb, c, act, m=2.0 * c.m)
+    assert np.array_equal(r1.list, r2.list)
+    assert np.array_equal(2.0 * r1.acc, r2.acc)
+    assert np.array_equal(2.0 * r1.jrk, r2.jrk)
+    assert np.array_equal(2.0 * r1.pot, r2.pot)
+
+
+def test_time_reversal_is_exact(king):
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    c, act = king
+    z = np.zeros(act.size)
+    with GpuNb(c.n) as nb:
+        r1 = _regf(nb, c, act, dtr=z)
+        r2 = _regf(nb, c, act, v=-c.v, dtr=z)
+    assert np.array_equal(r1.list, r2.list)
+    assert np.array_equal(r1.acc, r2.acc)
+    assert np.array_equal(r1.pot, r2.pot)
+    assert np.array_equal(-r1.jrk, r2.jrk)
+
+
+def test_translation_invariance(king):
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    c, act = king
+    shift = np.array([0.37, -1.25, 2.5])
+    with GpuNb(c.n) as nb:
+        r1 = _regf(nb, c, act)
+        r2 = _regf(nb, c, act, x=c.x + shift)
+    # the FP64 neighbour decision sees shifted coordinates: pairs whose
+    # criterion value lies within rounding of h2 may flip; none do here
+    assert np.array_equal(r1.list, r2.list)
+    assert np.percentile(rel_vec_err(r2.acc, r1.acc), 99) < 1e-6
+    assert np.max(np.abs(r2.pot - r1.pot) / r1.pot) < 1e-6
+
+
+def test_permutation_of_the_j_set(king):
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    c, act = king
+    perm = np.random.default_rng(8).permutation(c.n)
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(c.n)
+    with GpuNb(c.n) as nb:
+        r1 = _regf(nb, c, act)
+        nb.send(c.m[perm], c.x[perm], c.v[perm])
+        r2 = nb.regf(c.h2()[act], c.dtr[act], c.x[act], c.v[act], LMAX, NNBMAX)
+    assert np.array_equal(r1.list[:, 0], r2.list[:, 0])
+    for q in range(0, act.size, 97):
+        k = r1.list[q, 0]
+        got = np.sort(perm[r2.list[q, 1:1 + k]])
+        assert np.array_equal(got, r1.list[q, 1:1 + k])
+    assert np.percentile(rel_vec_err(r2.acc, r1.acc), 99) < 1e-6
