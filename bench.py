@@ -524,7 +524,8 @@ def main():
         lib.gpunb_set_timing(1)
         evs = []
         for _ in range(k):
-            flush.zero_()                      # L2 flush between steps (untimed)
+            with torch.cuda.stream(stream):    # L2 flush between steps, on the timed
+                flush.zero_()                  # stream before its start event (untimed)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
