@@ -558,6 +558,17 @@ def main():
     kt = np.asarray(kt).reshape(args.steps, len(BLOCKS))
     big = kt[:, BLOCKS.index(65536)]
     k_ms = float(np.mean(big))
+    # every block's pair kernel: duration, pairs/s and the bound that applies
+    # (small blocks read each j tile once: 52 B per body from L2/HBM, and are
+    # latency-bound; large ones are FP32-bound)
+    per_block = {}
+    for q, ni in enumerate(BLOCKS):
+        bm = float(np.mean(kt[:, q]))
+        gp = ni * N / (bm * 1e-3) / 1e9
+        per_block[str(ni)] = {"kernel_ms": bm, "gpairs_s": gp,
+                              "frac_fp32_nominal": gp * 1e9 * FLOPS_PER_PAIR / 1e12 /
+                              fp32_peak_tflops(gpu_info()[1], clk.get("sm_max_mhz") or 2070.0),
+                              "bound": "fp32" if ni >= 1024 else "latency (j set read once)"}
     pairs_big = 65536 * N
     achieved_tflops = pairs_big * FLOPS_PER_PAIR / (k_ms * 1e-3) / 1e12
     name, n_sm = gpu_info()
@@ -658,6 +669,7 @@ def main():
                  "kernel_ms_ni65536": float(np.mean(fp64_big)),
                  "speedup_split_over_fp64_kernel": float(np.mean(fp64_big)) / k_ms},
         "rel_err_vs_fp64_kernel": errs,
+        "pair_kernel_per_block": per_block,
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved_tflops / peak,
                      "frac_at_load_clock": achieved_tflops / fp32_peak_tflops(n_sm, load_mhz),
