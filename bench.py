@@ -132,6 +132,39 @@ def read_traffic():
 
 
 # --------------------------------------------------------------------------
+def cpu_side_checks(c, irr_check=None, pot_result=None):
+    """The CPU-baseline leg's work for the side legs: the irregular force of
+    the FP64 oracle (timed, and the GPU block checked against it) and the
+    potential of the FP32 port (timed) and of the FP64 oracle (check)."""
+    from oracle import oracle as O
+    out = {}
+    if irr_check is not None:
+        x, v, f, fdot, m, t0, lists, ti, act = irr_check["state"]
+        a, j, nid = irr_check["gpu"]
+        O.irr_fp64(x, v, f, fdot, m, t0, lists, ti, act)
+        t = time.perf_counter()
+        oa, oj, on = O.irr_fp64(x, v, f, fdot, m, t0, lists, ti, act)
+        dt = time.perf_counter() - t
+        ok = np.linalg.norm(oa, axis=1) > 0
+        ea = np.linalg.norm(a[ok] - oa[ok], axis=1) / np.linalg.norm(oa[ok], axis=1)
+        out["irregular"] = {"kind": "FP64 oracle (oracle/irr_fp64.c)", "cores": O.num_threads(),
+                            "ni": int(len(act)),
+                            "gpairs_s": int(lists[act, 0].sum()) / dt / 1e9,
+                            "gpu_max_rel_err_vs_fp64_oracle": float(ea.max()),
+                            "gpu_nnbid_identical": bool(np.array_equal(nid, on))}
+    if pot_result is not None:
+        n = c.n
+        t = time.perf_counter()
+        O.Port.pot(c.m, c.x)
+        dt = time.perf_counter() - t
+        ref = O.pot_fp64(c.m, c.x, 1, 2048)
+        out["potential"] = {"kind": "port (FP32 restatement of src/Main/pot.avx.cpp)",
+                            "cores": O.num_threads(), "gpairs_s": n * n / dt / 1e9,
+                            "gpu_max_rel_err_vs_fp64_oracle":
+                                float(np.max(np.abs(pot_result[:2048] - ref) / ref))}
+    return out
+
+
 def cpu_baseline(c, acts, budget_s: float = 10.0):
     """The portable FP32 restatement of the reference CPU path (OpenMP, all
     host cores) on whole steps of the same workload, as many as fit in
@@ -323,7 +356,7 @@ def king1m_leg(n_sm: int, peak_mhz: float):
             "lists_identical_to_fp64_kernel": bool(np.array_equal(lst, r.list))}
 
 
-def irregular_leg(c, h2, lists_src, cpu: bool):
+def irregular_leg(c, h2, lists_src):
     """Irregular (neighbour) force through the irr_simd_* ABI (the drop-in
     for src/Main/irr.avx.cpp): the bench's Plummer N = 65536 with the
     neighbour lists of its ni = 65536 regular block (the particle itself
@@ -374,30 +407,20 @@ def irregular_leg(c, h2, lists_src, cpu: bool):
                 ts.append(time.perf_counter() - t)
         out["predict_send_ms"] = 1e3 * min(tp[1:])
         out["send_host_arrays_ms"] = 1e3 * min(ts[1:])
-    if cpu:
-        from oracle import oracle as O
-        act = rng.permutation(n)[:16384]
-        O.irr_fp64(c.x, c.v, f, fdot, c.m, t0, lists, ti, act)
-        t = time.perf_counter()
-        oa, oj, on = O.irr_fp64(c.x, c.v, f, fdot, c.m, t0, lists, ti, act)
-        dt = time.perf_counter() - t
-        with IrrSimd(n, lmax) as irr:
-            irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
-            irr.set_lists(lists)
-            a, j, nid = irr.firr(ti, act)
-        ok = np.linalg.norm(oa, axis=1) > 0
-        ea = np.linalg.norm(a[ok] - oa[ok], axis=1) / np.linalg.norm(oa[ok], axis=1)
-        out["cpu_fp64_oracle"] = {"gpairs_s": int(lists[act, 0].sum()) / dt / 1e9,
-                                  "ni": 16384, "cores": O.num_threads()}
-        out["max_rel_err_vs_fp64_oracle"] = float(ea.max())
-        out["nnbid_identical"] = bool(np.array_equal(nid, on))
-    return out
+    # a block of 16384 for the CPU-baseline leg (timing and FP64 check)
+    act = rng.permutation(n)[:16384]
+    with IrrSimd(n, lmax) as irr:
+        irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
+        irr.set_lists(lists)
+        a, j, nid = irr.firr(ti, act)
+    check = {"state": (c.x, c.v, f, fdot, c.m, t0, lists, ti, act), "gpu": (a, j, nid)}
+    return out, check
 
 
-def potential_leg(c, cpu: bool):
+def potential_leg(c):
     """gpupot_ (the energy check's potential, gpupot.gpu.cu:61-127) over all
-    bodies of the bench cluster, host ABI, against the FP32 port on the host
-    cores and the FP64 oracle on a sample."""
+    bodies of the bench cluster, host ABI.  Returns the line entry and the
+    result (checked against the FP64 oracle in the CPU-baseline leg)."""
     from nbody6ppgpu_gb300.gpunb import gpupot
     n = c.n
     gpupot(c.m, c.x)
@@ -408,15 +431,7 @@ def potential_leg(c, cpu: bool):
         best = min(best, time.perf_counter() - t)
     out = {"workload": "Plummer N=65536 (the bench cluster), all bodies, host ABI",
            "ms": best * 1e3, "gpairs_s": n * n / best / 1e9}
-    if cpu:
-        from oracle import oracle as O
-        t = time.perf_counter()
-        O.Port.pot(c.m, c.x)
-        dt = time.perf_counter() - t
-        out["cpu_port_gpairs_s"] = n * n / dt / 1e9
-        ref = O.pot_fp64(c.m, c.x, 1, 2048)
-        out["max_rel_err_vs_fp64_oracle"] = float(np.max(np.abs(p[:2048] - ref) / ref))
-    return out
+    return out, p
 
 
 def rs_predictor_leg(dev):
@@ -636,12 +651,12 @@ def main():
         batched = batched_leg(lib, dev, stream, steps=args.steps, warmup=args.warmup)
 
     nb.close()
-    irr = None
+    irr = irr_check = None
     if not args.no_irregular:
         lists_by_particle = np.zeros_like(outs[65536].list)
         lists_by_particle[acts[65536]] = outs[65536].list
-        irr = irregular_leg(c, h2, lists_by_particle, cpu=(rank == 0 and not args.no_cpu_baseline))
-    pot = potential_leg(c, cpu=(rank == 0 and not args.no_cpu_baseline))
+        irr, irr_check = irregular_leg(c, h2, lists_by_particle)
+    pot, pot_result = potential_leg(c)
     king = None
     if not args.no_large:
         king = king1m_leg(n_sm, peak_mhz)
@@ -650,6 +665,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu, _ = cpu_baseline(c, acts)
+        cpu.update(cpu_side_checks(c, irr_check, pot_result))
 
     # the library's own kernels per step: per send bbox_init, bbox, morton, pack;
     # per regf prep, pair kernel, merge, two scans, gather, offsets, plus the
