@@ -386,9 +386,6 @@ static long long tune_key(int nj, int ni, int mflag, int prec) {
   return ((long long)bucket(nj) << 24) | ((long long)bucket(ni) << 8) | (mflag << 1) | prec;
 }
 
-// j-splits for a persistent launch: about 32 work items per resident block,
-// so that the last round of items leaves little of the machine idle, with
-// at least 2 tiles per item.
 // j-splits: about 64 work items per resident block (the dynamic queue then
 // balances the blocks to within one short item), at least one tile per item.
 static int plan_splits(int variant, int ni, int ntile, bool mflag) {
