@@ -586,13 +586,13 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   double *din = g.iraw.as<double>();
   CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
   if (g.host_direct) {
-    CUDA_OR(cudaMemcpyAsync(din, h2, (size_t)ni * sizeof(double), cudaMemcpyHostToDevice, st), );
-    CUDA_OR(cudaMemcpyAsync(din + ni, dtr, (size_t)ni * sizeof(double), cudaMemcpyHostToDevice,
-                            st), );
-    CUDA_OR(cudaMemcpyAsync(din + 2 * (size_t)ni, xi, (size_t)ni * 3 * sizeof(double),
-                            cudaMemcpyHostToDevice, st), );
-    CUDA_OR(cudaMemcpyAsync(din + 5 * (size_t)ni, vi, (size_t)ni * 3 * sizeof(double),
-                            cudaMemcpyHostToDevice, st), );
+    HostCopyJobs jobs;
+    jobs.count = 4;
+    jobs.j[0] = HostCopyJob{h2, din, ni, 8};
+    jobs.j[1] = HostCopyJob{dtr, din + ni, ni, 8};
+    jobs.j[2] = HostCopyJob{xi, din + 2 * (size_t)ni, 3ll * ni, 8};
+    jobs.j[3] = HostCopyJob{vi, din + 5 * (size_t)ni, 3ll * ni, 8};
+    CUDA_OR(launch_host_copy(jobs, st), );
   } else {
     if (!g.hin.ensure(in_doubles * sizeof(double))) return;
     double *hin = g.hin.as<double>();
@@ -644,14 +644,15 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   if (g.host_direct) {
     // results straight into the caller's arrays; the device writes the rows
     CUDA_OR(launch_list_rows(o.dense, o.off, o.btot, o.nnb, ni, lmax, list, st), );
-    CUDA_OR(cudaMemcpyAsync(acc, o.acc, (size_t)ni * 3 * sizeof(double), cudaMemcpyDeviceToHost,
-                            st), );
-    CUDA_OR(cudaMemcpyAsync(jrk, o.jrk, (size_t)ni * 3 * sizeof(double), cudaMemcpyDeviceToHost,
-                            st), );
-    CUDA_OR(cudaMemcpyAsync(pot, o.pot, (size_t)ni * sizeof(double), cudaMemcpyDeviceToHost, st), );
     if (!g.hout.ensure(sizeof(int))) return;
     int *h_err = g.hout.as<int>();
-    CUDA_OR(cudaMemcpyAsync(h_err, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
+    HostCopyJobs jobs;
+    jobs.count = 4;
+    jobs.j[0] = HostCopyJob{o.acc, acc, 3ll * ni, 8};
+    jobs.j[1] = HostCopyJob{o.jrk, jrk, 3ll * ni, 8};
+    jobs.j[2] = HostCopyJob{o.pot, pot, ni, 8};
+    jobs.j[3] = HostCopyJob{g.err.p, h_err, 1, 4};
+    CUDA_OR(launch_host_copy(jobs, st), );
     CUDA_OR(cudaStreamSynchronize(st), );
     const double t_grav = wtime();
     g.time_grav += t_grav - t_begin;
@@ -810,11 +811,12 @@ void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
   CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
   if (n > 0 && g.host_direct) {
     double *d = g.jraw.as<double>();
-    CUDA_OR(cudaMemcpyAsync(d, mj, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st), );
-    CUDA_OR(cudaMemcpyAsync(d + n, xj, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice,
-                            st), );
-    CUDA_OR(cudaMemcpyAsync(d + 4 * (size_t)n, vj, (size_t)n * 3 * sizeof(double),
-                            cudaMemcpyHostToDevice, st), );
+    HostCopyJobs jobs;
+    jobs.count = 3;
+    jobs.j[0] = HostCopyJob{mj, d, n, 8};
+    jobs.j[1] = HostCopyJob{xj, d + n, 3ll * n, 8};
+    jobs.j[2] = HostCopyJob{vj, d + 4 * (size_t)n, 3ll * n, 8};
+    CUDA_OR(launch_host_copy(jobs, st), );
   } else if (n > 0) {
     double *h = g.hj.as<double>();
     hcopy(h, mj, (size_t)n * sizeof(double));
@@ -824,10 +826,18 @@ void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
                             st), );
   }
   if (send_common(n, st) != GPUNB_OK) return;
-  int herr = 0;
-  CUDA_OR(cudaMemcpyAsync(&herr, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
+  if (!g.hout.ensure(sizeof(int))) return;
+  int *herr = g.hout.as<int>();
+  if (g.host_direct) {
+    HostCopyJobs jobs;
+    jobs.count = 1;
+    jobs.j[0] = HostCopyJob{g.err.p, herr, 1, 4};
+    CUDA_OR(launch_host_copy(jobs, st), );
+  } else {
+    CUDA_OR(cudaMemcpyAsync(herr, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
+  }
   CUDA_OR(cudaStreamSynchronize(st), );
-  check_device_error(herr);
+  check_device_error(*herr);
   g.time_send += wtime() - t0;
 }
 

@@ -51,6 +51,20 @@ cudaError_t launch_list_gather(int *rows, int cap, const int *rowlen, const int 
 // rows may be host memory the device reaches coherently
 cudaError_t launch_list_rows(const int *dense, const int *off, const int *boff, const int *nnb,
                              int ni, int lmax, int *rows, cudaStream_t st);
+// up to HOSTCOPY_MAX element copies in one launch, one side of each in host
+// memory the device reaches coherently
+constexpr int HOSTCOPY_MAX = 4;
+struct HostCopyJob {
+  const void *src;
+  void *dst;
+  long long n;   // elements
+  int esize;     // 8 or 4 bytes
+};
+struct HostCopyJobs {
+  HostCopyJob j[HOSTCOPY_MAX];
+  int count;
+};
+cudaError_t launch_host_copy(const HostCopyJobs &jobs, cudaStream_t st);
 cudaError_t launch_list_finalize_offsets(int *off, const int *btot, int ni, cudaStream_t st);
 
 // spatial (Morton) ordering

@@ -15,6 +15,7 @@
 #include "regf_kernels.cuh"
 #include "launch.h"
 
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -1195,6 +1196,36 @@ cudaError_t launch_list_rows(const int *dense, const int *off, const int *boff, 
   const int threads = 256;
   const long long blocks = ((long long)ni * 32 + threads - 1) / threads;
   list_rows_kernel<<<(unsigned)blocks, threads, 0, st>>>(dense, off, boff, nnb, ni, lmax, rows);
+  return cudaGetLastError();
+}
+
+// Copies between the caller's host arrays and device buffers done by the
+// device itself over the coherent host path (one launch for up to
+// HOSTCOPY_MAX arrays instead of one pageable cudaMemcpy each, whose fixed
+// cost is ~11 us); 8-byte or 4-byte elements, coalesced across the warp.
+__global__ void host_copy_kernel(HostCopyJobs jobs) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int q = 0; q < jobs.count; ++q) {
+    const HostCopyJob J = jobs.j[q];
+    if (J.esize == 8) {
+      const double *src = (const double *)J.src;
+      double *dst = (double *)J.dst;
+      for (long long e = t0; e < J.n; e += stride) dst[e] = src[e];
+    } else {
+      const int *src = (const int *)J.src;
+      int *dst = (int *)J.dst;
+      for (long long e = t0; e < J.n; e += stride) dst[e] = src[e];
+    }
+  }
+}
+
+cudaError_t launch_host_copy(const HostCopyJobs &jobs, cudaStream_t st) {
+  long long tot = 0;
+  for (int q = 0; q < jobs.count; ++q) tot += jobs.j[q].n;
+  if (tot <= 0) return cudaSuccess;
+  const long long blocks = std::min<long long>((tot + 255) / 256, 2048);
+  host_copy_kernel<<<(unsigned)blocks, 256, 0, st>>>(jobs);
   return cudaGetLastError();
 }
 
