@@ -93,6 +93,17 @@ struct DevBuf {
     bytes = want;
     return true;
   }
+  // as ensure, and a newly created buffer is zero-filled
+  bool ensure_zero(size_t n) {
+    if (n <= bytes) return true;
+    if (!ensure(n)) return false;
+    if (cudaMemset(p, 0, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      fail(GPUNB_E_CUDA, "cudaMemset of %zu bytes failed", bytes);
+      return false;
+    }
+    return true;
+  }
   void release() {
     if (p) {
       cudaFree(p);
@@ -268,7 +279,7 @@ static bool devinit(int irank) {
   CUDA_OR(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking), false);
   CUDA_OR(cudaEventCreate(&g.ek0), false);
   CUDA_OR(cudaEventCreate(&g.ek1), false);
-  if (!g.err.ensure(sizeof(int)) || !g.bbox.ensure(8 * sizeof(int)) ||
+  if (!g.err.ensure(sizeof(int)) || !g.bbox.ensure_zero(BBOX_INTS * sizeof(int)) ||
       !g.queue.ensure(sizeof(int)))
     return false;
   char host[150] = {0};
@@ -386,13 +397,16 @@ static long long tune_key(int nj, int ni, int mflag, int prec) {
   return ((long long)bucket(nj) << 24) | ((long long)bucket(ni) << 8) | (mflag << 1) | prec;
 }
 
-// j-splits: about 64 work items per resident block (the dynamic queue then
+// j-splits: about 32 work items per resident block (the dynamic queue then
 // balances the blocks to within one short item), at least one tile per item.
+// Measured on GB300 (Plummer N = 65536, blocks of 16384 and 65536): 32 items
+// per block beat 64 by 1-1.3% (half the partial sums to write and merge) and
+// 16 by about as much (coarser balance).
 static int plan_splits(int variant, int ni, int ntile, bool mflag) {
   const VariantDesc d = regf_variant(variant);
   const int gx = (ni + d.itile() - 1) / d.itile();
   const int bps = regf_ds_blocks_per_sm(variant, mflag);
-  const long long want = 64ll * g.n_sm * bps;
+  const long long want = 32ll * g.n_sm * bps;
   long long s = (want + gx - 1) / gx;
   const int smax = std::max(1, ntile);
   if (s > smax) s = smax;

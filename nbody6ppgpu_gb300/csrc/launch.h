@@ -69,6 +69,13 @@ cudaError_t launch_list_finalize_offsets(int *off, const int *btot, int ni, cuda
 
 // spatial (Morton) ordering
 size_t order_temp_bytes(int n);
+// bounding-box buffer: [0..6) the box, [BBOX_TICKET] the last-block ticket
+// (zero between launches), [BBOX_PART..) the per-block partial boxes
+constexpr int BBOX_THREADS = 256;
+constexpr int BBOX_MAX_BLOCKS = 256;
+constexpr int BBOX_TICKET = 7;
+constexpr int BBOX_PART = 8;
+constexpr int BBOX_INTS = BBOX_PART + 6 * BBOX_MAX_BLOCKS;
 cudaError_t launch_bbox(const double *x, int n, int *bb, cudaStream_t st);
 cudaError_t launch_order(const double *x, int n, const int *bb, unsigned long long *keys,
                          unsigned long long *keys_alt, int *vals_alt, int *perm, void *temp,

@@ -23,13 +23,15 @@ __device__ __forceinline__ int f2ord(float f) {
 }
 __device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
-__global__ void bbox_init_kernel(int *bb) {
-  if (threadIdx.x < 3) bb[threadIdx.x] = f2ord(INFINITY);
-  else if (threadIdx.x < 6) bb[threadIdx.x] = f2ord(-INFINITY);
-}
-
-// bb[0..2] = min, bb[3..5] = max of the FP32-rounded coordinates
-__global__ void bbox_kernel(const double *__restrict__ x, int n, int *bb) {
+// bb[0..2] = min, bb[3..5] = max of the FP32-rounded coordinates (as
+// order-preserving ints).  Each block reduces its share and writes one
+// partial box; the last block to finish (ticket bb[BBOX_TICKET]) reduces the
+// partials and resets the ticket, so one launch does the whole reduction and
+// needs no initialisation.  The ticket is zeroed when the buffer is created.
+__global__ void __launch_bounds__(BBOX_THREADS) bbox_kernel(const double *__restrict__ x, int n,
+                                                            int *bb) {
+  __shared__ float s[BBOX_THREADS / 32][6];
+  __shared__ bool last;
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 #pragma unroll
@@ -46,13 +48,36 @@ __global__ void bbox_kernel(const double *__restrict__ x, int n, int *bb) {
       hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
     }
   }
-  if ((threadIdx.x & 31) == 0) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      atomicMin(bb + c, f2ord(lo[c]));
-      atomicMax(bb + 3 + c, f2ord(hi[c]));
+      s[warp][c] = lo[c];
+      s[warp][3 + c] = hi[c];
     }
   }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int q = threadIdx.x;
+    float r = s[0][q];
+    for (int w = 1; w < BBOX_THREADS / 32; ++w) r = q < 3 ? fminf(r, s[w][q]) : fmaxf(r, s[w][q]);
+    bb[BBOX_PART + 6 * blockIdx.x + q] = f2ord(r);
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(bb + BBOX_TICKET, 1) == (int)gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  if (threadIdx.x < 6) {
+    const int q = threadIdx.x;
+    int r = __ldcg(bb + BBOX_PART + q);
+    for (int b = 1; b < (int)gridDim.x; ++b) {
+      const int u = __ldcg(bb + BBOX_PART + 6 * b + q);
+      r = q < 3 ? min(r, u) : max(r, u);
+    }
+    bb[q] = r;
+  }
+  if (threadIdx.x == 0) bb[BBOX_TICKET] = 0;
 }
 
 // spread the low 16 bits of v to every third bit
@@ -174,11 +199,12 @@ size_t order_temp_bytes(int n) {
 }
 
 cudaError_t launch_bbox(const double *x, int n, int *bb, cudaStream_t st) {
-  bbox_init_kernel<<<1, 32, 0, st>>>(bb);
-  if (n > 0) {
-    const int blocks = std::min(1024, (n + 255) / 256);
-    bbox_kernel<<<blocks, 256, 0, st>>>(x, n, bb);
-  }
+  // two bodies per thread at least; an empty set still runs one block (box
+  // of +inf / -inf, as for the FP32 coordinates of no body)
+  const int per_block = 2 * BBOX_THREADS;
+  const int blocks = std::max(1, std::min(BBOX_MAX_BLOCKS, (std::max(n, 0) + per_block - 1) /
+                                                              per_block));
+  bbox_kernel<<<blocks, BBOX_THREADS, 0, st>>>(x, std::max(n, 0), bb);
   return cudaGetLastError();
 }
 

@@ -40,12 +40,12 @@ namespace gpunb {
 // Tile slot p holds body perm[p] (identity when perm is null; perm[p] = -1
 // marks a padding slot).
 
-// block-wide maxima of NV doubles (JT threads), results in every thread
+// block-wide maxima of NV floats (JT threads), results in every thread
 template <int NV>
-__device__ __forceinline__ void block_max(double (&a)[NV], double (*s)[NV]) {
+__device__ __forceinline__ void block_maxf(float (&a)[NV], float (*s)[NV]) {
 #pragma unroll
   for (int q = 0; q < NV; ++q)
-    for (int o = 16; o > 0; o >>= 1) a[q] = fmax(a[q], __shfl_xor_sync(0xffffffffu, a[q], o));
+    for (int o = 16; o > 0; o >>= 1) a[q] = fmaxf(a[q], __shfl_xor_sync(0xffffffffu, a[q], o));
   if ((threadIdx.x & 31) == 0) {
 #pragma unroll
     for (int q = 0; q < NV; ++q) s[threadIdx.x >> 5][q] = a[q];
@@ -53,13 +53,20 @@ __device__ __forceinline__ void block_max(double (&a)[NV], double (*s)[NV]) {
   __syncthreads();
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
-    double r = s[0][q];
-    for (int w = 1; w < JT / 32; ++w) r = fmax(r, s[w][q]);
+    float r = s[0][q];
+    for (int w = 1; w < JT / 32; ++w) r = fmaxf(r, s[w][q]);
     a[q] = r;
   }
   __syncthreads();
 }
 
+// The tile centre O is an FP32 number (the midpoint of the tile's box of
+// FP32-rounded coordinates), so its double-single form is (O, 0) and only the
+// double-single split and the tile-relative difference x - O need FP64
+// arithmetic (on GB300 about 1/64 of the FP32 rate).  The tile maxima are
+// formed in FP32 from the rounded values and widened by 2^-18 with upward
+// rounding: the FP32 evaluation of |v|, |x - O| and sqrt(m) is within 2^-21
+// of the exact value, so the stored maxima stay upper bounds.
 __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restrict__ m,
                                                          const double *__restrict__ x,
                                                          const double *__restrict__ v, int nj,
@@ -67,52 +74,53 @@ __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restric
                                                          float *__restrict__ tiles, int *err) {
   const int t = blockIdx.x, l = threadIdx.x, p = t * JT + l;
   float *T = tiles + (size_t)t * TILE_FLOATS;
-  __shared__ double s_red6[JT / 32][6];
-  __shared__ double s_red4[JT / 32][4];
+  __shared__ float s_red6[JT / 32][6];
+  __shared__ float s_red4[JT / 32][4];
   const int j = perm ? perm[p] : (p < nj ? p : -1);   // -1: padding slot
-  double xj[3] = {0.0, 0.0, 0.0}, vj[3] = {0.0, 0.0, 0.0}, mj = 0.0;
+  double xj[3] = {0.0, 0.0, 0.0};
+  float xf[3] = {0.f, 0.f, 0.f}, vf[3] = {0.f, 0.f, 0.f}, mf = 0.f;
   if (j >= 0) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       xj[c] = x[3 * j + c];
-      vj[c] = v[3 * j + c];
+      xf[c] = (float)xj[c];
+      vf[c] = (float)v[3 * j + c];
     }
-    mj = m[j];
-    if (isnan(xj[0]) || isnan(xj[1]) || isnan(xj[2]) || isnan(vj[0]) || isnan(vj[1]) ||
-        isnan(vj[2]) || isnan(mj))
+    mf = (float)m[j];
+    if (isnan(xf[0]) || isnan(xf[1]) || isnan(xf[2]) || isnan(vf[0]) || isnan(vf[1]) ||
+        isnan(vf[2]) || isnan(mf))
       raise_error(err, GPUNB_E_NAN);
   }
-  // tile centre: midpoint of the real bodies' bounding box
-  double bb[6];
+  // tile centre: midpoint of the real bodies' box (FP32)
+  float bb[6];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    bb[c] = j >= 0 ? xj[c] : -INFINITY;        // max
-    bb[3 + c] = j >= 0 ? -xj[c] : -INFINITY;   // -min
+    bb[c] = j >= 0 ? xf[c] : -INFINITY;        // max
+    bb[3 + c] = j >= 0 ? -xf[c] : -INFINITY;   // -min
   }
-  block_max<6>(bb, s_red6);
-  double o[3];
+  block_maxf<6>(bb, s_red6);
+  float o[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const double hi = bb[c], lo = -bb[3 + c];
-    o[c] = (hi >= lo) ? 0.5 * lo + 0.5 * hi : 0.0;   // no real body: O = 0
-    if (isnan(o[c])) o[c] = 0.0;
+    const float hi = bb[c], lo = -bb[3 + c];
+    o[c] = (hi >= lo) ? 0.5f * lo + 0.5f * hi : 0.f;   // no real body: O = 0
+    if (!isfinite(o[c])) o[c] = 0.f;
   }
-  double r2 = 0.0;
+  float r2 = 0.f, v2 = 0.f;
   if (j >= 0) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const double d = xj[c] - o[c];
-      r2 += d * d;
-      T[(F_XR + c) * JT + l] = (float)d;
-      float h, lo;
-      ds_split(xj[c], h, lo);
-      T[(F_XH + c) * JT + l] = h;
-      T[(F_XL + c) * JT + l] = lo;
+      const float d = (float)(xj[c] - (double)o[c]);
+      r2 = fmaf(d, d, r2);
+      v2 = fmaf(vf[c], vf[c], v2);
+      T[(F_XR + c) * JT + l] = d;
+      T[(F_XH + c) * JT + l] = xf[c];
+      T[(F_XL + c) * JT + l] = (float)(xj[c] - (double)xf[c]);
     }
-    T[F_VX * JT + l] = (float)vj[0];
-    T[F_VY * JT + l] = (float)vj[1];
-    T[F_VZ * JT + l] = (float)vj[2];
-    T[F_MN * JT + l] = (float)(-0.5 * mj);
+    T[F_VX * JT + l] = vf[0];
+    T[F_VY * JT + l] = vf[1];
+    T[F_VZ * JT + l] = vf[2];
+    T[F_MN * JT + l] = -0.5f * mf;
   } else {
     // padding body: massless and far away, never a neighbour candidate
     T[F_XR * JT + l] = 1.0e15f;
@@ -124,23 +132,20 @@ __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restric
     T[F_VX * JT + l] = 0.f; T[F_VY * JT + l] = 0.f; T[F_VZ * JT + l] = 0.f;
     T[F_MN * JT + l] = -0.f;
   }
-  // tile maxima of |v|, m and |x - O|, rounded up when narrowed; body count
-  double mx[4] = {j >= 0 ? sqrt(vj[0] * vj[0] + vj[1] * vj[1] + vj[2] * vj[2]) : 0.0, mj,
-                  sqrt(r2), j >= 0 ? (double)(l + 1) : 0.0};   // real slots fill from 0
-  block_max<4>(mx, s_red4);
-  const double vm = mx[0], mm = mx[1], rad = mx[2], nr = mx[3];
+  // tile maxima of |v|, m and |x - O|; body count (real slots fill from 0)
+  float mx[4] = {sqrtf(v2), mf, sqrtf(r2), j >= 0 ? (float)(l + 1) : 0.f};
+  block_maxf<4>(mx, s_red4);
   if (l == 0) {
+    constexpr float grow = 1.0f + 0x1p-18f;
     float *M = T + NFIELD * JT;
-    M[M_VMAX] = (float)(vm * (1.0 + 0x1p-20));
-    M[M_SMAX] = (float)(sqrt(fmax(mm, 0.0)) * (1.0 + 0x1p-20));
-    M[M_COUNT] = (float)nr;
-    M[M_RAD] = (float)(rad * (1.0 + 0x1p-20));
+    M[M_VMAX] = __fmul_ru(mx[0], grow);
+    M[M_SMAX] = __fmul_ru(sqrtf(fmaxf(mx[1], 0.f)), grow);
+    M[M_COUNT] = mx[3];
+    M[M_RAD] = __fmul_ru(mx[2], grow);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      float h, lo;
-      ds_split(o[c], h, lo);
-      M[M_OH + c] = h;
-      M[M_OL + c] = lo;
+      M[M_OH + c] = o[c];
+      M[M_OL + c] = 0.f;
     }
     M[M_OH + 3] = 0.f;
     M[M_OL + 3] = 0.f;
