@@ -19,6 +19,16 @@ __device__ __forceinline__ f2 add2(f2 a, f2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
 
+// Hardware reciprocal square root estimate (about 2^-22 relative error; the
+// pair loops refine it with one Newton step).  The .ftz form is the bare
+// estimate instruction: inputs below 2^-126 (distances below 1e-19) read as
+// zero and give +inf, exactly like coincident bodies.
+__device__ __forceinline__ float rsqrt_est(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // ---------------------------------------------------------------------------
 // Double-single: x = hi + lo with hi = fl32(x), lo = fl32(x - hi).
 // Round-to-nearest split (valid for any |x| in float range), unlike the

@@ -102,10 +102,10 @@ __global__ void __launch_bounds__(32 * WI) pot_ds_kernel(const float *__restrict
         const f2 dy = add2(add2(yh, nyh[k]), add2(yl, nyl[k]));
         const f2 dz = add2(add2(zh, nzh[k]), add2(zl, nzl[k]));
         const f2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-        const f2 y0 = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        const f2 y0 = make_float2(rsqrt_est(r2.x), rsqrt_est(r2.y));
         f2 z = mul2(y0, fma2(mul2(r2, y0), y0, mk2(-3.0f)));   // -2/r
-        z.x = r2.x > 0.f ? z.x : 0.f;                         // skip coincident bodies
-        z.y = r2.y > 0.f ? z.y : 0.f;
+        z.x = r2.x >= 0x1p-126f ? z.x : 0.f;   // skip coincident bodies (r < 1e-19)
+        z.y = r2.y >= 0x1p-126f ? z.y : 0.f;
         q[k] = fma2(mn, z, q[k]);                              // += m/r
       }
     }

@@ -317,7 +317,7 @@ __device__ __forceinline__ void pair_geo(const IState &I, const TileCtx &C, cons
   g.r2 = fma2(g.dz, g.dz, fma2(g.dy, g.dy, mul2(g.dx, g.dx)));
   g.rv = fma2(g.dz, g.dvz, fma2(g.dy, g.dvy, mul2(g.dx, g.dvx)));
   // rsqrt estimate + one Newton step, scaled: z = y0 (x y0^2 - 3) = -2/r
-  const f2 y0 = make_float2(rsqrtf(g.r2.x), rsqrtf(g.r2.y));
+  const f2 y0 = make_float2(rsqrt_est(g.r2.x), rsqrt_est(g.r2.y));
   g.z = mul2(y0, fma2(mul2(g.r2, y0), y0, mk2(-3.0f)));
 }
 
