@@ -536,14 +536,18 @@ def main():
                                        ni * NNBMAX, NNBMAX, 0, sp)
             assert rc == 0, rc
 
-    def timed_steps(k, precision):
+    def timed_steps(k, precision, graphs=False, timing=True):
+        """k steps, each bracketed by CUDA events on the library's stream.
+        graphs: replay each call shape as a CUDA graph (gpunb_set_graphs);
+        timing: per-pair-kernel events as well (calls then run without graphs)."""
         nb.set_precision(precision)
+        lib.gpunb_set_graphs(1 if graphs else 0)
         for _ in range(args.warmup):
             dev_step()
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-        lib.gpunb_set_timing(1)
+        lib.gpunb_set_timing(1 if timing else 0)
         evs = []
         for _ in range(k):
             with torch.cuda.stream(stream):    # L2 flush between steps, on the timed
@@ -555,8 +559,9 @@ def main():
             e1.record(stream)
             evs.append((e0, e1))
         torch.cuda.synchronize()
-        kt = nb.kernel_times(max_n=64 * k + 64)
+        kt = nb.kernel_times(max_n=64 * k + 64) if timing else []
         lib.gpunb_set_timing(0)
+        lib.gpunb_set_graphs(0)
         if dist:
             dist.barrier()
         ms = [a.elapsed_time(b) for a, b in evs]
@@ -566,10 +571,13 @@ def main():
     clocks = Clocks(local)
     clocks.start()
     t_wall = time.perf_counter()
-    ms, kt = timed_steps(args.steps, "split")
+    ms, _ = timed_steps(args.steps, "split", graphs=True, timing=False)
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     step_ms = float(sum(ms) / len(ms))
+    # the same steps without graphs, with per-pair-kernel events (roofline)
+    kt_steps = max(4, min(args.steps, 16))
+    ms_nograph, kt = timed_steps(kt_steps, "split", graphs=False, timing=True)
     if dist:
         t = torch.tensor([step_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -577,7 +585,7 @@ def main():
     pairs_per_step = N * sum(BLOCKS)
     value = ws * pairs_per_step / (step_ms * 1e-3) / 1e9
     # pair-kernel launches of the dominant block (ni = N), in launch order
-    kt = np.asarray(kt).reshape(args.steps, len(BLOCKS))
+    kt = np.asarray(kt).reshape(kt_steps, len(BLOCKS))
     big = kt[:, BLOCKS.index(65536)]
     k_ms = float(np.mean(big))
     # every block's pair kernel: duration, pairs/s and the bound that applies
@@ -674,7 +682,7 @@ def main():
         cpu, _ = cpu_baseline(c, acts)
         cpu.update(cpu_side_checks(c, irr_check, pot_result))
 
-    # the library's own kernels per step: per send bbox_init, bbox, morton, pack;
+    # the library's own kernels per step: per send copy, bbox, morton, pack;
     # per regf prep, pair kernel, merge, two scans, gather, offsets, plus the
     # Morton key kernel of the i-ordering when ni >= 256.  The Morton sorts are
     # CUB radix sorts (43 launches per step in the ncu launch list).
@@ -682,11 +690,13 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "ms_per_step_without_graphs": float(np.mean(ms_nograph)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Plummer sphere, Kroupa IMF, Henon units)",
         "config": {"workload": WORKLOAD, "N": N, "blocks": BLOCKS, "nb_target": NB_TARGET,
                    "nnbmax": NNBMAX, "precision": "split FP32 (double-single positions)",
                    "l2": "flushed (256 MB write) between timed steps",
+                   "launch": "device entry points replayed as CUDA graphs, one per call shape",
                    "parallelism": f"replicas x{ws}"},
         "fp64": {"value": fp64_value, "unit": "Gpairs/s",
                  "kernel_ms_ni65536": float(np.mean(fp64_big)),

@@ -127,6 +127,13 @@ void gpunb_last_launch(int *variant, int *splits, int *grid_x);
  * (count or -count), list_off[ni+1] (offsets of accepted rows in list) and
  * list[...] (capacity list_cap ints; ni*nnbmax always suffices). */
 int gpunb_send_device(int nj, const double *m, const double *x, const double *v, void *stream);
+/* Device-side errors of the device entry points (a NaN input, an exhausted
+ * wait) are raised by the kernels into the library's error word, which
+ * these calls do not read back.  gpunb_device_status synchronises `stream`
+ * (NULL: the library's stream), returns that word (0 or a GPUNB_E_* code),
+ * records a nonzero code as the calls on host arrays do, and clears the
+ * word.  The host-array calls clear it when they start. */
+int gpunb_device_status(void *stream);
 int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double *xi,
                       const double *vi, double *acc, double *jrk, double *pot, int *nnb,
                       int *list_off, int *list, size_t list_cap, int nnbmax, int m_flag,
@@ -149,9 +156,12 @@ int gpunb_batch_regf_device(int ncl, const int *ni, const double *h2, const doub
 /* Launch plan of the last batched call: kernel variant and work items. */
 int gpunb_batch_last_plan(int *variant, int *items);
 
-/* CUDA graphs for the batched entry points: with flag = 1, the first call of a
- * shape (set sizes, active counts, buffers) runs normally and is then
- * captured; later calls of that shape replay the graph.  Default 0. */
+/* CUDA graphs for the device entry points (gpunb_send_device,
+ * gpunb_regf_device and the batched pair): with flag = 1, the first call of a
+ * shape (sizes, active counts, caller pointers, stream, launch plan) runs
+ * normally and is then captured; later calls of that shape replay the graph
+ * while no library buffer has moved.  Calls made with per-launch timing on
+ * (gpunb_set_timing) run without graphs.  Default 0. */
 void gpunb_set_graphs(int flag);
 
 /* Potential of gpupot_ for callers that cannot allocate device memory (no

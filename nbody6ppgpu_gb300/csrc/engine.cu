@@ -157,6 +157,24 @@ static int run_graphed(GraphEntry &e, bool enabled, cudaStream_t st, F issue) {
   return rc;
 }
 
+// CUDA-graph replay (gpunb_set_graphs): the batched entry points keep one
+// graph per plan; the single-set device entry points keep one per call key
+// (sizes, caller pointers, stream and launch plan), at most kMaxDevGraphs.
+static bool g_use_graphs = false;
+static std::map<std::vector<long long>, GraphEntry> g_dev_graphs;
+constexpr size_t kMaxDevGraphs = 64;
+
+static void dev_graphs_drop() {
+  for (auto &kv : g_dev_graphs) graph_drop(kv.second);
+  g_dev_graphs.clear();
+}
+
+static GraphEntry &dev_graph(const std::vector<long long> &key) {
+  if (g_dev_graphs.size() >= kMaxDevGraphs && g_dev_graphs.find(key) == g_dev_graphs.end())
+    dev_graphs_drop();
+  return g_dev_graphs[key];
+}
+
 struct PinBuf {
   void *p = nullptr;
   size_t bytes = 0;
@@ -800,6 +818,7 @@ void gpunb_close_(void) {
   }
   if (g.stream) cudaStreamSynchronize(g.stream);
   batch_release();
+  dev_graphs_drop();
   g.jraw.release(); g.jtiles.release(); g.hj.release();
   g.iraw.release(); g.part.release(); g.cnt.release(); g.rows.release();
   g.rowlen.release(); g.off.release(); g.btot.release(); g.dense.release();
@@ -1063,13 +1082,37 @@ int gpunb_send_device(int nj, const double *m, const double *x, const double *v,
     return GPUNB_E_CAPACITY;
   }
   cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
-  double *d = g.jraw.as<double>();
-  if (nj > 0) {
-    CUDA_OR(cudaMemcpyAsync(d, m, (size_t)nj * sizeof(double), cudaMemcpyDeviceToDevice, st), GPUNB_E_CUDA);
-    CUDA_OR(cudaMemcpyAsync(d + nj, x, (size_t)nj * 3 * sizeof(double), cudaMemcpyDeviceToDevice, st), GPUNB_E_CUDA);
-    CUDA_OR(cudaMemcpyAsync(d + 4 * (size_t)nj, v, (size_t)nj * 3 * sizeof(double), cudaMemcpyDeviceToDevice, st), GPUNB_E_CUDA);
-  }
-  return send_common(nj, st);
+  auto issue = [&](cudaStream_t s) -> int {
+    double *d = g.jraw.as<double>();
+    HostCopyJobs jobs;   // one copy kernel for the three arrays
+    jobs.count = 3;
+    jobs.j[0] = HostCopyJob{m, d, nj, 8};
+    jobs.j[1] = HostCopyJob{x, d + nj, 3ll * nj, 8};
+    jobs.j[2] = HostCopyJob{v, d + 4 * (size_t)nj, 3ll * nj, 8};
+    CUDA_OR(launch_host_copy(jobs, s), GPUNB_E_CUDA);
+    return send_common(nj, s);
+  };
+  int rc;
+  if (g_use_graphs && !g.timing)
+    rc = run_graphed(dev_graph({0, nj, (long long)(uintptr_t)m, (long long)(uintptr_t)x,
+                                (long long)(uintptr_t)v, (long long)(uintptr_t)st}),
+                     true, st, issue);
+  else
+    rc = issue(st);
+  if (rc == GPUNB_OK) g.nj = nj;
+  return rc;
+}
+
+int gpunb_device_status(void *stream) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!g.devinit || !g.err.p) return GPUNB_E_NO_DEVICE;
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  int herr = 0;
+  CUDA_OR(cudaStreamSynchronize(st), GPUNB_E_CUDA);
+  CUDA_OR(cudaMemcpy(&herr, g.err.p, sizeof(int), cudaMemcpyDeviceToHost), GPUNB_E_CUDA);
+  CUDA_OR(cudaMemset(g.err.p, 0, sizeof(int)), GPUNB_E_CUDA);
+  check_device_error(herr);
+  return herr;
 }
 
 int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double *xi,
@@ -1087,33 +1130,45 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
     return GPUNB_E_ARG;
   }
   cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
-  ISet is;
-  is.h2 = h2; is.dtr = dtr; is.x = xi; is.v = vi; is.ni = ni;
-  is.perm = nullptr;
-  is.rec = nullptr;
-  if (g.precision == 0 && order_iset(is, st) != GPUNB_OK) return GPUNB_E_ALLOC;
   const bool mflag = m_flag != 0;
   int variant, S;
   choose_plan(ni, mflag, variant, S);
   g.num_inter += (long long)ni * g.nj;
   g.ini += ni;
   g.icall++;
-  int rc = run_pair_pass(is, nnbmax, mflag, variant, S, st, false);
-  if (rc != GPUNB_OK) return rc;
-  const int nb = list_scan_blocks(ni);
-  if (!g.rowlen.ensure((size_t)ni * sizeof(int)) || !g.btot.ensure((size_t)(nb + 1) * sizeof(int)))
-    return GPUNB_E_ALLOC;
-  RegfDev o;
-  o.acc = acc; o.jrk = jrk; o.pot = pot; o.nnb = nnb;
-  o.rowlen = g.rowlen.as<int>(); o.off = list_off; o.btot = g.btot.as<int>(); o.dense = list;
-  const int ni_pad = g.precision == 1
-                         ? ((ni + FP64_THREADS - 1) / FP64_THREADS) * FP64_THREADS
-                         : ((ni + regf_variant(variant).itile() - 1) / regf_variant(variant).itile()) *
-                               regf_variant(variant).itile();
-  rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, list_cap, st);
-  if (rc != GPUNB_OK) return rc;
-  CUDA_OR(launch_list_finalize_offsets(list_off, o.btot, ni, st), GPUNB_E_CUDA);
-  return GPUNB_OK;
+  auto issue = [&](cudaStream_t s) -> int {
+    ISet is;
+    is.h2 = h2; is.dtr = dtr; is.x = xi; is.v = vi; is.ni = ni;
+    is.perm = nullptr;
+    is.rec = nullptr;
+    if (g.precision == 0 && order_iset(is, s) != GPUNB_OK) return GPUNB_E_ALLOC;
+    int rc = run_pair_pass(is, nnbmax, mflag, variant, S, s, false);
+    if (rc != GPUNB_OK) return rc;
+    const int nb = list_scan_blocks(ni);
+    if (!g.rowlen.ensure((size_t)ni * sizeof(int)) ||
+        !g.btot.ensure((size_t)(nb + 1) * sizeof(int)))
+      return GPUNB_E_ALLOC;
+    RegfDev o;
+    o.acc = acc; o.jrk = jrk; o.pot = pot; o.nnb = nnb;
+    o.rowlen = g.rowlen.as<int>(); o.off = list_off; o.btot = g.btot.as<int>(); o.dense = list;
+    const int itile = g.precision == 1 ? FP64_THREADS : regf_variant(variant).itile();
+    const int ni_pad = ((ni + itile - 1) / itile) * itile;
+    rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, list_cap, s);
+    if (rc != GPUNB_OK) return rc;
+    CUDA_OR(launch_list_finalize_offsets(list_off, o.btot, ni, s), GPUNB_E_CUDA);
+    return GPUNB_OK;
+  };
+  // timing mode records host-side event bookkeeping per launch: run eagerly
+  if (g_use_graphs && !g.timing) {
+    const std::vector<long long> key = {
+        1, ni, g.nj, nnbmax, m_flag, (long long)list_cap, g.precision, variant, S,
+        (long long)(uintptr_t)h2, (long long)(uintptr_t)dtr, (long long)(uintptr_t)xi,
+        (long long)(uintptr_t)vi, (long long)(uintptr_t)acc, (long long)(uintptr_t)jrk,
+        (long long)(uintptr_t)pot, (long long)(uintptr_t)nnb, (long long)(uintptr_t)list_off,
+        (long long)(uintptr_t)list, (long long)(uintptr_t)st};
+    return run_graphed(dev_graph(key), true, st, issue);
+  }
+  return issue(st);
 }
 
 }  // extern "C"

@@ -9,6 +9,7 @@
 // depend on the order beyond FP32 summation order; the order itself is a pure
 // function of the positions (deterministic bounding box, stable radix sort).
 #include <algorithm>
+#include <climits>
 #include <cub/device/device_radix_sort.cuh>
 
 #include "common.cuh"
@@ -68,14 +69,35 @@ __global__ void __launch_bounds__(BBOX_THREADS) bbox_kernel(const double *__rest
   if (threadIdx.x == 0) last = atomicAdd(bb + BBOX_TICKET, 1) == (int)gridDim.x - 1;
   __syncthreads();
   if (!last) return;
+  // last block: thread b reads partial b (all loads in flight at once), then
+  // the same warp + shared-memory reduction (on order-preserving ints)
+  __shared__ int si[BBOX_THREADS / 32][6];
+  int r[6];
+#pragma unroll
+  for (int q = 0; q < 6; ++q) r[q] = q < 3 ? INT_MAX : INT_MIN;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += BBOX_THREADS) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const int u = __ldcg(bb + BBOX_PART + 6 * b + q);
+      r[q] = q < 3 ? min(r[q], u) : max(r[q], u);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 6; ++q)
+    for (int o = 16; o > 0; o >>= 1) {
+      const int u = __shfl_xor_sync(0xffffffffu, r[q], o);
+      r[q] = q < 3 ? min(r[q], u) : max(r[q], u);
+    }
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) si[warp][q] = r[q];
+  }
+  __syncthreads();
   if (threadIdx.x < 6) {
     const int q = threadIdx.x;
-    int r = __ldcg(bb + BBOX_PART + q);
-    for (int b = 1; b < (int)gridDim.x; ++b) {
-      const int u = __ldcg(bb + BBOX_PART + 6 * b + q);
-      r = q < 3 ? min(r, u) : max(r, u);
-    }
-    bb[q] = r;
+    int t = si[0][q];
+    for (int w = 1; w < BBOX_THREADS / 32; ++w) t = q < 3 ? min(t, si[w][q]) : max(t, si[w][q]);
+    bb[q] = t;
   }
   if (threadIdx.x == 0) bb[BBOX_TICKET] = 0;
 }

@@ -200,22 +200,27 @@ __global__ void regf_prep_kernel(const ISet is, float4 *__restrict__ rec, int *e
   const int i = is.perm ? is.perm[slot] : slot;
   if (i < 0) return;   // padding slot of a batched layout (never read)
   const double x0 = is.x[3 * i], x1 = is.x[3 * i + 1], x2 = is.x[3 * i + 2];
-  const double v0 = is.v[3 * i], v1 = is.v[3 * i + 1], v2 = is.v[3 * i + 2];
-  const double h2 = is.h2[i], dtr = is.dtr[i];
-  if (isnan(x0) || isnan(x1) || isnan(x2) || isnan(v0) || isnan(v1) || isnan(v2) || isnan(h2) ||
-      isnan(dtr))
-    raise_error(err, GPUNB_E_NAN);
+  // FP32 from here on except the double-single split (FP64 runs at about
+  // 1/64 of the FP32 rate on GB300).  The bounds are formed from the rounded
+  // values (within 2^-22 of the exact ones) and widened with upward rounding
+  // by 2^-12 + 2^-20, so they stay above sqrt(h2)(1 + 2^-12) etc.
+  const float v0 = (float)is.v[3 * i], v1 = (float)is.v[3 * i + 1], v2 = (float)is.v[3 * i + 2];
+  const float h2 = (float)is.h2[i], dtr = (float)is.dtr[i];
   float xh, xl, yh, yl, zh, zl;
   ds_split(x0, xh, xl);
   ds_split(x1, yh, yl);
   ds_split(x2, zh, zl);
-  const double grow = 1.0 + 0x1p-12;
+  if (isnan(xh) || isnan(yh) || isnan(zh) || isnan(v0) || isnan(v1) || isnan(v2) || isnan(h2) ||
+      isnan(dtr))
+    raise_error(err, GPUNB_E_NAN);
+  constexpr float grow = 1.0f + 0x1p-12f + 0x1p-20f;
+  const float va = sqrtf(fmaf(v0, v0, fmaf(v1, v1, v2 * v2)));
   float4 *r = rec + 4 * (size_t)slot;
   r[0] = make_float4(-xh, -yh, -zh, -xl);
-  r[1] = make_float4(-yl, -zl, -(float)v0, -(float)v1);
-  r[2] = make_float4(-(float)v2, (float)(sqrt(fmax(h2, 0.0)) * grow), (float)(fabs(dtr) * grow),
-                     (float)(sqrt(v0 * v0 + v1 * v1 + v2 * v2) * grow));
-  r[3] = make_float4((float)h2, (float)dtr, __int_as_float(i), 0.f);
+  r[1] = make_float4(-yl, -zl, -v0, -v1);
+  r[2] = make_float4(-v2, __fmul_ru(sqrtf(fmaxf(h2, 0.f)), grow), __fmul_ru(fabsf(dtr), grow),
+                     __fmul_ru(va, grow));
+  r[3] = make_float4(h2, dtr, __int_as_float(i), 0.f);
 }
 
 __device__ __forceinline__ void load_istate(IState &I, const float4 *__restrict__ rec, int slot,
@@ -750,10 +755,11 @@ __device__ __forceinline__ void merge_store(const double *s, int i, const int *_
 // belongs to i = perm[s] (identity without a permutation).
 //
 // Many j-splits (small active blocks): one block of MERGE_THREADS per slot,
-// each thread summing a strided subset of the splits, then a fixed
-// shared-memory tree, so the order of the FP64 additions is the same in
-// every run.
+// each thread summing a strided subset of the splits (four splits' loads in
+// flight at a time, added in split order), then a fixed shared-memory tree,
+// so the order of the FP64 additions is the same in every run.
 constexpr int MERGE_THREADS = 128;
+constexpr int MERGE_UNROLL = 4;
 __global__ void __launch_bounds__(MERGE_THREADS)
     regf_merge_wide_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
                            const int *__restrict__ perm, const int *__restrict__ cnt, int nnbmax,
@@ -765,10 +771,19 @@ __global__ void __launch_bounds__(MERGE_THREADS)
   double s[NQ];
 #pragma unroll
   for (int c = 0; c < NQ; ++c) s[c] = 0.0;
-  for (int k = t; k < S; k += MERGE_THREADS) {
-    const double *p = part + (size_t)k * NQ * ni_pad + slot;
+  for (int k0 = t; k0 < S; k0 += MERGE_THREADS * MERGE_UNROLL) {
+    double a[MERGE_UNROLL][NQ];
 #pragma unroll
-    for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * ni_pad];
+    for (int u = 0; u < MERGE_UNROLL; ++u) {
+      const int k = k0 + u * MERGE_THREADS;
+      const double *p = part + (size_t)k * NQ * ni_pad + slot;
+#pragma unroll
+      for (int c = 0; c < NQ; ++c) a[u][c] = (k < S) ? p[(size_t)c * ni_pad] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < MERGE_UNROLL; ++u)
+#pragma unroll
+      for (int c = 0; c < NQ; ++c) s[c] += a[u][c];
   }
 #pragma unroll
   for (int c = 0; c < NQ; ++c) sh[c][t] = s[c];
@@ -982,14 +997,84 @@ __device__ __forceinline__ void gather_row_regs(const int *__restrict__ row, int
   }
 }
 
+// Bucket sort of a row of 33..256 distinct ids by one warp: 32 buckets
+// spanning [min, max] of the row, filled through shared-memory counters; each
+// id's place is then its bucket's start plus the number of smaller ids in the
+// bucket.  The ids are distinct, so the result does not depend on the order
+// in which the counters hand out bucket slots.  Returns false, with nothing
+// written, when a bucket holds more than GATHER_BUCKET_MAX ids (ids clustered
+// in index): the caller then uses the sorting network.
+constexpr int GATHER_BUCKET_MAX = 24;
+__device__ __forceinline__ bool gather_row_buckets(const int *__restrict__ row, int n, int lane,
+                                                   int *__restrict__ sb, int *__restrict__ start,
+                                                   int *__restrict__ out) {
+  int v[8], b[8], pos[8];
+  int lo = INT_MAX, hi = INT_MIN;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int u = r * 32 + lane;
+    v[r] = (u < n) ? row[u] : 0;
+    if (u < n) {
+      lo = min(lo, v[r]);
+      hi = max(hi, v[r]);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  // bucket = floor((v - lo) * 32 / (hi - lo + 1)), in FP32: a non-decreasing
+  // function of v, which is all the bucket order needs
+  const float scale = 32.0f / ((float)hi - (float)lo + 1.0f);
+  start[lane] = 0;
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int u = r * 32 + lane;
+    b[r] = min(31, max(0, (int)((float)(v[r] - lo) * scale)));
+    if (u < n) pos[r] = atomicAdd(&start[b[r]], 1);
+  }
+  __syncwarp();
+  const int c = start[lane];
+  if (__any_sync(0xffffffffu, c > GATHER_BUCKET_MAX)) return false;
+  int ex = c;   // inclusive scan of the bucket sizes
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, ex, o);
+    if (lane >= o) ex += y;
+  }
+  start[lane] = ex - c;
+  if (lane == 31) start[32] = ex;
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int u = r * 32 + lane;
+    if (u < n) sb[start[b[r]] + pos[r]] = v[r];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    if (r * 32 >= n) break;
+    const int u = r * 32 + lane;
+    if (u < n) {
+      const int s0 = start[b[r]], s1 = start[b[r] + 1];
+      int rank = s0;
+      for (int k = s0; k < s1; ++k) rank += sb[k] < v[r];
+      out[rank] = v[r];
+    }
+  }
+  return true;
+}
+
 // Row i (its accepted neighbours, appended in any order by the pair kernel)
 // -> ascending, into the compacted list at off[i] + boff[i / SCAN_ITEMS].
-// Rows of up to 256 ids are sorted in registers, up to GATHER_SMEM_IDS in
-// shared memory, longer ones in place (odd-even transposition).
+// Rows of up to 32 ids are sorted in registers, up to 256 by buckets (or in
+// registers when their ids cluster), up to GATHER_SMEM_IDS in shared memory,
+// longer ones in place (odd-even transposition).
 __global__ void __launch_bounds__(32 * GATHER_WARPS) list_gather_kernel(
     int *__restrict__ rows, int cap, const int *__restrict__ len, const int *__restrict__ off,
     const int *__restrict__ boff, int ni, int *__restrict__ dense) {
   __shared__ int buf[GATHER_WARPS][GATHER_SMEM_IDS];
+  __shared__ int bcnt[GATHER_WARPS][33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = blockIdx.x * GATHER_WARPS + warp;
   if (i >= ni) return;
@@ -998,6 +1083,7 @@ __global__ void __launch_bounds__(32 * GATHER_WARPS) list_gather_kernel(
   int *row = rows + (size_t)i * cap;
   const int o = off[i] + boff[i / SCAN_ITEMS];
   if (n <= 32) { gather_row_regs<1>(row, n, lane, dense + o); return; }
+  if (n <= 256 && gather_row_buckets(row, n, lane, buf[warp], bcnt[warp], dense + o)) return;
   if (n <= 64) { gather_row_regs<2>(row, n, lane, dense + o); return; }
   if (n <= 128) { gather_row_regs<4>(row, n, lane, dense + o); return; }
   if (n <= 256) { gather_row_regs<8>(row, n, lane, dense + o); return; }

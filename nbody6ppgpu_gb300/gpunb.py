@@ -87,6 +87,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                                      C.c_int, C.c_void_p], C.c_int),
         "gpunb_batch_last_plan": ([ip, ip], C.c_int),
         "gpunb_set_graphs": ([C.c_int], None),
+        "gpunb_device_status": ([C.c_void_p], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

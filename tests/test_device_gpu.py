@@ -1,0 +1,129 @@
+"""The single-set device entry points (gpunb_send_device / gpunb_regf_device):
+the same results as the host-array ABI, CUDA-graph replay that reproduces
+eager calls bit for bit on changed inputs, and device-side errors read back
+through gpunb_device_status."""
+import numpy as np
+import pytest
+
+from nbody6ppgpu_gb300 import ics
+from nbody6ppgpu_gb300.gpunb import GpuNb, load
+
+pytestmark = pytest.mark.gpu
+
+N = 8192
+NNBMAX = 256
+
+
+@pytest.fixture(scope="module")
+def case():
+    c = ics.plummer(N, seed=31, masses="kroupa", nb_target=60.0)
+    return c, c.h2()
+
+
+class DeviceCall:
+    """Device copies of one j-set and one active block, and the outputs."""
+
+    def __init__(self, c, h2, act):
+        import torch
+        self.torch = torch
+        dev = torch.device("cuda", 0)
+        T = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(dev, dtype=torch.float64)
+        self.m, self.x, self.v = T(c.m), T(c.x), T(c.v)
+        self.h2, self.dtr, self.xi, self.vi = T(h2[act]), T(c.dtr[act]), T(c.x[act]), T(c.v[act])
+        ni = len(act)
+        self.ni = ni
+        self.acc = torch.empty((ni, 3), dtype=torch.float64, device=dev)
+        self.jrk = torch.empty((ni, 3), dtype=torch.float64, device=dev)
+        self.pot = torch.empty(ni, dtype=torch.float64, device=dev)
+        self.nnb = torch.empty(ni, dtype=torch.int32, device=dev)
+        self.off = torch.empty(ni + 1, dtype=torch.int32, device=dev)
+        self.lst = torch.empty(ni * NNBMAX, dtype=torch.int32, device=dev)
+
+    def run(self, lib):
+        self.torch.cuda.synchronize()   # the library works on its own stream
+        rc = lib.gpunb_send_device(N, self.m.data_ptr(), self.x.data_ptr(), self.v.data_ptr(), None)
+        assert rc == 0
+        rc = lib.gpunb_regf_device(self.ni, self.h2.data_ptr(), self.dtr.data_ptr(),
+                                   self.xi.data_ptr(), self.vi.data_ptr(), self.acc.data_ptr(),
+                                   self.jrk.data_ptr(), self.pot.data_ptr(), self.nnb.data_ptr(),
+                                   self.off.data_ptr(), self.lst.data_ptr(), self.ni * NNBMAX,
+                                   NNBMAX, 0, None)
+        assert rc == 0
+        assert lib.gpunb_device_status(None) == 0
+        off = self.off.cpu().numpy()
+        lst = self.lst.cpu().numpy()
+        return (self.acc.cpu().numpy(), self.jrk.cpu().numpy(), self.pot.cpu().numpy(),
+                self.nnb.cpu().numpy(), [lst[off[i]:off[i + 1]].copy() for i in range(self.ni)])
+
+
+@pytest.mark.parametrize("ni", [37, 1024, N])
+def test_device_entry_points_match_host_abi(case, ni):
+    c, h2 = case
+    act = ics.active_set(N, ni, seed=ni)
+    lib = load()
+    with GpuNb(N) as nb:
+        nb.send(c.m, c.x, c.v)
+        host = nb.regf(h2[act], c.dtr[act], c.x[act], c.v[act], NNBMAX + 1, NNBMAX)
+        acc, jrk, pot, nnb, rows = DeviceCall(c, h2, act).run(lib)
+    assert np.array_equal(acc, host.acc) and np.array_equal(jrk, host.jrk)
+    assert np.array_equal(pot, host.pot)
+    assert np.array_equal(nnb, host.list[:, 0])
+    for i in range(ni):
+        k = host.list[i, 0]
+        assert np.array_equal(rows[i], host.list[i, 1:1 + k] if k > 0 else []), i
+
+
+@pytest.mark.parametrize("ni", [37, 4096])
+def test_graph_replay_matches_eager_calls(case, ni):
+    """Eager results for inputs A and B; then, with graphs on, A (eager run
+    and capture), B and A again (replays): the same bits every time."""
+    c, h2 = case
+    act = ics.active_set(N, ni, seed=ni + 1)
+    lib = load()
+    with GpuNb(N) as nb:
+        d = DeviceCall(c, h2, act)
+        a_eager = d.run(lib)
+        x0, xi0 = d.x.clone(), d.xi.clone()
+        d.x.add_(1e-3)          # B: the whole system shifted and the j-set perturbed
+        d.x[::7].mul_(1.01)
+        d.xi.copy_(d.x[d.torch.as_tensor(act, device=d.x.device)])
+        b_eager = d.run(lib)
+        lib.gpunb_set_graphs(1)
+        try:
+            d.x.copy_(x0); d.xi.copy_(xi0)
+            a_cap = d.run(lib)
+            d.x.add_(1e-3)
+            d.x[::7].mul_(1.01)
+            d.xi.copy_(d.x[d.torch.as_tensor(act, device=d.x.device)])
+            b_rep = d.run(lib)
+            d.x.copy_(x0); d.xi.copy_(xi0)
+            a_rep = d.run(lib)
+        finally:
+            lib.gpunb_set_graphs(0)
+    for got, want in ((a_cap, a_eager), (b_rep, b_eager), (a_rep, a_eager)):
+        for g_, w_ in zip(got[:4], want[:4]):
+            assert np.array_equal(g_, w_)
+        assert all(np.array_equal(p, q) for p, q in zip(got[4], want[4]))
+    assert not np.array_equal(a_eager[0], b_eager[0])
+
+
+def test_device_status_reports_nan(case):
+    c, h2 = case
+    act = ics.active_set(N, 64, seed=5)
+    lib = load()
+    with GpuNb(N) as nb:
+        d = DeviceCall(c, h2, act)
+        d.xi[3, 1] = float("nan")
+        d.torch.cuda.synchronize()
+        lib.gpunb_clear_error()
+        rc = lib.gpunb_send_device(N, d.m.data_ptr(), d.x.data_ptr(), d.v.data_ptr(), None)
+        assert rc == 0
+        rc = lib.gpunb_regf_device(d.ni, d.h2.data_ptr(), d.dtr.data_ptr(), d.xi.data_ptr(),
+                                   d.vi.data_ptr(), d.acc.data_ptr(), d.jrk.data_ptr(),
+                                   d.pot.data_ptr(), d.nnb.data_ptr(), d.off.data_ptr(),
+                                   d.lst.data_ptr(), d.ni * NNBMAX, NNBMAX, 0, None)
+        assert rc == 0                                    # queued; the kernel flags the NaN
+        assert lib.gpunb_device_status(None) == 3         # GPUNB_E_NAN
+        assert lib.gpunb_last_error() == 3
+        lib.gpunb_clear_error()
+        assert lib.gpunb_device_status(None) == 0         # the word was cleared
