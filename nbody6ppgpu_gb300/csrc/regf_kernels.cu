@@ -145,10 +145,11 @@ __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restric
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       M[M_OH + c] = o[c];
-      M[M_OL + c] = 0.f;
+      // half-extent of the box about O (0 for an empty tile)
+      M[M_BOX + c] = (bb[c] >= -bb[3 + c]) ? __fmul_ru(0.5f * (bb[c] + bb[3 + c]), grow) : 0.f;
     }
     M[M_OH + 3] = 0.f;
-    M[M_OL + 3] = 0.f;
+    M[M_BOX + 3] = 0.f;
   }
 }
 
@@ -559,24 +560,36 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
       const float *M = T + NFIELD * JT;
       const float vmax = M[M_VMAX], smax = M[M_SMAX], rad = M[M_RAD];
       const float ohx = M[M_OH], ohy = M[M_OH + 1], ohz = M[M_OH + 2];
-      const float olx = M[M_OL], oly = M[M_OL + 1], olz = M[M_OL + 2];
+      const float bx = M[M_BOX], by = M[M_BOX + 1], bz = M[M_BOX + 2];
       const int jbeg = wj * JW;
 #pragma unroll
       for (int k = 0; k < IPT; ++k) {
         TileCtx C;
         // O - x_i from the double-single parts, rounded once to FP32
-        C.ox = mk2(__fadd_rn(__fadd_rn(ohx, I[k].nxh), __fadd_rn(olx, I[k].nxl)));
-        C.oy = mk2(__fadd_rn(__fadd_rn(ohy, I[k].nyh), __fadd_rn(oly, I[k].nyl)));
-        C.oz = mk2(__fadd_rn(__fadd_rn(ohz, I[k].nzh), __fadd_rn(olz, I[k].nzl)));
+        C.ox = mk2(__fadd_rn(__fadd_rn(ohx, I[k].nxh), I[k].nxl));
+        C.oy = mk2(__fadd_rn(__fadd_rn(ohy, I[k].nyh), I[k].nyl));
+        C.oz = mk2(__fadd_rn(__fadd_rn(ohz, I[k].nzh), I[k].nzl));
         const float base = I[k].dv * (I[k].va + vmax);
         float b = MFLAG ? fmaf(I[k].s, smax, base) : I[k].s + base;
         b = fmaf(rad, 0x1p-20f, b);   // the tile-relative rounding, 2^-22 (R + r) per axis
         C.H = (I[k].s < 0.f) ? -1.0f : b * b;
         C.R = rad;
-        // near tiles (|O - x_i| < 2R for a lane of the warp) take the
-        // double-single path, the others the tile-relative one
+        // The tile-relative difference (x_j - O) + o errs by less than
+        // 2^-24 (R + |o| + |dx|) per component.  Every j of the tile lies at
+        // least max(|o| - R, d_box) from x_i (d_box: distance to the tile's
+        // box); while that bound is at least (R + |o|)/3 the error stays
+        // below 2^-22 |dx|, as for every tile with |o| >= 2R.  A tile where
+        // the bound fails for a lane of the warp (|o| < 2R and
+        // R + |o| > 3 d_box) is near and takes the double-single path.
         const float o2 = C.ox.x * C.ox.x + C.oy.x * C.oy.x + C.oz.x * C.oz.x;
-        const bool near = (I[k].s >= 0.f) && (o2 < GPUNB_NEAR_K2 * rad * rad);
+        bool near = (I[k].s >= 0.f) && (o2 < GPUNB_NEAR_K2 * rad * rad);
+        if (near) {
+          const float ex = fmaxf(fabsf(C.ox.x) - bx, 0.f);
+          const float ey = fmaxf(fabsf(C.oy.x) - by, 0.f);
+          const float ez = fmaxf(fabsf(C.oz.x) - bz, 0.f);
+          const float ro = rad + sqrtf(o2);
+          near = ro * ro > 9.0f * (ex * ex + ey * ey + ez * ez);
+        }
         if (__any_sync(0xffffffffu, near)) {
           C.nxh = mk2(I[k].nxh); C.nyh = mk2(I[k].nyh); C.nzh = mk2(I[k].nzh);
           C.nxl = mk2(I[k].nxl); C.nyl = mk2(I[k].nyl); C.nzl = mk2(I[k].nzl);

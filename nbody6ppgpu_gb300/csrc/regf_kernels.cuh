@@ -19,8 +19,9 @@ namespace gpunb {
 //     carries an absolute error below 2^-22 (R + |dx|) per component, within
 //     2^-21 |dx| for the tiles this path is used for (|o| >= 2R);
 //   * as double-single hi/lo pairs, for the tiles near the warp's i-particles
-//     (|o| < 2R for one of them): dx = (hi_j - hi_i) + (lo_j - lo_i), three
-//     additions per component, error 2^-23 |dx|.
+//     (for one of them |o| < 2R and R + |o| > 3 d, d the distance to the
+//     tile's box): dx = (hi_j - hi_i) + (lo_j - lo_i), three additions per
+//     component, error 2^-23 |dx|.
 constexpr int JT = 128;
 enum JField {
   F_XR = 0, F_YR, F_ZR, F_VX, F_VY, F_VZ, F_MN,   // far tiles read these 7
@@ -37,9 +38,9 @@ static_assert(TILE_BYTES % 16 == 0, "tile must be a multiple of 16 bytes");
 // metadata (float offsets from NFIELD*JT):
 //   [0] max |v_j| over the tile (rounded up)   [1] sqrt(max m_j) (rounded up)
 //   [2] number of real bodies                  [3] tile radius R (rounded up)
-//   [4..6] hi parts of O (x, y, z)              [7] unused
-//   [8..10] lo parts of O                       [11] unused
-enum TileMeta { M_VMAX = 0, M_SMAX, M_COUNT, M_RAD, M_OH = 4, M_OL = 8 };
+//   [4..6] O (x, y, z), an FP32 number          [7] unused
+//   [8..10] half-extents of the tile's box      [11] unused
+enum TileMeta { M_VMAX = 0, M_SMAX, M_COUNT, M_RAD, M_OH = 4, M_BOX = 8 };
 
 // FP64 j tile for the plain FP64 kernel (three bulk copies per tile).
 constexpr int JT64 = 64;
