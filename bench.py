@@ -646,14 +646,21 @@ def main():
             nb.send(c.m, c.x, c.v)
             outs[ni] = nb.regf(*hin[ni], LMAX, NNBMAX, out=outs.get(ni))
 
-    for _ in range(args.warmup):
-        host_step()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        host_step()
-    e2e_s = (time.perf_counter() - t0) / args.steps
+    def host_steps(graphs):
+        lib.gpunb_set_graphs(1 if graphs else 0)   # each call shape replayed as a graph
+        for _ in range(args.warmup):
+            host_step()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            host_step()
+        dt = (time.perf_counter() - t0) / args.steps
+        lib.gpunb_set_graphs(0)
+        return dt
+
+    e2e_nograph_s = host_steps(False)
+    e2e_s = host_steps(True)
     if dist:
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -714,6 +721,7 @@ def main():
                      "peak_source": f"nominal FP32: {n_sm} SMs x 128 lanes x 2 x {peak_mhz:.0f} MHz"
                                     " (MEASURED_PEAKS.json has no FP32 entry)"},
         "e2e": {"value": ws * pairs_per_step / e2e_s / 1e9, "unit": "Gpairs/s",
+                "value_without_graphs": ws * pairs_per_step / e2e_nograph_s / 1e9,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": own_per_step * args.steps,
         "library_launches": {"cub_radix_sort": 43 * args.steps},

@@ -156,12 +156,14 @@ int gpunb_batch_regf_device(int ncl, const int *ni, const double *h2, const doub
 /* Launch plan of the last batched call: kernel variant and work items. */
 int gpunb_batch_last_plan(int *variant, int *items);
 
-/* CUDA graphs for the device entry points (gpunb_send_device,
- * gpunb_regf_device and the batched pair): with flag = 1, the first call of a
- * shape (sizes, active counts, caller pointers, stream, launch plan) runs
- * normally and is then captured; later calls of that shape replay the graph
- * while no library buffer has moved.  Calls made with per-launch timing on
- * (gpunb_set_timing) run without graphs.  Default 0. */
+/* CUDA graphs: with flag = 1, the first call of a shape (sizes, active
+ * counts, caller pointers, stream, launch plan) runs normally and is then
+ * captured; later calls of that shape replay the graph while no library
+ * buffer has moved.  Covers gpunb_send_device, gpunb_regf_device, the batched
+ * pair, and gpunb_send_ / gpunb_regf_ where the device reads host memory
+ * directly (gpunb_set_host_path).  Calls made with per-launch timing on
+ * (gpunb_set_timing) run without graphs.  Default 0, or the value of the
+ * environment variable GPUNB_GRAPHS. */
 void gpunb_set_graphs(int flag);
 
 /* Potential of gpupot_ for callers that cannot allocate device memory (no

@@ -183,6 +183,7 @@ struct PinBuf {
     if (p) cudaFreeHost(p);
     p = nullptr;
     bytes = 0;
+    ++g_alloc_gen;   // pinned buffers appear in captured graphs too
     size_t want = n + n / 4 + 256;
     if (cudaMallocHost(&p, want) != cudaSuccess) {
       cudaGetLastError();
@@ -193,7 +194,10 @@ struct PinBuf {
     return true;
   }
   void release() {
-    if (p) cudaFreeHost(p);
+    if (p) {
+      cudaFreeHost(p);
+      ++g_alloc_gen;
+    }
     p = nullptr;
     bytes = 0;
   }
@@ -317,6 +321,7 @@ static bool devinit(int irank) {
   g.devinit = true;
   if (const char *p = getenv("GPUNB_TUNE_CACHE")) gpunb_tune_load(p);
   if (const char *p = getenv("GPUNB_AUTOTUNE")) g.autotune_on = atoi(p);
+  if (const char *p = getenv("GPUNB_GRAPHS")) g_use_graphs = atoi(p) != 0;
   return true;
 }
 
@@ -592,6 +597,90 @@ static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out
 }
 
 // ---------------------------------------------------------------------------
+// host-buffer regf where the device reads and writes the caller's arrays
+// (coherent host memory): every step is device work, so the call is one
+// launch sequence, replayed as a CUDA graph per call key when graphs are on.
+static void regf_host_direct(int ni, const double *h2, const double *dtr, const double (*xi)[3],
+                             const double (*vi)[3], double (*acc)[3], double (*jrk)[3],
+                             double *pot, int lmax, int nnbmax, int *list, int m_flag,
+                             double t_begin) {
+  cudaStream_t st = g.stream;
+  const bool mflag = m_flag != 0;
+  int variant, S;
+  choose_plan(ni, mflag, variant, S);
+  if (!g.hout.ensure(sizeof(int))) return;
+  int *h_err = g.hout.as<int>();
+  auto issue = [&](cudaStream_t s) -> int {
+    double *din = g.iraw.as<double>();
+    CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), s), GPUNB_E_CUDA);
+    HostCopyJobs jobs;
+    jobs.count = 4;
+    jobs.j[0] = HostCopyJob{h2, din, ni, 8};
+    jobs.j[1] = HostCopyJob{dtr, din + ni, ni, 8};
+    jobs.j[2] = HostCopyJob{xi, din + 2 * (size_t)ni, 3ll * ni, 8};
+    jobs.j[3] = HostCopyJob{vi, din + 5 * (size_t)ni, 3ll * ni, 8};
+    CUDA_OR(launch_host_copy(jobs, s), GPUNB_E_CUDA);
+    ISet is;
+    is.h2 = din;
+    is.dtr = din + ni;
+    is.x = din + 2 * (size_t)ni;
+    is.v = din + 5 * (size_t)ni;
+    is.ni = ni;
+    is.perm = nullptr;
+    is.rec = nullptr;
+    if (g.precision == 0 && order_iset(is, s) != GPUNB_OK) return GPUNB_E_ALLOC;
+    int rc = run_pair_pass(is, nnbmax, mflag, variant, S, s, false);
+    if (rc != GPUNB_OK) return rc;
+    const int nb = list_scan_blocks(ni);
+    if (!g.outblk.ensure((size_t)7 * ni * sizeof(double) + (size_t)(ni + 2) * sizeof(int)) ||
+        !g.rowlen.ensure((size_t)ni * sizeof(int)) ||
+        !g.off.ensure((size_t)(ni + 1) * sizeof(int)) ||
+        !g.btot.ensure((size_t)(nb + 1) * sizeof(int)) ||
+        !g.dense.ensure((size_t)ni * std::max(nnbmax, 1) * sizeof(int)))
+      return GPUNB_E_ALLOC;
+    double *ob = g.outblk.as<double>();
+    RegfDev o;
+    o.acc = ob;
+    o.jrk = ob + 3 * (size_t)ni;
+    o.pot = ob + 6 * (size_t)ni;
+    o.nnb = (int *)(ob + 7 * (size_t)ni);
+    o.rowlen = g.rowlen.as<int>();
+    o.off = g.off.as<int>();
+    o.btot = g.btot.as<int>();
+    o.dense = g.dense.as<int>();
+    const int itile = g.precision == 1 ? FP64_THREADS : regf_variant(variant).itile();
+    const int ni_pad = ((ni + itile - 1) / itile) * itile;
+    rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, 0, s);
+    if (rc != GPUNB_OK) return rc;
+    // results straight into the caller's arrays; the device writes the rows
+    CUDA_OR(launch_list_rows(o.dense, o.off, o.btot, o.nnb, ni, lmax, list, s), GPUNB_E_CUDA);
+    HostCopyJobs oj;
+    oj.count = 4;
+    oj.j[0] = HostCopyJob{o.acc, acc, 3ll * ni, 8};
+    oj.j[1] = HostCopyJob{o.jrk, jrk, 3ll * ni, 8};
+    oj.j[2] = HostCopyJob{o.pot, pot, ni, 8};
+    oj.j[3] = HostCopyJob{g.err.p, h_err, 1, 4};
+    CUDA_OR(launch_host_copy(oj, s), GPUNB_E_CUDA);
+    return GPUNB_OK;
+  };
+  int rc;
+  if (g_use_graphs && !g.timing) {
+    const std::vector<long long> key = {
+        3, ni, g.nj, lmax, nnbmax, m_flag, g.precision, variant, S,
+        (long long)(uintptr_t)h2, (long long)(uintptr_t)dtr, (long long)(uintptr_t)xi,
+        (long long)(uintptr_t)vi, (long long)(uintptr_t)acc, (long long)(uintptr_t)jrk,
+        (long long)(uintptr_t)pot, (long long)(uintptr_t)list, (long long)(uintptr_t)st};
+    rc = run_graphed(dev_graph(key), true, st, issue);
+  } else {
+    rc = issue(st);
+  }
+  if (rc != GPUNB_OK) return;
+  CUDA_OR(cudaStreamSynchronize(st), );
+  g.time_grav += wtime() - t_begin;
+  check_device_error(*h_err);
+}
+
+// ---------------------------------------------------------------------------
 // host-buffer regf: the gpunb_regf_ contract
 static void regf_host(int ni, const double *h2, const double *dtr, const double (*xi)[3],
                       const double (*vi)[3], double (*acc)[3], double (*jrk)[3], double *pot,
@@ -616,6 +705,11 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   const size_t in_doubles = (size_t)8 * ni;
   if (!g.iraw.ensure(in_doubles * sizeof(double))) return;
   double *din = g.iraw.as<double>();
+  if (g.host_direct && !(g.autotune_on && g.precision == 0 && g.force_variant < 0 &&
+                         g.tune.find(tune_key(g.nj, ni, mflag, 0)) == g.tune.end())) {
+    regf_host_direct(ni, h2, dtr, xi, vi, acc, jrk, pot, lmax, nnbmax, list, m_flag, t_begin);
+    return;
+  }
   CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
   if (g.host_direct) {
     HostCopyJobs jobs;
@@ -841,16 +935,46 @@ void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
   const double t0 = wtime();
   g.isend++;
   cudaStream_t st = g.stream;
+  if (g.host_direct) {
+    // the device reads the caller's arrays: the whole call is device work,
+    // replayed as a CUDA graph per (n, arrays) when graphs are on
+    if (!g.hout.ensure(sizeof(int))) return;
+    int *herr = g.hout.as<int>();
+    auto issue = [&](cudaStream_t s) -> int {
+      CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), s), GPUNB_E_CUDA);
+      if (n > 0) {
+        double *d = g.jraw.as<double>();
+        HostCopyJobs jobs;
+        jobs.count = 3;
+        jobs.j[0] = HostCopyJob{mj, d, n, 8};
+        jobs.j[1] = HostCopyJob{xj, d + n, 3ll * n, 8};
+        jobs.j[2] = HostCopyJob{vj, d + 4 * (size_t)n, 3ll * n, 8};
+        CUDA_OR(launch_host_copy(jobs, s), GPUNB_E_CUDA);
+      }
+      const int rc = send_common(n, s);
+      if (rc != GPUNB_OK) return rc;
+      HostCopyJobs ej;
+      ej.count = 1;
+      ej.j[0] = HostCopyJob{g.err.p, herr, 1, 4};
+      CUDA_OR(launch_host_copy(ej, s), GPUNB_E_CUDA);
+      return GPUNB_OK;
+    };
+    int rc;
+    if (g_use_graphs && !g.timing)
+      rc = run_graphed(dev_graph({2, n, (long long)(uintptr_t)mj, (long long)(uintptr_t)xj,
+                                  (long long)(uintptr_t)vj, (long long)(uintptr_t)st}),
+                       true, st, issue);
+    else
+      rc = issue(st);
+    if (rc != GPUNB_OK) return;
+    g.nj = n;
+    CUDA_OR(cudaStreamSynchronize(st), );
+    check_device_error(*herr);
+    g.time_send += wtime() - t0;
+    return;
+  }
   CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
-  if (n > 0 && g.host_direct) {
-    double *d = g.jraw.as<double>();
-    HostCopyJobs jobs;
-    jobs.count = 3;
-    jobs.j[0] = HostCopyJob{mj, d, n, 8};
-    jobs.j[1] = HostCopyJob{xj, d + n, 3ll * n, 8};
-    jobs.j[2] = HostCopyJob{vj, d + 4 * (size_t)n, 3ll * n, 8};
-    CUDA_OR(launch_host_copy(jobs, st), );
-  } else if (n > 0) {
+  if (n > 0) {
     double *h = g.hj.as<double>();
     hcopy(h, mj, (size_t)n * sizeof(double));
     hcopy(h + n, xj, (size_t)n * 3 * sizeof(double));
@@ -861,14 +985,7 @@ void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
   if (send_common(n, st) != GPUNB_OK) return;
   if (!g.hout.ensure(sizeof(int))) return;
   int *herr = g.hout.as<int>();
-  if (g.host_direct) {
-    HostCopyJobs jobs;
-    jobs.count = 1;
-    jobs.j[0] = HostCopyJob{g.err.p, herr, 1, 4};
-    CUDA_OR(launch_host_copy(jobs, st), );
-  } else {
-    CUDA_OR(cudaMemcpyAsync(herr, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
-  }
+  CUDA_OR(cudaMemcpyAsync(herr, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
   CUDA_OR(cudaStreamSynchronize(st), );
   check_device_error(*herr);
   g.time_send += wtime() - t0;

@@ -193,6 +193,10 @@ class GpuNb:
         through pinned buffers.  Returns the mode in effect."""
         return self.lib.gpunb_set_host_path(1 if direct else 0)
 
+    def set_graphs(self, on: bool) -> None:
+        """gpunb_set_graphs: replay each call shape as a CUDA graph."""
+        self.lib.gpunb_set_graphs(1 if on else 0)
+
     def set_timing(self, on: bool) -> None:
         self.lib.gpunb_set_timing(1 if on else 0)
 

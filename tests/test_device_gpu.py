@@ -5,6 +5,7 @@ through gpunb_device_status."""
 import numpy as np
 import pytest
 
+from conftest import rows_equal
 from nbody6ppgpu_gb300 import ics
 from nbody6ppgpu_gb300.gpunb import GpuNb, load
 
@@ -127,3 +128,48 @@ def test_device_status_reports_nan(case):
         assert lib.gpunb_last_error() == 3
         lib.gpunb_clear_error()
         assert lib.gpunb_device_status(None) == 0         # the word was cleared
+
+
+def test_host_abi_graph_replay_matches_eager(case):
+    """gpunb_send_ / gpunb_regf_ replayed as graphs (device reading the host
+    arrays directly) give the eager results bit for bit on changed inputs."""
+    c, h2 = case
+    act = ics.active_set(N, 2000, seed=7)
+    with GpuNb(N) as nb:
+        if not nb.set_host_path(True):
+            pytest.skip("the device does not read host memory directly here")
+        x = c.x.copy()
+        xi = x[act].copy()
+        vi = c.v[act].copy()
+        h2a, dtra = h2[act].copy(), c.dtr[act].copy()
+
+        def call(out=None):
+            nb.send(c.m, x, c.v)
+            r = nb.regf(h2a, dtra, xi, vi, NNBMAX + 1, NNBMAX, out=out)
+            return r.acc.copy(), r.jrk.copy(), r.pot.copy(), r.list.copy(), r
+
+        a_eager = call()
+        x += 1e-3
+        x[::5] *= 1.01
+        xi[:] = x[act]
+        b_eager = call()
+        out = b_eager[4]
+        nb.set_graphs(True)
+        try:
+            x[:] = c.x
+            xi[:] = x[act]
+            a_cap = call(out)
+            x += 1e-3
+            x[::5] *= 1.01
+            xi[:] = x[act]
+            b_rep = call(out)
+            x[:] = c.x
+            xi[:] = x[act]
+            a_rep = call(out)
+        finally:
+            nb.set_graphs(False)
+    for got, want in ((a_cap, a_eager), (b_rep, b_eager), (a_rep, a_eager)):
+        for g_, w_ in zip(got[:3], want[:3]):
+            assert np.array_equal(g_, w_)
+        assert rows_equal(got[3], want[3]) == []   # entries past a row's count are unset
+    assert not np.array_equal(a_eager[0], b_eager[0])
