@@ -173,3 +173,28 @@ def test_host_abi_graph_replay_matches_eager(case):
             assert np.array_equal(g_, w_)
         assert rows_equal(got[3], want[3]) == []   # entries past a row's count are unset
     assert not np.array_equal(a_eager[0], b_eager[0])
+
+
+def test_graphs_follow_buffer_growth(case):
+    """A call shape captured, then a larger j-set that makes the library grow
+    its buffers, then the first shape again: the replay must not use the old
+    buffers (results equal an eager call)."""
+    c, h2 = case
+    act = ics.active_set(N, 500, seed=11)
+    big = ics.plummer(2 * N, seed=32, masses="kroupa", nb_target=60.0)
+    lib = load()
+    with GpuNb(2 * N) as nb:
+        d = DeviceCall(c, h2, act)
+        want = d.run(lib)
+        lib.gpunb_set_graphs(1)
+        try:
+            d.run(lib)                                    # eager run + capture
+            nb.send(big.m, big.x, big.v)                  # grows the library's buffers
+            nb.regf(big.h2()[:4096], big.dtr[:4096], big.x[:4096], big.v[:4096],
+                    NNBMAX + 1, NNBMAX)
+            got = d.run(lib)
+        finally:
+            lib.gpunb_set_graphs(0)
+    for g_, w_ in zip(got[:4], want[:4]):
+        assert np.array_equal(g_, w_)
+    assert all(np.array_equal(p, q) for p, q in zip(got[4], want[4]))
