@@ -62,11 +62,44 @@ __device__ __forceinline__ void flag(int *err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
 
+// Predicted state of every particle, 8 doubles each {x[3], m, v[3], 0}, for
+// the large blocks where the particles' lists cover the set many times over:
+// each prediction is then made once instead of once per listing.  Same
+// arithmetic as the per-pair prediction, so the same bits.
+constexpr int PRED = 8;
+__global__ void irr_pred_kernel(int n, const double *__restrict__ rec, double ti,
+                                double *__restrict__ pred) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[3], v[3], m;
+  predict(rec + (size_t)i * REC, ti, x, v, m);
+  double2 *q = reinterpret_cast<double2 *>(pred + (size_t)i * PRED);
+  q[0] = make_double2(x[0], x[1]);
+  q[1] = make_double2(x[2], m);
+  q[2] = make_double2(v[0], v[1]);
+  q[3] = make_double2(v[2], 0.0);
+}
+
+template <bool PRE>
+__device__ __forceinline__ void state(const double *__restrict__ rec,
+                                      const double *__restrict__ pred, int i, double ti,
+                                      double x[3], double v[3], double &m) {
+  if (PRE) {
+    const double2 *q = reinterpret_cast<const double2 *>(pred + (size_t)i * PRED);
+    const double2 a = q[0], b = q[1], c = q[2], d = q[3];
+    x[0] = a.x; x[1] = a.y; x[2] = b.x; m = b.y;
+    v[0] = c.x; v[1] = c.y; v[2] = d.x;
+  } else {
+    predict(rec + (size_t)i * REC, ti, x, v, m);
+  }
+}
+
+template <bool PRE>
 __global__ void __launch_bounds__(32 * IRR_WARPS)
-    irr_firr_kernel(int n, const double *__restrict__ rec, int lmax, const int *__restrict__ lists,
-                    double ti, int ni, const int *__restrict__ addr, int base,
-                    double *__restrict__ acc, double *__restrict__ jrk, int *__restrict__ nnbid,
-                    int *__restrict__ err) {
+    irr_firr_kernel(int n, const double *__restrict__ rec, const double *__restrict__ pred,
+                    int lmax, const int *__restrict__ lists, double ti, int ni,
+                    const int *__restrict__ addr, int base, double *__restrict__ acc,
+                    double *__restrict__ jrk, int *__restrict__ nnbid, int *__restrict__ err) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   for (int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); k < ni; k += nwarps) {
@@ -78,7 +111,7 @@ __global__ void __launch_bounds__(32 * IRR_WARPS)
       if (lane == 0) flag(err, GPUNB_E_ARG);
     } else {
       double xi[3], vi[3], mi;
-      predict(rec + (size_t)i * REC, ti, xi, vi, mi);
+      state<PRE>(rec, pred, i, ti, xi, vi, mi);
       const int *row = lists + (size_t)i * lmax;
       int nnb = row[0];
       if (nnb < 0 || nnb > lmax - 1) {
@@ -92,7 +125,7 @@ __global__ void __launch_bounds__(32 * IRR_WARPS)
           continue;
         }
         double xj[3], vj[3], mj;
-        predict(rec + (size_t)j * REC, ti, xj, vj, mj);
+        state<PRE>(rec, pred, j, ti, xj, vj, mj);
         const double dx = xj[0] - xi[0], dy = xj[1] - xi[1], dz = xj[2] - xi[2];
         const double dvx = vj[0] - vi[0], dvy = vj[1] - vi[1], dvz = vj[2] - vi[2];
         const double r2 = dx * dx + dy * dy + dz * dz;
@@ -246,6 +279,7 @@ struct State {
   unsigned epoch = 0;
   std::vector<int> uniq;
   DevBuf rec_d, list_d, addr_d, out_d, nid_d, idx_d, stage_d, off_d, err_d, pm_d, px_d, pv_d;
+  DevBuf pred_d;   // predicted states of all particles (large blocks)
   PinBuf stage_h, idx_h, off_h, err_h;
   double time_grav = 0.0;
   unsigned long long num_inter = 0, num_fcall = 0, num_steps = 0;
@@ -281,7 +315,7 @@ static double wtime() {
 
 static void release_all() {
   for (DevBuf *b : {&S.rec_d, &S.list_d, &S.addr_d, &S.out_d, &S.nid_d, &S.idx_d, &S.stage_d,
-                    &S.off_d, &S.err_d, &S.pm_d, &S.px_d, &S.pv_d})
+                    &S.off_d, &S.err_d, &S.pm_d, &S.px_d, &S.pv_d, &S.pred_d})
     b->release();
   for (PinBuf *b : {&S.stage_h, &S.idx_h, &S.off_h, &S.err_h}) b->release();
   S.rec_h.clear();
@@ -406,13 +440,22 @@ static bool upload() {
   return true;
 }
 
-static int launch_firr(int n, const double *rec, int lmax, const int *lists, double ti, int ni,
-                       const int *addr, int base, double *acc, double *jrk, int *nnbid, int *err,
-                       cudaStream_t st) {
+// pred: scratch of n * PRED doubles.  Blocks of at least n/32 particles
+// predict every particle once first (with ~100 neighbours each, the lists
+// then name every particle several times); smaller ones predict per listing.
+static int launch_firr(int n, const double *rec, double *pred, int lmax, const int *lists,
+                       double ti, int ni, const int *addr, int base, double *acc, double *jrk,
+                       int *nnbid, int *err, cudaStream_t st) {
   if (ni <= 0) return GPUNB_OK;
   const long long blocks = std::min<long long>((ni + IRR_WARPS - 1) / IRR_WARPS, 1ll << 20);
-  irr_firr_kernel<<<(unsigned)blocks, 32 * IRR_WARPS, 0, st>>>(n, rec, lmax, lists, ti, ni, addr,
-                                                               base, acc, jrk, nnbid, err);
+  if (pred && 32ll * ni >= n) {
+    irr_pred_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, rec, ti, pred);
+    irr_firr_kernel<true><<<(unsigned)blocks, 32 * IRR_WARPS, 0, st>>>(
+        n, rec, pred, lmax, lists, ti, ni, addr, base, acc, jrk, nnbid, err);
+  } else {
+    irr_firr_kernel<false><<<(unsigned)blocks, 32 * IRR_WARPS, 0, st>>>(
+        n, rec, nullptr, lmax, lists, ti, ni, addr, base, acc, jrk, nnbid, err);
+  }
   return cudaGetLastError() == cudaSuccess ? GPUNB_OK : GPUNB_E_CUDA;
 }
 
@@ -555,10 +598,18 @@ static void firr_vec(double ti, int ni, const int *addr, double (*acc)[3], doubl
   cudaStream_t st = S.st;
   if (!upload()) return;
   IRR_CUDA(cudaMemsetAsync(S.err_d.p, 0, sizeof(int), st), );
+  double *pred = nullptr;
+  if (32ll * ni >= S.nmax) {
+    if (!S.pred_d.ensure((size_t)S.nmax * PRED * sizeof(double))) {
+      failf(GPUNB_E_ALLOC, "irr: prediction buffer allocation failed");
+      return;
+    }
+    pred = S.pred_d.as<double>();
+  }
   if (S.direct) {
     // address list read, results written in the caller's arrays
-    if (launch_firr(S.nmax, S.rec_d.as<double>(), S.lmax, S.list_d.as<int>(), ti, ni, addr, 1,
-                    &acc[0][0], &jrk[0][0], nnbid, S.err_d.as<int>(), st) != GPUNB_OK) {
+    if (launch_firr(S.nmax, S.rec_d.as<double>(), pred, S.lmax, S.list_d.as<int>(), ti, ni,
+                    addr, 1, &acc[0][0], &jrk[0][0], nnbid, S.err_d.as<int>(), st) != GPUNB_OK) {
       failf(GPUNB_E_CUDA, "irr: force kernel launch failed");
       return;
     }
@@ -572,7 +623,7 @@ static void firr_vec(double ti, int ni, const int *addr, double (*acc)[3], doubl
     IRR_CUDA(cudaMemcpyAsync(S.addr_d.p, addr, (size_t)ni * sizeof(int), cudaMemcpyHostToDevice,
                              st), );
     double *o = S.out_d.as<double>();
-    if (launch_firr(S.nmax, S.rec_d.as<double>(), S.lmax, S.list_d.as<int>(), ti, ni,
+    if (launch_firr(S.nmax, S.rec_d.as<double>(), pred, S.lmax, S.list_d.as<int>(), ti, ni,
                     S.addr_d.as<int>(), 1, o, o + 3 * (size_t)ni, S.nid_d.as<int>(),
                     S.err_d.as<int>(), st) != GPUNB_OK) {
       failf(GPUNB_E_CUDA, "irr: force kernel launch failed");
@@ -696,7 +747,7 @@ int irr_firr_device(int n, const double *rec, int lmax, const int *lists, double
                     const int *addr, double *acc, double *jrk, int *nnbid, void *stream) {
   if (n < 0 || lmax < 1 || ni < 0) return GPUNB_E_ARG;
   cudaStream_t st = stream ? (cudaStream_t)stream : S.st;
-  return launch_firr(n, rec, lmax, lists, ti, ni, addr, 0, acc, jrk, nnbid, nullptr, st);
+  return launch_firr(n, rec, nullptr, lmax, lists, ti, ni, addr, 0, acc, jrk, nnbid, nullptr, st);
 }
 
 }  // extern "C"

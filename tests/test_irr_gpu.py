@@ -192,3 +192,19 @@ def test_send_predicted_equals_host_prediction_then_send():
         r2 = nb.regf(h2, dtr, xp[act], vp[act], 129, 128)
     for a, b in ((r1.acc, r2.acc), (r1.jrk, r2.jrk), (r1.pot, r2.pot), (r1.list, r2.list)):
         assert np.array_equal(a, b)
+
+
+def test_whole_set_prediction_gives_the_same_bits():
+    """Blocks of at least n/32 particles predict every particle once before the
+    force loop; smaller blocks predict each listed neighbour in the loop.  The
+    arithmetic is the same, so a particle's result does not depend on which
+    path its block took."""
+    g = load_golden("irr_plummer2048")
+    n = len(g["m"])
+    small = np.arange(0, n, 97)[:40]            # 40 < n/32: per-listing prediction
+    large = np.arange(n)                        # whole-set prediction
+    with _irr(g) as irr:
+        a_s, j_s, n_s = irr.firr(float(g["ti"]), small)
+        a_l, j_l, n_l = irr.firr(float(g["ti"]), large)
+    assert np.array_equal(a_s, a_l[small]) and np.array_equal(j_s, j_l[small])
+    assert np.array_equal(n_s, n_l[small])
