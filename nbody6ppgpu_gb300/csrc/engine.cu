@@ -525,8 +525,8 @@ static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, in
 
 static int finish_lists(int ni, int nnbmax, int S, int ni_pad, const int *perm, const RegfDev &o,
                         size_t list_cap, cudaStream_t st) {
-  CUDA_OR(launch_regf_merge(g.part.as<double>(), S, ni, ni_pad, perm, g.cnt.as<int>(), nnbmax,
-                            o.acc, o.jrk, o.pot, o.nnb, o.rowlen, st),
+  CUDA_OR(launch_regf_merge(g.part.as<double>(), g.precision == 0, S, ni, ni_pad, perm,
+                            g.cnt.as<int>(), nnbmax, o.acc, o.jrk, o.pot, o.nnb, o.rowlen, st),
           GPUNB_E_CUDA);
   CUDA_OR(launch_list_scan(o.rowlen, ni, o.off, o.btot, st), GPUNB_E_CUDA);
   (void)list_cap;

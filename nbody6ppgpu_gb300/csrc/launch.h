@@ -31,9 +31,10 @@ cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int
 cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const ISet &is,
                              const RegfOut &out, cudaStream_t st);
 constexpr int FP64_THREADS = 128;
-cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *perm,
-                              const int *cnt, int nnbmax, double *acc, double *jrk, double *pot,
-                              int *nnb, int *rowlen, cudaStream_t st);
+// ff: the partials are float-float pairs (split kernel), else doubles (FP64 kernel)
+cudaError_t launch_regf_merge(const double *part, bool ff, int S, int ni, int ni_pad,
+                              const int *perm, const int *cnt, int nnbmax, double *acc,
+                              double *jrk, double *pot, int *nnb, int *rowlen, cudaStream_t st);
 // batched clusters: tiles[k] = {slot0, nslots, first partial row, number of rows}
 cudaError_t launch_regf_merge_batch(const double *part, const int4 *tiles, int ntiles, int itile,
                                     const int *perm, const int *cnt, int nnbmax, double *acc,

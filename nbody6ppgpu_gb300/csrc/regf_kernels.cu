@@ -657,9 +657,9 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
         const int col = pcol0 + wi * 32 * IPT + k * 32 + lane;
 #pragma unroll
         for (int c = 0; c < NQ; ++c) {
-          const double v = (double)ffs[((0 * NQ + c) * IPT + k) * NT + tid] +
-                           (double)ffs[((1 * NQ + c) * IPT + k) * NT + tid];
-          out.part[((size_t)prow * NQ + c) * out.ni_pad + col] = v;
+          const float2 v = make_float2(ffs[((0 * NQ + c) * IPT + k) * NT + tid],
+                                       ffs[((1 * NQ + c) * IPT + k) * NT + tid]);
+          reinterpret_cast<float2 *>(out.part)[((size_t)prow * NQ + c) * out.ni_pad + col] = v;
         }
       }
     }
@@ -765,7 +765,40 @@ __device__ __forceinline__ void merge_store(const double *s, int i, const int *_
 }
 
 // Partial sums are stored by processing slot (column); the result of slot s
-// belongs to i = perm[s] (identity without a permutation).
+// belongs to i = perm[s] (identity without a permutation).  The split kernel
+// stores each partial as a float-float pair (hi, lo) in the 8-byte slot and
+// the merges add those pairs exactly-rounded on the FP32 pipe (FF); the FP64
+// kernel stores doubles, added in FP64.  Either way the order is fixed.
+template <bool FF>
+struct PartAcc {
+  double d[NQ];
+  float h[NQ], l[NQ];
+  __device__ __forceinline__ PartAcc() {
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) {
+      d[c] = 0.0;
+      h[c] = l[c] = 0.f;
+    }
+  }
+  // adds partial c, loaded as the 8 bytes of its slot (for FF the float
+  // pair (hi, lo) at the slot's low and high 4 bytes)
+  __device__ __forceinline__ void add_slot(int c, double v) {
+    if (FF) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+      ff_add(h[c], l[c], __int_as_float((int)(unsigned int)b), __int_as_float((int)(b >> 32)));
+    } else {
+      d[c] += v;
+    }
+  }
+  // adds the NQ partials of one split, entry c at p[c * stride]
+  __device__ __forceinline__ void add(const double *__restrict__ p, size_t stride) {
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) add_slot(c, p[c * stride]);
+  }
+  __device__ __forceinline__ double value(int c) const {
+    return FF ? (double)h[c] + (double)l[c] : d[c];
+  }
+};
 //
 // Many j-splits (small active blocks): one block of MERGE_THREADS per slot,
 // each thread summing a strided subset of the splits (four splits' loads in
@@ -773,6 +806,7 @@ __device__ __forceinline__ void merge_store(const double *s, int i, const int *_
 // so the order of the FP64 additions is the same in every run.
 constexpr int MERGE_THREADS = 128;
 constexpr int MERGE_UNROLL = 4;
+template <bool FF>
 __global__ void __launch_bounds__(MERGE_THREADS)
     regf_merge_wide_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
                            const int *__restrict__ perm, const int *__restrict__ cnt, int nnbmax,
@@ -781,10 +815,9 @@ __global__ void __launch_bounds__(MERGE_THREADS)
                            int *__restrict__ rowlen) {
   __shared__ double sh[NQ][MERGE_THREADS];
   const int slot = blockIdx.x, t = threadIdx.x;
-  double s[NQ];
-#pragma unroll
-  for (int c = 0; c < NQ; ++c) s[c] = 0.0;
+  PartAcc<FF> acc_t;
   for (int k0 = t; k0 < S; k0 += MERGE_THREADS * MERGE_UNROLL) {
+    // four splits' loads in flight, then added in split order
     double a[MERGE_UNROLL][NQ];
 #pragma unroll
     for (int u = 0; u < MERGE_UNROLL; ++u) {
@@ -796,10 +829,11 @@ __global__ void __launch_bounds__(MERGE_THREADS)
 #pragma unroll
     for (int u = 0; u < MERGE_UNROLL; ++u)
 #pragma unroll
-      for (int c = 0; c < NQ; ++c) s[c] += a[u][c];
+      for (int c = 0; c < NQ; ++c) acc_t.add_slot(c, a[u][c]);
   }
+  double s[NQ];
 #pragma unroll
-  for (int c = 0; c < NQ; ++c) sh[c][t] = s[c];
+  for (int c = 0; c < NQ; ++c) sh[c][t] = acc_t.value(c);
   __syncthreads();
   for (int w = MERGE_THREADS / 2; w > 0; w >>= 1) {
     if (t < w) {
@@ -821,6 +855,7 @@ __global__ void __launch_bounds__(MERGE_THREADS)
 // in warp order: the same FP64 order in every run, with MERGE_KW times the
 // memory parallelism of a thread per slot.
 constexpr int MERGE_KW = 8;
+template <bool FF>
 __global__ void __launch_bounds__(32 * MERGE_KW)
     regf_merge_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
                       const int *__restrict__ perm, const int *__restrict__ cnt, int nnbmax,
@@ -829,18 +864,14 @@ __global__ void __launch_bounds__(32 * MERGE_KW)
   __shared__ double sh[MERGE_KW][NQ][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int slot = blockIdx.x * 32 + lane;
+  PartAcc<FF> acc_t;
+  if (slot < ni) {
+    for (int k = w; k < S; k += MERGE_KW)
+      acc_t.add(part + (size_t)k * NQ * ni_pad + slot, (size_t)ni_pad);
+  }
   double s[NQ];
 #pragma unroll
-  for (int c = 0; c < NQ; ++c) s[c] = 0.0;
-  if (slot < ni) {
-    for (int k = w; k < S; k += MERGE_KW) {
-      const double *p = part + (size_t)k * NQ * ni_pad + slot;
-#pragma unroll
-      for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * ni_pad];
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < NQ; ++c) sh[w][c][lane] = s[c];
+  for (int c = 0; c < NQ; ++c) sh[w][c][lane] = acc_t.value(c);
   __syncthreads();
   if (w == 0 && slot < ni) {
 #pragma unroll
@@ -864,14 +895,12 @@ __global__ void regf_merge_batch_kernel(const double *__restrict__ part,
                                         int *__restrict__ rowlen) {
   const int4 td = tiles[blockIdx.x];   // slot0, nslots, row0, nrow
   for (int u = threadIdx.x; u < td.y; u += blockDim.x) {
+    PartAcc<true> acc_t;   // the batched pair is always the split kernel
+    for (int k = 0; k < td.w; ++k)
+      acc_t.add(part + (size_t)(td.z + k) * NQ * itile + u, (size_t)itile);
     double s[NQ];
 #pragma unroll
-    for (int c = 0; c < NQ; ++c) s[c] = 0.0;
-    for (int k = 0; k < td.w; ++k) {
-      const double *p = part + (size_t)(td.z + k) * NQ * itile + u;
-#pragma unroll
-      for (int c = 0; c < NQ; ++c) s[c] += p[(size_t)c * itile];
-    }
+    for (int c = 0; c < NQ; ++c) s[c] = acc_t.value(c);
     merge_store(s, perm[td.x + u], cnt, nnbmax, acc, jrk, pot, nnb, rowlen);
   }
 }
@@ -1226,18 +1255,29 @@ cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const IS
   return cudaGetLastError();
 }
 
-cudaError_t launch_regf_merge(const double *part, int S, int ni, int ni_pad, const int *perm,
-                              const int *cnt, int nnbmax, double *acc, double *jrk, double *pot,
-                              int *nnb, int *rowlen, cudaStream_t st) {
+cudaError_t launch_regf_merge(const double *part, bool ff, int S, int ni, int ni_pad,
+                              const int *perm, const int *cnt, int nnbmax, double *acc,
+                              double *jrk, double *pot, int *nnb, int *rowlen, cudaStream_t st) {
   // many splits of a small block: a block per i-slot (threads over splits);
   // otherwise a thread per i-slot, whose reads are coalesced across the warp
-  if (S >= 32 && ni < 8192)
-    regf_merge_wide_kernel<<<ni, MERGE_THREADS, 0, st>>>(part, S, ni, ni_pad, perm, cnt, nnbmax,
-                                                         acc, jrk, pot, nnb, rowlen);
-  else
-    regf_merge_kernel<<<(ni + 31) / 32, 32 * MERGE_KW, 0, st>>>(part, S, ni, ni_pad, perm, cnt,
-                                                                nnbmax, acc, jrk, pot, nnb,
-                                                                rowlen);
+  if (S >= 32 && ni < 8192) {
+    if (ff)
+      regf_merge_wide_kernel<true><<<ni, MERGE_THREADS, 0, st>>>(part, S, ni, ni_pad, perm, cnt,
+                                                                 nnbmax, acc, jrk, pot, nnb,
+                                                                 rowlen);
+    else
+      regf_merge_wide_kernel<false><<<ni, MERGE_THREADS, 0, st>>>(part, S, ni, ni_pad, perm, cnt,
+                                                                  nnbmax, acc, jrk, pot, nnb,
+                                                                  rowlen);
+  } else {
+    const int nb = (ni + 31) / 32;
+    if (ff)
+      regf_merge_kernel<true><<<nb, 32 * MERGE_KW, 0, st>>>(part, S, ni, ni_pad, perm, cnt,
+                                                            nnbmax, acc, jrk, pot, nnb, rowlen);
+    else
+      regf_merge_kernel<false><<<nb, 32 * MERGE_KW, 0, st>>>(part, S, ni, ni_pad, perm, cnt,
+                                                             nnbmax, acc, jrk, pot, nnb, rowlen);
+  }
   return cudaGetLastError();
 }
 
