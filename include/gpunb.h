@@ -83,7 +83,8 @@ void gpunb_clear_error(void);
 void gpunb_set_abort_on_error(int flag);    /* 1 (default): print + abort() */
 
 /* Pair kernel selection: 0 = split precision (FP32 arithmetic on double-single
- * positions, FP64 merges and neighbour re-tests; default), 1 = plain FP64. */
+ * positions, float-float merges and FP64 neighbour re-tests; default),
+ * 1 = plain FP64. */
 void gpunb_set_precision(int mode);
 
 /* Force a launch shape (variant index, j-splits); -1/0 restores the

@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(128) regf_fp64_kernel(const JSet js, const ISe
 }
 
 // ---------------------------------------------------------------------------
-// Merge of the S j-split partials in FP64, fixed order s = 0..S-1 (the
+// Merge of the S j-split partials, fixed order s = 0..S-1 (the
 // deterministic replacement of force_reduce_kernel + the host sum over GPUs,
 // gpunb.velocity.cu:441-496,822-845).  Also turns counts into the in-band
 // overflow flag of gpunb.velocity.cu:872-877 / reg.avx.cpp:320-321.
