@@ -26,7 +26,7 @@ import time
 import numpy as np
 
 from . import ics
-from .rsharness import Harness
+from .rsharness import PRED_BAND, Harness
 from .rsmlp import RSMLP
 
 
@@ -43,7 +43,7 @@ def make(model: str, n: int, seed: int, target: float, q: float = 0.5):
 
 
 def run(model="king", n=16384, ticks=64, nnbopt=100, nnbmax=200, levels=6, epochs=25,
-        train_seeds=(11, 12), eval_seed=13, q=0.5, rounds=1):
+        train_seeds=(11, 12), eval_seed=13, q=0.5, rounds=1, band=PRED_BAND):
     """rounds > 1: after the first fit, harvest again on the training seeds
     with the predictor in the loop (the states it leads to), add those pairs
     and refit -- the usual remedy for the shift between the plain rule's
@@ -54,7 +54,8 @@ def run(model="king", n=16384, ticks=64, nnbopt=100, nnbmax=200, levels=6, epoch
     for rnd in range(rounds):
         t0 = time.perf_counter()
         for s in train_seeds:
-            h = Harness(make(model, n, s, nnbopt, q), nnbopt, nnbmax, harvest=True, levels=levels)
+            h = Harness(make(model, n, s, nnbopt, q), nnbopt, nnbmax, harvest=True, levels=levels,
+                        band=band)
             h.run(ticks, predictor=mlp)
             x, y = h.dataset()
             h.close()
@@ -68,13 +69,14 @@ def run(model="king", n=16384, ticks=64, nnbopt=100, nnbmax=200, levels=6, epoch
     X = np.concatenate(X)
     Y = np.concatenate(Y)
     c = make(model, n, eval_seed, nnbopt, q)
-    out = {"model": model, "q": q, "n": n, "ticks": ticks, "rounds": rounds, "nnbopt": nnbopt,
+    out = {"model": model, "q": q, "n": n, "ticks": ticks, "rounds": rounds, "band": band,
+           "nnbopt": nnbopt,
            "nnbmax": nnbmax,
            "levels": levels, "train_pairs": int(len(X)), "label_variance": float(Y.var()),
            "train_mse_first_epoch": losses[0], "train_mse_last_epoch": losses[-1],
            "harvest_s": t_harvest, "train_s": t_train}
     for name, pred in (("plain", None), ("predictor", mlp)):
-        h = Harness(c, nnbopt, nnbmax, levels=levels)
+        h = Harness(c, nnbopt, nnbmax, levels=levels, band=band)
         s = h.run(ticks, predictor=pred).as_dict()
         h.close()
         out[name] = {k: s[k] for k in ("first_call_overflows", "overflow_events",
@@ -99,9 +101,11 @@ def main():
     ap.add_argument("--epochs", type=int, default=25)
     ap.add_argument("--rounds", type=int, default=1,
                     help="harvest rounds (later ones with the predictor in the loop)")
+    ap.add_argument("--band", type=float, nargs=2, default=PRED_BAND,
+                    help="accept a prediction whose implied count lies in [lo, hi] x target")
     a = ap.parse_args()
     print(json.dumps(run(a.model, a.n, a.ticks, a.nnbopt, a.nnbmax, a.levels, epochs=a.epochs,
-                         q=a.q, rounds=a.rounds)), flush=True)
+                         q=a.q, rounds=a.rounds, band=tuple(a.band))), flush=True)
 
 
 if __name__ == "__main__":

@@ -107,11 +107,19 @@ def label_log_radius(x: np.ndarray, v: np.ndarray, dtr: np.ndarray, idx: np.ndar
     return out
 
 
+# accepted range of the count a predicted radius implies at the current
+# density, as a multiple of the plain rule's target (the device update kernel
+# uses the same bounds)
+PRED_BAND = (0.25, 1.5)
+
+
 class Harness:
     def __init__(self, cluster: ics.Cluster, nnbopt: int, nnbmax: int, smax: float = 0.125,
                  levels: int = 4, params: rsrule.RSParams | None = None, rs=None,
-                 harvest: bool = False, rs0_factor: float = 1.0):
+                 harvest: bool = False, rs0_factor: float = 1.0,
+                 band: tuple[float, float] = PRED_BAND):
         self.c = cluster
+        self.band = band
         self.n = cluster.n
         self.nnbopt, self.nnbmax = nnbopt, nnbmax
         self.m = cluster.m.copy()
@@ -220,9 +228,13 @@ class Harness:
             y = predictor.predict(F)
             self.stats.predict_seconds += time.perf_counter() - t0
             # count implied at the predicted radius (local density unchanged);
-            # outside 0.5-1.5 x the rule's own target the plain rule is used
+            # outside band (default 0.25-1.5) x the rule's own target the plain
+            # rule is used.  The band is measured at the current density, so it
+            # reaches lower: in a contraction a correct prediction of a strong
+            # shrink implies a low count at today's density.
             pred_count = (nnb + 1.0) * np.exp(3.0 * y) - 1.0
-            ok = (pred_count >= 0.5 * target) & (pred_count <= 1.5 * target) & np.isfinite(y)
+            lo, hi = self.band
+            ok = (pred_count >= lo * target) & (pred_count <= hi * target) & np.isfinite(y)
             new = np.where(ok, rs_old * np.exp(y), plain)
             self.src[idx] = ok
             self.stats.predictor_used += int(ok.sum())

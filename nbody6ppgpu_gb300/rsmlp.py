@@ -7,7 +7,7 @@ neighbours at the particle's next regular step under the kernel's membership
 test (position or predicted position inside RS), k the membership the plain
 rule aims at (src/Main/regcor_gpu.F:152-163).  It never touches forces: its
 output replaces the plain RS rule (regcor_gpu.F:146-253) only when the count
-it implies stays within 0.5-1.5 x that target; otherwise, and after any list
+it implies stays within 0.25-1.5 x that target; otherwise, and after any list
 overflow, the plain rules of `rsrule` apply.
 
 Features (per active particle, before its RS is updated):

@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 from nbody6ppgpu_gb300 import rsrule
+from nbody6ppgpu_gb300.rsharness import PRED_BAND
 
 pytestmark = pytest.mark.gpu
 
@@ -59,10 +60,11 @@ def test_fused_predictor_matches_host_path():
     plain = np.where(nnb < 2, rsrule.few_nb_rs(rs), plain)
     y = mlp.predict(F)
     pc = (np.maximum(nnb, 0) + 1.0) * np.exp(3.0 * y.astype(np.float64)) - 1.0
-    ok = (pc >= 0.5 * tgt) & (pc <= 1.5 * tgt) & np.isfinite(y)
+    lo, hi = PRED_BAND
+    ok = (pc >= lo * tgt) & (pc <= hi * tgt) & np.isfinite(y)
     want = np.where(ok, rs * np.exp(y.astype(np.float64)), plain)
     got, gtgt, used = rs_update_device(p, x, v, m, rs, nnb, nnb0, acc, jrk, dtr, mlp=mlp)
-    edge = (np.abs(pc - 0.5 * tgt) < 1e-4 * tgt) | (np.abs(pc - 1.5 * tgt) < 1e-4 * tgt)
+    edge = (np.abs(pc - lo * tgt) < 1e-4 * tgt) | (np.abs(pc - hi * tgt) < 1e-4 * tgt)
     assert np.array_equal(used.astype(bool)[~edge], ok[~edge])
     assert ok.sum() > 100 and (~ok).sum() > 100       # both branches exercised
     sel = ~edge
