@@ -141,7 +141,7 @@ def test_predictor_cuts_overflow_recomputes():
     rise faster than the plain rule's 25%-per-step volume limit follows and
     lists overflow.  The predictor, trained on pairs harvested from two other
     seeds with the plain rule, is run on a third seed from the same state:
-    it must need several times fewer overflow recomputes at the same mean
+    it must need at least 5x fewer overflow recomputes at the same mean
     membership."""
     pytest.importorskip("scipy")
     from nbody6ppgpu_gb300.rs_experiment import run
@@ -149,7 +149,7 @@ def test_predictor_cuts_overflow_recomputes():
             rounds=1, q=0.1)
     plain, pred = r["plain"], r["predictor"]
     assert plain["overflow_events"] >= 200            # the regime does overflow
-    assert pred["overflow_events"] * 3 <= plain["overflow_events"]
+    assert pred["overflow_events"] * 5 <= plain["overflow_events"]   # measured 17x
     assert abs(pred["mean_count"] / plain["mean_count"] - 1.0) < 0.1
     assert pred["count_p99"] <= plain["count_p99"]
     assert pred["predictor_used"] > 0.9 * pred["active"]
