@@ -234,7 +234,8 @@ int gpunb_rsmlp_adam(float *wf, float *m1, float *m2, const float *grad, float l
  * fpoly0.F:153-158 for counts below 2 when few_nb_rule), and, when wq is not
  * NULL, the MLP proposal from the 8 features of each particle normalised by
  * norm[0..7] (mean) and norm[8..15] (spread), taken where the count it implies
- * at the current density stays within 0.25-1.5 x the rule's target.  Inputs per
+ * at the current density stays within [band_lo, band_hi] x the rule's target
+ * (0.5-1.5 when the fields are 0).  Inputs per
  * active particle i < ni: x, v ([ni][3]), m_scaled (mass x N), rs, nnb (count,
  * self excluded), nnb0 (previous count), acc, jrk ([ni][3], regular force and
  * derivative; only read with wq), dtr.  Outputs rs_new[ni], and when not NULL
@@ -247,6 +248,7 @@ typedef struct {
   double rscale, rc, rsfac; /* RSCALE, RC, RSFAC */
   double bodym;             /* mean mass */
   double rdens[3];          /* density centre RDENS */
+  double band_lo, band_hi;  /* acceptance band of the MLP proposal (0: 0.5, 1.5) */
 } gpunb_rs_params;
 int gpunb_rs_update_device(int ni, const gpunb_rs_params *p, const double *x, const double *v,
                            const double *m_scaled, const double *rs, const int *nnb,

@@ -100,7 +100,8 @@ __global__ void __launch_bounds__(MLP_THREADS)
 // shell square root, inward reduction; the zero-neighbour branch :120-143),
 // optionally the few-member rule of fpoly0.F:153-158, and -- with weights --
 // the learned proposal: features, MLP, and the plain rule as fallback when the
-// count it implies at the current density leaves 0.25-1.5 x the rule's target.
+// count it implies at the current density leaves the band (default 0.5-1.5 x
+// the rule's target).
 __device__ void rs_plain(const gpunb_rs_params &p, double rs, int nnb, int nnb0,
                          const double *x, const double *v, double dtr, double &out,
                          double &target) {
@@ -194,7 +195,9 @@ __global__ void __launch_bounds__(MLP_THREADS)
       xf[q] = (float)((f[q] - (double)norm[q]) / (double)norm[MLP_IN + q]);
     const float y = mlp_eval(s, xf);
     const double pc = (nn + 1.0) * exp(3.0 * (double)y) - 1.0;
-    if (isfinite(y) && pc >= 0.25 * tgt && pc <= 1.5 * tgt) {
+    const double blo = p.band_lo > 0.0 ? p.band_lo : 0.5;
+    const double bhi = p.band_hi > 0.0 ? p.band_hi : 1.5;
+    if (isfinite(y) && pc >= blo * tgt && pc <= bhi * tgt) {
       nw = r0 * exp((double)y);
       u = 1;
     }

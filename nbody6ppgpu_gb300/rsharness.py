@@ -109,8 +109,11 @@ def label_log_radius(x: np.ndarray, v: np.ndarray, dtr: np.ndarray, idx: np.ndar
 
 # accepted range of the count a predicted radius implies at the current
 # density, as a multiple of the plain rule's target (the device update kernel
-# uses the same bounds)
-PRED_BAND = (0.25, 1.5)
+# takes the same bounds): 0.5-1.5 by default; WIDE_BAND lowers the floor so
+# that in a contraction a correct prediction of a strong shrink, which implies
+# a low count at today's density, is not rejected
+PRED_BAND = (0.5, 1.5)
+WIDE_BAND = (0.25, 1.5)
 
 
 class Harness:
@@ -228,10 +231,7 @@ class Harness:
             y = predictor.predict(F)
             self.stats.predict_seconds += time.perf_counter() - t0
             # count implied at the predicted radius (local density unchanged);
-            # outside band (default 0.25-1.5) x the rule's own target the plain
-            # rule is used.  The band is measured at the current density, so it
-            # reaches lower: in a contraction a correct prediction of a strong
-            # shrink implies a low count at today's density.
+            # outside band x the rule's own target the plain rule is used
             pred_count = (nnb + 1.0) * np.exp(3.0 * y) - 1.0
             lo, hi = self.band
             ok = (pred_count >= lo * target) & (pred_count <= hi * target) & np.isfinite(y)

@@ -7,7 +7,7 @@ neighbours at the particle's next regular step under the kernel's membership
 test (position or predicted position inside RS), k the membership the plain
 rule aims at (src/Main/regcor_gpu.F:152-163).  It never touches forces: its
 output replaces the plain RS rule (regcor_gpu.F:146-253) only when the count
-it implies stays within 0.25-1.5 x that target; otherwise, and after any list
+it implies stays within 0.5-1.5 x that target (the band is a parameter); otherwise, and after any list
 overflow, the plain rules of `rsrule` apply.
 
 Features (per active particle, before its RS is updated):
@@ -198,15 +198,17 @@ class RSParamsC(C.Structure):
     """gpunb_rs_params (include/gpunb.h)."""
     _fields_ = [("nnbopt", C.c_int), ("nnbmax", C.c_int), ("nb_flag", C.c_int),
                 ("few_nb_rule", C.c_int), ("rscale", C.c_double), ("rc", C.c_double),
-                ("rsfac", C.c_double), ("bodym", C.c_double), ("rdens", C.c_double * 3)]
+                ("rsfac", C.c_double), ("bodym", C.c_double), ("rdens", C.c_double * 3),
+                ("band_lo", C.c_double), ("band_hi", C.c_double)]
 
 
 def rs_update_device(p, x, v, m_scaled, rs, nnb, nnb0, acc, jrk, dtr, mlp: "RSMLP | None" = None,
-                     few_nb_rule: bool = True, device: int = 0):
+                     few_nb_rule: bool = True, device: int = 0, band=(0.5, 1.5)):
     """gpunb_rs_update_device on host arrays (copied to the device and back):
     the plain RS rule of `rsrule.regcor_rs` (with the few-member rule when
     few_nb_rule) and, with `mlp`, the learned proposal and its fallback, in
-    one kernel.  p: rsrule.RSParams.  Returns (rs_new, target, used)."""
+    one kernel.  p: rsrule.RSParams; band: acceptance band of the proposal.
+    Returns (rs_new, target, used)."""
     import torch
     lib = load()
     fn = lib.gpunb_rs_update_device
@@ -220,7 +222,7 @@ def rs_update_device(p, x, v, m_scaled, rs, nnb, nnb0, acc, jrk, dtr, mlp: "RSML
 
     cp = RSParamsC(int(p.nnbopt), int(p.nnbmax), int(p.nb_flag), int(few_nb_rule),
                    float(p.rscale), float(p.rc), float(p.rsfac), float(p.bodym),
-                   (C.c_double * 3)(0.0, 0.0, 0.0))
+                   (C.c_double * 3)(0.0, 0.0, 0.0), float(band[0]), float(band[1]))
     X, V, M, R = d(x), d(v), d(m_scaled), d(rs)
     NB, NB0 = d(nnb, torch.int32), d(nnb0, torch.int32)
     A, J, DT = d(acc), d(jrk), d(dtr)

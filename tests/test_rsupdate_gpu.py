@@ -63,7 +63,8 @@ def test_fused_predictor_matches_host_path():
     lo, hi = PRED_BAND
     ok = (pc >= lo * tgt) & (pc <= hi * tgt) & np.isfinite(y)
     want = np.where(ok, rs * np.exp(y.astype(np.float64)), plain)
-    got, gtgt, used = rs_update_device(p, x, v, m, rs, nnb, nnb0, acc, jrk, dtr, mlp=mlp)
+    got, gtgt, used = rs_update_device(p, x, v, m, rs, nnb, nnb0, acc, jrk, dtr, mlp=mlp,
+                                       band=PRED_BAND)
     edge = (np.abs(pc - lo * tgt) < 1e-4 * tgt) | (np.abs(pc - hi * tgt) < 1e-4 * tgt)
     assert np.array_equal(used.astype(bool)[~edge], ok[~edge])
     assert ok.sum() > 100 and (~ok).sum() > 100       # both branches exercised
