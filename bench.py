@@ -172,10 +172,10 @@ def cpu_side_checks(c, irr_check=None, pot_result=None):
     return out
 
 
-def cpu_baseline(c, acts, budget_s: float = 10.0):
+def cpu_baseline(c, acts, sample_s: float = 10.0):
     """The portable FP32 restatement of the reference CPU path (OpenMP, all
     host cores) on whole steps of the same workload, as many as fit in
-    about budget_s (at least one)."""
+    about sample_s (at least one)."""
     from oracle import oracle as O
     port = O.Port()
     h2 = c.h2()
@@ -189,7 +189,7 @@ def cpu_baseline(c, acts, budget_s: float = 10.0):
             port.regf(h2[a], c.dtr[a], c.x[a], c.v[a], LMAX, NNBMAX)
             pairs += ni * N
         steps += 1
-        if time.perf_counter() - t0 > budget_s or steps >= 20:
+        if time.perf_counter() - t0 > sample_s or steps >= 20:
             break
     dt = time.perf_counter() - t0
     return {"value": pairs / dt / 1e9, "unit": "Gpairs/s", "cores": O.num_threads(),

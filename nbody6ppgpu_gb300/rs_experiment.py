@@ -3,7 +3,7 @@ predictor with the plain rule as fallback.
 
     python -m nbody6ppgpu_gb300.rs_experiment --n 16384 --ticks 64 --model king
 
-1. Harvest (features, label) pairs by running the regular-step driver with the
+1. Harvest (features, label) pairs by running the regular-step harness with the
    plain rule on two seeded clusters (the pairs the integrator itself
    generates); train the MLP on the GPU kernels (Adam, FP32 master, BF16
    weights).

@@ -1,4 +1,4 @@
-"""Regular-step driver for the neighbour-radius experiments.
+"""Regular-step harness for the neighbour-radius experiments.
 
 Drives libgpunb.so the way NBODY6++'s regular section does (intgrt.F:912-944,
 util_gpu.F:33-116): every tick the whole j-set is sent, the particles whose

@@ -1,6 +1,6 @@
 """The RS update on the device (gpunb_rs_update_device): the plain rule
 against rsrule.regcor_rs (itself checked against hand-worked cases of the
-Fortran), and the fused MLP proposal against the host path of the driver
+Fortran), and the fused MLP proposal against the host path of the harness
 (features -> forward kernel -> band check -> fallback)."""
 import numpy as np
 import pytest
