@@ -135,6 +135,16 @@ int gpunb_send_device(int nj, const double *m, const double *x, const double *v,
  * records a nonzero code as the calls on host arrays do, and clears the
  * word.  The host-array calls clear it when they start. */
 int gpunb_device_status(void *stream);
+
+/* Test support for the failure paths (no reference counterpart; neither
+ * faults nor hangs the device).  gpunb_test_bounded_wait queues one thread
+ * that waits, at most `polls` polls, on an mbarrier that nothing completes,
+ * then records GPUNB_E_TIMEOUT in the device error word as the library's
+ * kernels do when a bounded wait gives up (read it with
+ * gpunb_device_status); the context stays usable.  gpunb_test_fail_allocs
+ * makes the next n device-buffer allocations report GPUNB_E_ALLOC. */
+int gpunb_test_bounded_wait(int polls, void *stream);
+void gpunb_test_fail_allocs(int n);
 int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double *xi,
                       const double *vi, double *acc, double *jrk, double *pot, int *nnb,
                       int *list_off, int *list, size_t list_cap, int nnbmax, int m_flag,

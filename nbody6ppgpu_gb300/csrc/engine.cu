@@ -74,6 +74,8 @@ static double wtime() {
 // Incremented whenever a device buffer moves: captured CUDA graphs hold raw
 // addresses and are replayed only while this count is unchanged.
 static unsigned long long g_alloc_gen = 0;
+// gpunb_test_fail_allocs: the next n device allocations report failure
+static int g_fail_allocs = 0;
 
 struct DevBuf {
   void *p = nullptr;
@@ -85,6 +87,11 @@ struct DevBuf {
     bytes = 0;
     ++g_alloc_gen;
     size_t want = n + n / 4 + 256;
+    if (g_fail_allocs > 0) {
+      --g_fail_allocs;
+      fail(GPUNB_E_ALLOC, "cudaMalloc of %zu bytes failed (test hook)", want);
+      return false;
+    }
     if (cudaMalloc(&p, want) != cudaSuccess) {
       cudaGetLastError();
       fail(GPUNB_E_ALLOC, "cudaMalloc of %zu bytes failed", want);
@@ -1218,6 +1225,36 @@ int gpunb_send_device(int nj, const double *m, const double *x, const double *v,
     rc = issue(st);
   if (rc == GPUNB_OK) g.nj = nj;
   return rc;
+}
+
+// A wait that nothing completes: one thread polls an mbarrier that no copy or
+// arrival will ever complete, at most `polls` times, then records a timeout
+// the way the library's kernels do when a bounded wait gives up.
+__global__ void bounded_wait_probe_kernel(unsigned int polls, int *err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    if (!mbar_wait_bounded(&bar, 0u, polls)) raise_error(err, GPUNB_E_TIMEOUT);
+  }
+}
+
+int gpunb_test_bounded_wait(int polls, void *stream) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  if (!devinit(0)) return GPUNB_E_NO_DEVICE;
+  if (polls < 1 || polls > (1 << 22)) {
+    fail(GPUNB_E_ARG, "gpunb_test_bounded_wait: polls %d outside [1, 2^22]", polls);
+    return GPUNB_E_ARG;
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  bounded_wait_probe_kernel<<<1, 32, 0, st>>>((unsigned int)polls, g.err.as<int>());
+  CUDA_OR(cudaGetLastError(), GPUNB_E_CUDA);
+  return GPUNB_OK;
+}
+
+void gpunb_test_fail_allocs(int n) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  g_fail_allocs = n > 0 ? n : 0;
 }
 
 int gpunb_device_status(void *stream) {

@@ -88,6 +88,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "gpunb_batch_last_plan": ([ip, ip], C.c_int),
         "gpunb_set_graphs": ([C.c_int], None),
         "gpunb_device_status": ([C.c_void_p], C.c_int),
+        "gpunb_test_bounded_wait": ([C.c_int, C.c_void_p], C.c_int),
+        "gpunb_test_fail_allocs": ([C.c_int], None),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

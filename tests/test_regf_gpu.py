@@ -185,6 +185,40 @@ def test_errors_are_reported(lib):
         assert np.all(np.isfinite(r.acc))
 
 
+def test_bounded_wait_gives_up_and_the_context_stays_usable(lib):
+    """A device wait that nothing completes gives up after its poll limit and
+    records GPUNB_E_TIMEOUT; the host reads it and the next calls work."""
+    g = load_golden("plummer2048_equal")
+    lib.gpunb_clear_error()
+    with GpuNb(len(g["m"])):
+        assert lib.gpunb_test_bounded_wait(1000, None) == 0
+        assert lib.gpunb_device_status(None) == 6           # GPUNB_E_TIMEOUT
+        lib.gpunb_clear_error()
+        assert lib.gpunb_device_status(None) == 0
+    res = run_golden(g)
+    assert rows_equal(res.list, unpack_list(g["fp64_cnt"], g["fp64_ids"], int(g["lmax"]))) == []
+    check_forces(res, g["fp64_acc"], g["fp64_jrk"], g["fp64_pot"])
+
+
+def test_allocation_failure_is_reported_and_recovered(lib):
+    g = load_golden("plummer2048_equal")
+    lib.gpunb_clear_error()
+    with GpuNb(len(g["m"])) as nb:
+        lib.gpunb_test_fail_allocs(1)          # the first send's tile buffer
+        try:
+            with pytest.raises(GpunbError) as e:
+                nb.send(g["m"], g["x"], g["v"])
+            assert e.value.code == 8
+        finally:
+            lib.gpunb_test_fail_allocs(0)
+        nb.send(g["m"], g["x"], g["v"])
+        ii = g["ii"]
+        res = nb.regf(g["h2"], g["dtr"], g["x"][ii], g["v"][ii], int(g["lmax"]),
+                      int(g["nnbmax"]), int(g["m_flag"]))
+    assert rows_equal(res.list, unpack_list(g["fp64_cnt"], g["fp64_ids"], int(g["lmax"]))) == []
+    check_forces(res, g["fp64_acc"], g["fp64_jrk"], g["fp64_pot"])
+
+
 def test_gpupot_golden(lib):
     g = load_golden("pot_plummer2048")
     p = gpupot(g["m"], g["x"])
