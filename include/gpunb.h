@@ -65,7 +65,8 @@ void gpunb_profile_(int *irank);
 
 /* Potential for the energy check: pot[k] = sum_{j: r2 > 0} m_j / r_ij for
  * i = istart-1+k, k < ni, over n bodies (reference: gpupot_,
- * src/Main/gpupot.gpu.cu:61-127; CPU src/Main/pot.avx.cpp:72-159). */
+ * src/Main/gpupot.gpu.cu:61-127; CPU src/Main/pot.avx.cpp:72-159).  Bodies
+ * closer than 1e-19 (r2 below 2^-126) count as coincident. */
 void gpupot_(int *irank, int *istart, int *ni, int *n, double m[], double x[][3],
              double pot[]);
 
