@@ -143,7 +143,8 @@ int gpunb_device_status(void *stream);
  * then records GPUNB_E_TIMEOUT in the device error word as the library's
  * kernels do when a bounded wait gives up (read it with
  * gpunb_device_status); the context stays usable.  gpunb_test_fail_allocs
- * makes the next n device-buffer allocations report GPUNB_E_ALLOC. */
+ * makes the next n device-buffer allocations of the regular-force library
+ * state report GPUNB_E_ALLOC. */
 int gpunb_test_bounded_wait(int polls, void *stream);
 void gpunb_test_fail_allocs(int n);
 int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double *xi,
