@@ -1,7 +1,7 @@
 """One regular-force block on a seeded cluster, through the host ABI: the
 case the kernel profiles are taken on.
 
-    python -m nbody6ppgpu_gb300.cases --model plummer --n 65536 --ni 65536 --reps 4
+    python -m experiments.cases --model plummer --n 65536 --ni 65536 --reps 4
 
 Sends the j-set once and calls gpunb_regf_ `reps` times on the same active
 set (the first call warms the library up; a profiler is pointed at a later
@@ -12,8 +12,8 @@ from __future__ import annotations
 
 import argparse
 
-from . import ics
-from .gpunb import GpuNb
+from nbody6ppgpu_gb300 import ics
+from nbody6ppgpu_gb300.gpunb import GpuNb
 
 
 def main():

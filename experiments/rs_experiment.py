@@ -1,7 +1,7 @@
 """Neighbour-radius experiment: the plain RS rule against the learned
 predictor with the plain rule as fallback.
 
-    python -m nbody6ppgpu_gb300.rs_experiment --n 16384 --ticks 64 --model king
+    python -m experiments.rs_experiment --n 16384 --ticks 64 --model king
 
 1. Harvest (features, label) pairs by running the regular-step harness with the
    plain rule on two seeded clusters (the pairs the integrator itself
@@ -25,9 +25,9 @@ import time
 
 import numpy as np
 
-from . import ics
-from .rsharness import PRED_BAND, Harness
-from .rsmlp import RSMLP
+from nbody6ppgpu_gb300 import ics
+from nbody6ppgpu_gb300.rsharness import PRED_BAND, Harness
+from nbody6ppgpu_gb300.rsmlp import RSMLP
 
 
 def make(model: str, n: int, seed: int, target: float, q: float = 0.5):

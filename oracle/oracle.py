@@ -27,13 +27,13 @@ _I = C.POINTER(C.c_int)
 _lib = None
 
 
-def build(ref: bool = False) -> None:
-    """make liboracle.so (and the reference AVX libraries when ref=True and
-    the reference sources are present)."""
+def build(ref_dir: str | os.PathLike | None = None) -> None:
+    """make liboracle.so, and the reference AVX libraries when ref_dir names
+    the reference's source tree (x86_64 hosts only)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
-    if ref and platform.machine() == "x86_64" and Path(os.environ.get(
-            "REF", "/root/reference")).joinpath("src/Main/reg.avx.cpp").exists():
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True,
+    if ref_dir and platform.machine() == "x86_64" and Path(ref_dir).joinpath(
+            "src/Main/reg.avx.cpp").exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={ref_dir}"], check=True,
                        capture_output=True)
 
 
@@ -97,6 +97,51 @@ def pot_fp64(m, x, istart=1, ni=None):
     pot = np.empty(ni)
     lib().oracle_pot_fp64(int(istart), int(ni), n, _dp(m), _dp(x), _dp(pot))
     return pot
+
+
+# ---------------------------------------------------------------------------
+# Parity bound of the split-precision regular force (the FP64 oracle as truth).
+#
+# A regular force or jerk is a sum of N pair terms q_ij.  FP32 arithmetic
+# errs per term by a few units of 2^-24 of |q_ij|, so the error of the sum
+# scales with S_i = sum_j |q_ij|, not with |Q_i|: for a particle whose terms
+# cancel (kappa_i = S_i / |Q_i| large) the plain relative error grows with
+# kappa_i whatever the FP32 formulation.  The bound therefore measures each
+# particle against max(|Q_i|, S_i / KAPPA0): the plain relative error
+# wherever the sum cancels by less than KAPPA0, and 1e-6 S_i / KAPPA0 for a
+# residue of stronger cancellation.  The potential (all terms positive) is
+# held to the plain relative error.
+SPLIT_TOL = 1e-6
+KAPPA0 = 8.0
+
+
+def parity_errors(acc, jrk, pot, ref_acc, ref_jrk, ref_pot, accabs, jrkabs) -> dict:
+    """Per-particle errors of (acc, jrk, pot) against the FP64 oracle's
+    (ref_acc, ref_jrk, ref_pot) with its term sums accabs, jrkabs (the
+    with_abs outputs of regf_fp64).  Returns the plain relative maxima and
+    99th percentiles, the cancellation-aware maxima (the bound), the maxima
+    normalised by S_i, and the particles above SPLIT_TOL in plain terms with
+    the smallest cancellation ratio among them."""
+    acc, jrk, ref_acc, ref_jrk = (np.asarray(a, dtype=np.float64).reshape(-1, 3)
+                                  for a in (acc, jrk, ref_acc, ref_jrk))
+    pot, ref_pot, accabs, jrkabs = (np.asarray(a, dtype=np.float64).ravel()
+                                    for a in (pot, ref_pot, accabs, jrkabs))
+    out = {"n": int(acc.shape[0]), "kappa0": KAPPA0}
+    for name, got, ref, s in (("acc", acc, ref_acc, accabs), ("jrk", jrk, ref_jrk, jrkabs)):
+        d = np.linalg.norm(got - ref, axis=1)
+        q = np.linalg.norm(ref, axis=1)
+        rel = d / np.maximum(q, 1e-300)
+        kap = s / np.maximum(q, 1e-300)
+        bound = d / np.maximum(np.maximum(q, s / KAPPA0), 1e-300)
+        above = rel > SPLIT_TOL
+        out[name] = {"max": float(rel.max()), "p99": float(np.percentile(rel, 99)),
+                     "bound_max": float(bound.max()),
+                     "sum_norm_max": float((d / np.maximum(s, 1e-300)).max()),
+                     "above_tol": int(above.sum()),
+                     "min_kappa_above_tol": float(kap[above].min()) if above.any() else None}
+    ep = np.abs(pot - ref_pot) / np.maximum(np.abs(ref_pot), 1e-300)
+    out["pot"] = {"max": float(ep.max()), "p99": float(np.percentile(ep, 99))}
+    return out
 
 
 class Port:

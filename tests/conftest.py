@@ -43,3 +43,20 @@ def rows_equal(a, b):
 
 def rel_vec_err(a, b):
     return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+
+
+def check_split(acc, jrk, pot, ref_acc, ref_jrk, ref_pot, accabs, jrkabs, ok=None):
+    """The split-precision parity bound (oracle.parity_errors): per particle,
+    force and jerk within 1e-6 of max(|Q_i|, S_i / KAPPA0), the potential
+    within 1e-6 relative, and the plain relative errors of force and jerk
+    within 1e-6 at the 99th percentile.  ok selects rows (accepted lists)."""
+    from oracle import oracle as O
+    if ok is not None:
+        acc, jrk, pot, ref_acc, ref_jrk, ref_pot, accabs, jrkabs = (
+            np.asarray(a)[ok] for a in (acc, jrk, pot, ref_acc, ref_jrk, ref_pot, accabs, jrkabs))
+    e = O.parity_errors(acc, jrk, pot, ref_acc, ref_jrk, ref_pot, accabs, jrkabs)
+    for q in ("acc", "jrk"):
+        assert e[q]["bound_max"] <= O.SPLIT_TOL, (q, e[q])
+        assert e[q]["p99"] <= O.SPLIT_TOL, (q, e[q])
+    assert e["pot"]["max"] <= O.SPLIT_TOL, e["pot"]
+    return e

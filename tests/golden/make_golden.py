@@ -11,6 +11,7 @@ any host, without the reference present.
 """
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
@@ -49,7 +50,8 @@ def regf_case(name, m, x, v, h2, dtr, ii, lmax, nnbmax, m_flag, ref):
 
 
 def main():
-    O.build(ref=True)
+    # the reference's source tree: $NBODY6PP_REFERENCE, else /root/reference
+    O.build(ref_dir=os.environ.get("NBODY6PP_REFERENCE", "/root/reference"))
     if not O.RefAVX.available():
         raise SystemExit("reference AVX library not available (needs x86_64 and the sources)")
     ref = O.RefAVX(1 << 16)

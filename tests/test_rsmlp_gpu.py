@@ -144,7 +144,7 @@ def test_predictor_cuts_overflow_recomputes():
     it must need at least 5x fewer overflow recomputes at the same mean
     membership."""
     pytest.importorskip("scipy")
-    from nbody6ppgpu_gb300.rs_experiment import run
+    from experiments.rs_experiment import run
     r = run(model="king", n=8192, ticks=256, nnbopt=100, nnbmax=200, levels=6, epochs=25,
             rounds=1, q=0.1)
     plain, pred = r["plain"], r["predictor"]
