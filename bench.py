@@ -37,8 +37,25 @@ NB_TARGET = 100.0
 NNBMAX = 512
 LMAX = NNBMAX + 1
 FLOPS_PER_PAIR = 60          # the reference's convention (gpunb.velocity.cu:894)
+RESORT_EVERY = 8             # j-set re-ordered on every 8th send (the library's default)
 METRIC = "regular force+jerk+NB Gpairs/s on 1 GB300: split-FP32 vs FP64 at rel.err<=1e-6"
 WORKLOAD = "plummer65536_kroupa_blocks_1_32_1024_16384_65536"
+
+
+def _jsonable(o):
+    """numpy scalars and arrays in the bench line as plain JSON values"""
+    if isinstance(o, np.generic):
+        return o.item()
+    if isinstance(o, np.ndarray):
+        return o.tolist()
+    raise TypeError(f"not JSON serialisable: {type(o).__name__}")
+
+
+def config(ws: int = 1) -> dict:
+    """The workload's config, identical in both arms of the bench."""
+    return {"workload": WORKLOAD, "N": N, "blocks": BLOCKS, "nb_target": NB_TARGET,
+            "nnbmax": NNBMAX, "l2": "flushed (256 MB write) between timed steps",
+            "parallelism": f"replicas x{ws}"}
 
 
 def make_inputs(seed: int = 2):
@@ -139,6 +156,25 @@ def read_traffic():
 
 
 # --------------------------------------------------------------------------
+def oracle_parity(name, m, x, v, h2, dtr, act, got, lmax, nnbmax, rows=512):
+    """Sampled rows of a split-precision block against the FP64 oracle:
+    the named bound of oracle.parity_errors (force and jerk against
+    max(|Q|, sum|q|/8), potential relative) next to the plain relative
+    maxima and 99th percentiles."""
+    from oracle import oracle as O
+    acc, jrk, pot = got
+    samp = np.linspace(0, len(act) - 1, min(rows, len(act))).astype(int)
+    a = act[samp]
+    oa, oj, op, lst, aa, ja = O.regf_fp64(m, x, v, h2[a], dtr[a], x[a], v[a], lmax, nnbmax,
+                                          with_abs=True)
+    ok = lst[:, 0] >= 0
+    e = O.parity_errors(acc[samp][ok], jrk[samp][ok], pot[samp][ok], oa[ok], oj[ok], op[ok],
+                        aa[ok], ja[ok])
+    e["block"] = name
+    e["rows_sampled"] = int(ok.sum())
+    return e
+
+
 def cpu_side_checks(c, irr_check=None, pot_result=None):
     """The CPU-baseline leg's work for the side legs: the irregular force of
     the FP64 oracle (timed, and the GPU block checked against it) and the
@@ -227,8 +263,9 @@ def run_reference(args, ws, rank):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Plummer/Kroupa)",
-            "config": {"workload": WORKLOAD, "N": N, "blocks": BLOCKS, "nnbmax": NNBMAX,
-                       "host_threads": O.num_threads()},
+            "config": config(args.gpus),
+            "impl_detail": {"host_threads": O.num_threads(),
+                            "code": "FP32 restatement of src/Main/reg.avx.cpp (OpenMP)"},
             "cpu_baseline": {"value": v, "unit": "Gpairs/s", "cores": O.num_threads(),
                              "kind": "port",
                              "sample": "every step = the full workload step on the host cores "
@@ -236,7 +273,7 @@ def run_reference(args, ws, rank):
                                        "source does not build on the aarch64 host)"},
             "e2e": {"value": v, "unit": "Gpairs/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line, default=_jsonable), flush=True)
     return 0
 
 
@@ -310,12 +347,27 @@ def batched_leg(lib, dev, stream, steps: int, warmup: int):
             "speedup_over_sequential": seq_ms / batched_ms}
 
 
-def king1m_leg(n_sm: int, peak_mhz: float):
-    """King W0 = 6, N = 2^20, Kroupa masses with 10% binaries as c.m. bodies,
-    RS for a mean of 100 neighbours, nbmax 1024: the split kernel at
-    ni in {1024, 16384, 262144, N} (host ABI, kernel time from the library's
-    CUDA events), the FP64 kernel at ni = 16384, and the split results against
-    the FP64 ones on that block."""
+KING_BLOCKS = [1024, 16384, 262144, 1 << 20]
+KING_NNBMAX = 1024
+
+
+def king1m_leg(lib, dev, stream, n_sm: int, peak_mhz: float, steps: int = 2, warmup: int = 2):
+    """The spec configuration as a full regular step: King W0 = 6,
+    N = 2^20, Kroupa masses with 10% binaries as c.m. bodies, RS for a mean of
+    100 neighbours, nbmax 1024; one step = send + regf for each block
+    ni in {1024, 16384, 262144, N} (1.39e12 pairs).
+      step      device-resident (gpunb_send_device + gpunb_regf_device on the
+                timed stream, calls replayed as CUDA graphs), CUDA events per
+                step, clocks sampled during the timed steps;
+      e2e       the same step through gpunb_send_ / gpunb_regf_ with host
+                arrays (copies and LISTGP rows included), wall clock;
+      blocks    pair-kernel time of each block (library CUDA events) and its
+                fraction of the FP32 peak: the roofline at ni = N;
+      fp64      the FP64 kernel on the ni = 16384 block.
+    Returns the line entry and what the oracle leg needs (the split results
+    of the 16384 block for the parity check, the 1024 block for the CPU
+    port's timing)."""
+    import torch
     from nbody6ppgpu_gb300 import ics
     from nbody6ppgpu_gb300.gpunb import GpuNb
     t0 = time.perf_counter()
@@ -324,43 +376,155 @@ def king1m_leg(n_sm: int, peak_mhz: float):
     n = k.n
     h2 = k.h2()
     peak = fp32_peak_tflops(n_sm, peak_mhz)
-    blocks = {}
-    ref = None
+    acts = {ni: ics.active_set(n, ni, seed=ni) for ni in KING_BLOCKS}
+    pairs = n * sum(KING_BLOCKS)
+    sp = stream.cuda_stream
+
+    def T(a, dt=torch.float64):
+        return torch.as_tensor(np.ascontiguousarray(a)).to(dev, dtype=dt)
+
+    jm, jx, jv = T(k.m), T(k.x), T(k.v)
+    blk = {}
+    for ni in KING_BLOCKS:
+        a = acts[ni]
+        blk[ni] = dict(h2=T(h2[a]), dtr=T(k.dtr[a]), x=T(k.x[a]), v=T(k.v[a]),
+                       acc=torch.empty((ni, 3), dtype=torch.float64, device=dev),
+                       jrk=torch.empty((ni, 3), dtype=torch.float64, device=dev),
+                       pot=torch.empty(ni, dtype=torch.float64, device=dev),
+                       nnb=torch.empty(ni, dtype=torch.int32, device=dev),
+                       off=torch.empty(ni + 1, dtype=torch.int32, device=dev),
+                       lst=torch.empty(ni * KING_NNBMAX, dtype=torch.int32, device=dev))
+
+    def dev_step():
+        for ni in KING_BLOCKS:
+            b = blk[ni]
+            assert lib.gpunb_send_device(n, jm.data_ptr(), jx.data_ptr(), jv.data_ptr(), sp) == 0
+            assert lib.gpunb_regf_device(ni, b["h2"].data_ptr(), b["dtr"].data_ptr(),
+                                         b["x"].data_ptr(), b["v"].data_ptr(),
+                                         b["acc"].data_ptr(), b["jrk"].data_ptr(),
+                                         b["pot"].data_ptr(), b["nnb"].data_ptr(),
+                                         b["off"].data_ptr(), b["lst"].data_ptr(),
+                                         ni * KING_NNBMAX, KING_NNBMAX, 0, sp) == 0
+
+    out = {"workload": "King W0=6, N=2^20, Kroupa, 10% binaries as c.m. bodies, target 100, "
+                       "nbmax 1024; one step = send + regf at ni in {1024, 16384, 262144, N}",
+           "setup_s": t_ics, "pairs_per_step": pairs}
     with GpuNb(n) as nb:
-        nb.send(k.m, k.x, k.v)
+        nb.set_precision("split")
+        # device-resident steps, graphs on
+        lib.gpunb_set_graphs(1)
+        for _ in range(warmup):
+            dev_step()
+        torch.cuda.synchronize()
+        clocks = Clocks(dev.index)
+        clocks.start()
+        evs = []
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dev_step()
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        lib.gpunb_set_graphs(0)
+        step_ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+        got16 = (blk[16384]["acc"].cpu().numpy(), blk[16384]["jrk"].cpu().numpy(),
+                 blk[16384]["pot"].cpu().numpy())
+        nnb = {ni: blk[ni]["nnb"].cpu().numpy() for ni in KING_BLOCKS}
+        # per-block pair-kernel times: one step without graphs, library events
         nb.set_timing(True)
-        for ni in (1024, 16384, 262144, n):
-            act = ics.active_set(n, ni, seed=ni)
-            best = None
-            for _ in range(3 if ni < n else 2):
-                r = nb.regf(h2[act], k.dtr[act], k.x[act], k.v[act], 1025, 1024)
-                ms = float(nb.kernel_times()[-1])
-                best = ms if best is None else min(best, ms)
-            gp = ni * n / (best * 1e-3) / 1e9
-            blocks[str(ni)] = {"kernel_ms": best, "gpairs_s": gp,
+        dev_step()
+        torch.cuda.synchronize()
+        kt = [float(t) for t in nb.kernel_times()]
+        nb.set_timing(False)
+        blocks = {}
+        for q, ni in enumerate(KING_BLOCKS):
+            gp = ni * n / (kt[q] * 1e-3) / 1e9
+            blocks[str(ni)] = {"kernel_ms": float(kt[q]), "gpairs_s": gp,
                                "frac_fp32": gp * 1e9 * FLOPS_PER_PAIR / 1e12 / peak,
-                               "overflows": int((r.list[:, 0] < 0).sum())}
-            if ni == 16384:
-                ref = (r.acc.copy(), r.jrk.copy(), r.pot.copy(), r.list.copy())
+                               "overflows": int((nnb[ni] < 0).sum()),
+                               "mean_neighbours": float(np.maximum(nnb[ni], 0).mean())}
+        # FP64 kernel on the 16384 block
         nb.set_precision("fp64")
-        act = ics.active_set(n, 16384, seed=16384)
-        r = nb.regf(h2[act], k.dtr[act], k.x[act], k.v[act], 1025, 1024)
+        nb.set_timing(True)
+        b = blk[16384]
+        assert lib.gpunb_send_device(n, jm.data_ptr(), jx.data_ptr(), jv.data_ptr(), sp) == 0
+        assert lib.gpunb_regf_device(16384, b["h2"].data_ptr(), b["dtr"].data_ptr(),
+                                     b["x"].data_ptr(), b["v"].data_ptr(), b["acc"].data_ptr(),
+                                     b["jrk"].data_ptr(), b["pot"].data_ptr(),
+                                     b["nnb"].data_ptr(), b["off"].data_ptr(),
+                                     b["lst"].data_ptr(), 16384 * KING_NNBMAX, KING_NNBMAX, 0,
+                                     sp) == 0
+        torch.cuda.synchronize()
         fp64_ms = float(nb.kernel_times()[-1])
-    a, j, p, lst = ref
-    ea = np.linalg.norm(a - r.acc, axis=1) / np.linalg.norm(r.acc, axis=1)
-    ej = np.linalg.norm(j - r.jrk, axis=1) / np.linalg.norm(r.jrk, axis=1)
-    ep = np.abs(p - r.pot) / np.abs(r.pot)
+        nb.set_timing(False)
+        a64 = (b["acc"].cpu().numpy(), b["jrk"].cpu().numpy(), b["pot"].cpu().numpy())
+        nb.set_precision("split")
+        del blk
+        torch.cuda.empty_cache()
+        # end to end through the host ABI, graphs on
+        hin = {ni: (h2[acts[ni]].copy(), k.dtr[acts[ni]].copy(), k.x[acts[ni]].copy(),
+                    k.v[acts[ni]].copy()) for ni in KING_BLOCKS}
+        outs = {}
+
+        def host_step():
+            for ni in KING_BLOCKS:
+                nb.send(k.m, k.x, k.v)
+                outs[ni] = nb.regf(*hin[ni], KING_NNBMAX + 1, KING_NNBMAX, out=outs.get(ni))
+
+        lib.gpunb_set_graphs(1)
+        for _ in range(max(1, warmup - 1)):
+            host_step()
+        t = time.perf_counter()
+        for _ in range(steps):
+            host_step()
+        e2e_s = (time.perf_counter() - t) / steps
+        lib.gpunb_set_graphs(0)
+    h2d = sum(56 * n + 64 * ni for ni in KING_BLOCKS)
+    d2h = sum(60 * ni + 4 * int(np.maximum(outs[ni].list[:, 0], 0).sum()) for ni in KING_BLOCKS)
+    a, j, p = got16
+    ea = np.linalg.norm(a - a64[0], axis=1) / np.linalg.norm(a64[0], axis=1)
+    ej = np.linalg.norm(j - a64[1], axis=1) / np.linalg.norm(a64[1], axis=1)
+    ep = np.abs(p - a64[2]) / np.abs(a64[2])
     fp64_gp = 16384 * n / (fp64_ms * 1e-3) / 1e9
-    return {"workload": "King W0=6, N=2^20, Kroupa, 10% binaries as c.m. bodies, target 100, "
-                        "nbmax 1024", "setup_s": t_ics, "blocks": blocks,
-            "fp64_ni16384": {"kernel_ms": fp64_ms, "gpairs_s": fp64_gp},
-            "speedup_split_over_fp64_kernel_ni16384": blocks["16384"]["gpairs_s"] / fp64_gp,
-            "speedup_split_ni_N_over_fp64_kernel": blocks[str(n)]["gpairs_s"] / fp64_gp,
-            "rel_err_vs_fp64_kernel_ni16384": {
-                "acc_p99": float(np.percentile(ea, 99)), "acc_max": float(ea.max()),
-                "jrk_p99": float(np.percentile(ej, 99)), "jrk_max": float(ej.max()),
-                "pot_max": float(ep.max())},
-            "lists_identical_to_fp64_kernel": bool(np.array_equal(lst, r.list))}
+    big = blocks[str(n)]
+    achieved = big["gpairs_s"] * FLOPS_PER_PAIR / 1e3
+    out.update({
+        "value": pairs / (step_ms * 1e-3) / 1e9, "unit": "Gpairs/s", "step_ms": step_ms,
+        "steps": steps, "warmup": warmup, "clocks": clk,
+        "e2e": {"value": pairs / e2e_s / 1e9, "unit": "Gpairs/s", "step_s": e2e_s,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "blocks": blocks,
+        "roofline": {"bound": "fp32", "kernel": "regf_ds_kernel (ni = N block)",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "flops_per_pair": FLOPS_PER_PAIR},
+        "fp64_ni16384": {"kernel_ms": fp64_ms, "gpairs_s": fp64_gp},
+        "speedup_split_over_fp64_kernel_ni16384": blocks["16384"]["gpairs_s"] / fp64_gp,
+        "speedup_split_ni_N_over_fp64_kernel": big["gpairs_s"] / fp64_gp,
+        "rel_err_vs_fp64_kernel_ni16384": {
+            "acc_p99": float(np.percentile(ea, 99)), "acc_max": float(ea.max()),
+            "jrk_p99": float(np.percentile(ej, 99)), "jrk_max": float(ej.max()),
+            "pot_max": float(ep.max())}})
+    check = ("King N=2^20 ni=16384", k.m, k.x, k.v, h2, k.dtr, acts[16384], got16,
+             KING_NNBMAX + 1, KING_NNBMAX)
+    cpu_block = (k, h2, acts[1024])
+    return out, check, cpu_block
+
+
+def king_cpu_block(k, h2, act):
+    """The FP32 port on the King 2^20 set: one block of 1024 active bodies
+    against all N (1.07e9 pairs) on the host cores."""
+    from oracle import oracle as O
+    port = O.Port()
+    port.send(k.m, k.x, k.v)
+    t = time.perf_counter()
+    port.regf(h2[act], k.dtr[act], k.x[act], k.v[act], KING_NNBMAX + 1, KING_NNBMAX)
+    dt = time.perf_counter() - t
+    return {"value": len(act) * k.n / dt / 1e9, "unit": "Gpairs/s", "cores": O.num_threads(),
+            "kind": "port", "sample": f"one block of {len(act)} active bodies against all "
+                                      f"{k.n} (FP32 restatement of src/Main/reg.avx.cpp)"}
 
 
 def irregular_leg(c, h2, lists_src):
@@ -496,6 +660,9 @@ def main():
 
     from nbody6ppgpu_gb300.gpunb import GpuNb, load
     lib = load()
+    # launch shapes from the autotuner: each block's (N, ni) bucket is tuned
+    # on its first call (a warm-up call, untimed) and cached
+    lib.gpunb_set_autotune(1)
     c, acts = make_inputs()
     h2 = c.h2()
     dev = torch.device("cuda", local)
@@ -523,6 +690,8 @@ def main():
 
     nb = GpuNb(N)
 
+    launch_plan = {}
+
     def dev_step():
         for ni in BLOCKS:
             b = blk[ni]
@@ -535,6 +704,11 @@ def main():
                                        b["off"].data_ptr(), b["lst"].data_ptr(),
                                        ni * NNBMAX, NNBMAX, 0, sp)
             assert rc == 0, rc
+            launch_plan[ni] = nb.last_launch()[:2]
+
+    import ctypes as _C
+    lib.gpunb_sort_count.restype = _C.c_longlong
+    sort_counter = {"timed": 0}
 
     def timed_steps(k, precision, graphs=False, timing=True):
         """k steps, each bracketed by CUDA events on the library's stream.
@@ -549,6 +723,7 @@ def main():
             dist.barrier()
         lib.gpunb_set_timing(1 if timing else 0)
         evs = []
+        s0 = lib.gpunb_sort_count()
         for _ in range(k):
             with torch.cuda.stream(stream):    # L2 flush between steps, on the timed
                 flush.zero_()                  # stream before its start event (untimed)
@@ -559,6 +734,7 @@ def main():
             e1.record(stream)
             evs.append((e0, e1))
         torch.cuda.synchronize()
+        sort_counter["timed"] = lib.gpunb_sort_count() - s0
         kt = nb.kernel_times(max_n=64 * k + 64) if timing else []
         lib.gpunb_set_timing(0)
         lib.gpunb_set_graphs(0)
@@ -572,6 +748,7 @@ def main():
     clocks.start()
     t_wall = time.perf_counter()
     ms, _ = timed_steps(args.steps, "split", graphs=True, timing=False)
+    sorts_timed = sort_counter["timed"]   # j-set re-orderings in the timed steps
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     step_ms = float(sum(ms) / len(ms))
@@ -618,6 +795,7 @@ def main():
     nb.set_precision("split")
     dev_step()
     torch.cuda.synchronize()
+    plan_split = dict(launch_plan)   # the split kernel's shapes (the FP64 pass follows)
     res_split = {ni: (blk[ni]["acc"].cpu().numpy().copy(), blk[ni]["jrk"].cpu().numpy().copy(),
                       blk[ni]["pot"].cpu().numpy().copy()) for ni in (1024, 16384)}
     fp64_ms, fp64_kt = timed_steps(max(1, args.fp64_steps), "fp64")
@@ -679,37 +857,51 @@ def main():
         lists_by_particle[acts[65536]] = outs[65536].list
         irr, irr_check = irregular_leg(c, h2, lists_by_particle)
     pot, pot_result = potential_leg(c)
-    king = None
+    king = king_check = king_cpu = None
     if not args.no_large:
-        king = king1m_leg(n_sm, peak_mhz)
+        king, king_check, king_cpu = king1m_leg(lib, dev, stream, n_sm, peak_mhz)
     rsp = rs_predictor_leg(dev)
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu, _ = cpu_baseline(c, acts)
         cpu.update(cpu_side_checks(c, irr_check, pot_result))
+        parity = {"bound": "per particle |dQ| <= 1e-6 max(|Q|, sum_j |q_ij| / 8) for force and "
+                           "jerk, |dpot| <= 1e-6 |pot|; plain relative errors beside it",
+                  "plummer65536_ni16384": oracle_parity(
+                      "Plummer N=65536 ni=16384", c.m, c.x, c.v, h2, c.dtr, acts[16384],
+                      res_split[16384], LMAX, NNBMAX)}
+        if king is not None:
+            parity["king1m_ni16384"] = oracle_parity(*king_check, rows=256)
+            king["cpu_baseline"] = king_cpu_block(*king_cpu)
 
-    # the library's own kernels per step: per send copy, bbox, morton, pack;
-    # per regf prep, pair kernel, merge, two scans, gather, offsets, plus the
-    # Morton key kernel of the i-ordering when ni >= 256.  The Morton sorts are
-    # CUB radix sorts (43 launches per step in the ncu launch list).
-    own_per_step = 4 * len(BLOCKS) + 7 * len(BLOCKS) + sum(ni >= 256 for ni in BLOCKS)
+    # the library's own kernels: per send copy and pack, plus bbox and Morton
+    # keys when the send re-orders the j-set; per regf prep, pair kernel,
+    # merge, two scans, gather, offsets, plus the Morton key kernel of the
+    # i-ordering when ni >= 256.  The Morton sorts are CUB radix sorts: 6
+    # launches per j-set re-ordering, 6 per i-ordering of 16384 or 65536
+    # bodies and 1 for 1024 (the launch list in profiles/).
+    own = args.steps * (2 * len(BLOCKS) + 7 * len(BLOCKS) + sum(ni >= 256 for ni in BLOCKS)) \
+        + 2 * sorts_timed
+    cub = args.steps * 13 + 6 * sorts_timed
     line = {
         "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
         "ms_per_step_without_graphs": float(np.mean(ms_nograph)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Plummer sphere, Kroupa IMF, Henon units)",
-        "config": {"workload": WORKLOAD, "N": N, "blocks": BLOCKS, "nb_target": NB_TARGET,
-                   "nnbmax": NNBMAX, "precision": "split FP32 (double-single positions)",
-                   "l2": "flushed (256 MB write) between timed steps",
-                   "launch": "device entry points replayed as CUDA graphs, one per call shape",
-                   "parallelism": f"replicas x{ws}"},
+        "config": config(ws),
+        "impl_detail": {"precision": "split FP32 (double-single positions)",
+                        "launch": "device entry points replayed as CUDA graphs, one per call "
+                                  "shape"},
         "fp64": {"value": fp64_value, "unit": "Gpairs/s",
                  "kernel_ms_ni65536": float(np.mean(fp64_big)),
                  "speedup_split_over_fp64_kernel": float(np.mean(fp64_big)) / k_ms},
         "rel_err_vs_fp64_kernel": errs,
         "pair_kernel_per_block": per_block,
+        "launch_plan_per_block": {str(ni): {"variant": v, "splits": sp_}
+                                  for ni, (v, sp_) in plan_split.items()},
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved_tflops / peak,
                      "frac_at_load_clock": achieved_tflops / fp32_peak_tflops(n_sm, load_mhz),
@@ -723,14 +915,18 @@ def main():
         "e2e": {"value": ws * pairs_per_step / e2e_s / 1e9, "unit": "Gpairs/s",
                 "value_without_graphs": ws * pairs_per_step / e2e_nograph_s / 1e9,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": own_per_step * args.steps,
-        "library_launches": {"cub_radix_sort": 43 * args.steps},
+        "gpu_launches": own,
+        "library_launches": {"cub_radix_sort": cub},
+        "j_set_reorderings": {"timed_sends": args.steps * len(BLOCKS), "reorderings": sorts_timed,
+                              "interval": RESORT_EVERY},
         "clocks": clk,
         "wall_s_timed_region": t_wall,
         "device": name,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if parity is not None:
+        line["parity_vs_fp64_oracle"] = parity
     if batched is not None:
         line["batched_clusters"] = batched
     if king is not None:
@@ -740,7 +936,7 @@ def main():
     line["potential"] = pot
     line["rs_predictor_inference"] = rsp
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json.dumps(line, default=_jsonable), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0

@@ -104,11 +104,35 @@ int gpunb_variant_info(int variant, int *ipt, int *warps_i, int *warps_j);
  * in effect, or -1 without a device.  Results are identical in both modes. */
 int gpunb_set_host_path(int mode);
 
-/* Autotuner: time every shape for (nj, ni) on the current j-set with
- * synthetic i-particles drawn from it, keep the fastest, and cache it per
- * (nj bucket, ni bucket).  Returns the chosen variant; *splits, *ms out. */
+/* Ordering of the j-set (no reference counterpart).  Every send packs the
+ * bodies into tiles that follow a Morton order; the order itself (bounding
+ * box, keys, radix sort) is recomputed when nj changes and on every
+ * `every`-th send (default 8, or the environment variable
+ * GPUNB_RESORT_EVERY), and the sends between reuse it with the tiles re-packed
+ * from the current positions.  Results do not depend on the order; only the
+ * tiles' spatial coherence, and with it the speed, would decay if bodies
+ * travelled far between re-orderings.  1 re-orders on every send.  The next
+ * send after this call re-orders.  Returns the previous interval;
+ * gpunb_sort_count returns the number of re-orderings so far. */
+int gpunb_set_resort_interval(int every);
+long long gpunb_sort_count(void);
+
+/* Autotuner.  With gpunb_set_autotune(1) (or the environment variable
+ * GPUNB_AUTOTUNE=1 at start-up) the first regf call of an (N, ni)
+ * half-octave bucket -- gpunb_regf_, gpunb_regf_device, or a batched call's
+ * (total bodies, total active) bucket -- times every launch shape (kernel
+ * variant: i-particles per thread, warps along i and j, j per warp vote; and
+ * the j-split count, or for batches the work items per resident block) on
+ * that call's own active block, caches the fastest and uses it from then on;
+ * later calls of the bucket read the cache.  Returns the previous setting.
+ * gpunb_autotune tunes the bucket of ni ahead of any call, on synthetic
+ * i-particles drawn from the current j-set; returns the chosen variant and
+ * *splits, *ms. */
+int gpunb_set_autotune(int flag);
 int gpunb_autotune(int ni, int m_flag, int *splits, float *ms);
-/* Load / save the tuning cache (text file); return the number of entries. */
+/* Save the tuning cache to a text file / replace the cache with a saved
+ * one; return the number of entries, or -1 when the file cannot be opened
+ * (the cache is then unchanged). */
 int gpunb_tune_load(const char *path);
 int gpunb_tune_save(const char *path);
 
@@ -180,17 +204,20 @@ int gpunb_batch_last_plan(int *variant, int *items);
 void gpunb_set_graphs(int flag);
 
 /* Potential of gpupot_ for callers that cannot allocate device memory (no
- * counterpart in the reference).  Meant for code that must not call
- * cudaMalloc: an energy check issued from inside a CUDA-graph-captured step,
- * or a host program whose own caching allocator already holds the free device
- * memory.  All pointers are device memory (m[n], x[n][3], pot[ni]); work is
- * queued on `stream` (a cudaStream_t).  The scratch is a fixed 4 MiB array in
- * the library image, present on every GPU that loads the library; the call
- * allocates nothing.  Limits: 1 <= n <= 65536, 1 <= istart, istart-1+ni <= n;
- * anything else returns GPUNB_E_ARG without launching.  The first call on a
- * device looks up the array's device address, so make it before any stream
- * capture.  Calls share the scratch: calls that overlap on the GPU race, so
- * serialise them on one stream.  Returns 0 or an error code. */
+ * counterpart in the reference).  Meant for host programs that must not call
+ * cudaMalloc: one whose own caching allocator already holds the free device
+ * memory (cudaMalloc would fail), or a step loop that cannot afford the
+ * device-wide synchronisation of cudaFree.  All pointers are device memory
+ * (m[n], x[n][3], pot[ni]); work is queued on `stream` (a cudaStream_t).  The
+ * scratch is a fixed 4 MiB array in the library image, present on every GPU
+ * that loads the library; the call allocates nothing.  Limits: 1 <= n <=
+ * 65536, 1 <= istart, istart-1+ni <= n; anything else returns GPUNB_E_ARG
+ * without launching.  The first call on a device looks up the array's device
+ * address.  The call waits for its own work on `stream` and returns 0 or an
+ * error code, including the codes its kernels raise (GPUNB_E_NAN for a NaN
+ * input, GPUNB_E_TIMEOUT for a bounded wait that gave up); with such a code
+ * every pot[k] is NaN.  Calls share the scratch: calls that overlap on the
+ * GPU race, so serialise them on one stream. */
 int gpupot_device_noalloc(int istart, int ni, int n, const double *m, const double *x,
                           double *pot, void *stream);
 
@@ -268,6 +295,56 @@ int gpunb_rs_update_device(int ni, const gpunb_rs_params *p, const double *x, co
                            const double *dtr, const void *wq, const float *wf,
                            const float *norm, double *rs_new, double *target, int *used,
                            void *stream);
+
+/* Regular corrector of an active block on the device (no reference
+ * counterpart as an entry point: it does, for every body of the block at
+ * once, the work of src/Main/regcor_gpu.F REGCOR_GPU, which the reference
+ * runs on the host body by body).  For body I = iact[k] (1-based), with its
+ * new regular force freg[k][3], derivative fdr[k][3] and new neighbour row
+ * nlist[k*lmax ..] (count, then ascending 1-based body indices, self
+ * removed): the RS rule with the c.m.-body and <= 3-neighbour branches
+ * (:120-252), the small-central-mass change for an empty list (:120-143), the
+ * force changes of lost and gained neighbours with the retention of old
+ * neighbours whose step is below SMIN (:262-460; a retained body is inserted
+ * into nlist and the row count updated), the Hermite corrector (:462-552:
+ * XN, XNDOT, FI, FR, FIDOT, FRDOT, D0, D0R..D3R, T0R; tidal FIDOT term for
+ * KZ(14) <= 2), the list copy LIST(.,I) = NLIST on a change (:608-616), the
+ * new regular step STEPR and the irregular step reduction (:618-800).  Not
+ * done here: XTRNLF, FCLOUD, CHECKL, FPCORR and the tidal energy ETIDE.
+ * All state arrays are device memory in the Fortran COMMON layout of all
+ * NTOT bodies (index I-1; vectors as [NTOT][3]); list is LIST(LMAX,NTOT)
+ * as [NTOT][lmax] with 1-based members.  The active bodies must be distinct.
+ * Asynchronous on `stream`; returns 0 or GPUNB_E_ARG. */
+typedef struct {
+  double time;              /* TIME */
+  double dtmin, smin, smax; /* DTMIN, SMIN, SMAX */
+  double etar;              /* ETAR */
+  double tidal4;            /* TIDAL(4) */
+  int kz14;                 /* KZ(14) */
+  int m_flag;               /* 1: mass-weighted neighbour criterion (KZ(39) = 2, 3) */
+  int nnbmax;               /* NNBMAX */
+  int n;                    /* N: single bodies 1..N, c.m. bodies N+1..NTOT */
+  int ntot;                 /* NTOT */
+  int ifirst;               /* IFIRST */
+  int lmax;                 /* row stride of list and nlist */
+  gpunb_rs_params rs;       /* NNBOPT, NNBMAX, RSCALE, RC, RSFAC, BODYM, RDENS, NB_FLAG */
+} gpunb_regcor_params;
+typedef struct {
+  const double *x, *xdot;         /* X, XDOT predicted to TIME */
+  const double *body;             /* BODY */
+  const double *h;                /* H(IPAIR) of the KS pairs (c.m. branch); may be NULL */
+  const double *x0, *x0dot;       /* X0, X0DOT */
+  double *t0r, *stepr, *step, *t0, *timenw;
+  double *fi, *fidot, *fr, *frdot;
+  double *d0, *d0r, *d1r, *d2r, *d3r;
+  double *xn, *xndot;             /* XN, XNDOT */
+  double *rs;                     /* RS */
+  int *list;                      /* LIST */
+  int *counters;                  /* NBVOID, NBSMIN, NBFLUX, NICONV increments; may be NULL */
+} gpunb_regcor_state;
+int gpunb_regcor_device(int ni, const int *iact, const double *freg, const double *fdr,
+                        int *nlist, const gpunb_regcor_params *p, const gpunb_regcor_state *s,
+                        void *stream);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIB = PKG / "libgpunb.so"
 SOURCES = ["regf_kernels.cu", "pot_kernels.cu", "order_kernels.cu", "engine.cu", "noalloc.cu",
-           "rsmlp.cu", "irr.cu", "peak.cu"]
+           "rsmlp.cu", "irr.cu", "peak.cu", "regcor.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -272,6 +272,12 @@ struct Engine {
   // (Grace + GB300 over NVLink-C2C); 0 = staged through pinned buffers
   int host_direct = 0;
   int host_direct_supported = 0;
+  // j-set ordering: re-sorted along the Morton curve when nj changes and on
+  // every resort_every-th send; the sends between reuse the permutation
+  int resort_every = 8;
+  int sends_since_sort = 0;
+  int sorted_nj = -1;
+  long long sorts = 0;
   // profile counters (GPUNB_profile)
   double time_send = 0, time_grav = 0, time_reduce = 0, time_out = 0;
   long long num_inter = 0;
@@ -287,6 +293,26 @@ static std::mutex g_mutex;
 // largest active block per call: the two-level list scan covers
 // SCAN_ITEMS * SCAN_ITEMS rows (4096 * 4096)
 constexpr int kMaxNi = 4096 * 4096;
+
+// Replaces the tuning cache with the entries of a saved file; -1 (cache
+// unchanged) when the file cannot be opened.  Caller holds g_mutex.
+static int tune_load(const char *path) {
+  FILE *f = path ? fopen(path, "r") : nullptr;
+  if (!f) return -1;
+  g.tune.clear();   // the file's entries replace the cache
+  int n = 0;
+  long long key;
+  int v, s;
+  float ms;
+  while (fscanf(f, "%lld %d %d %f", &key, &v, &s, &ms) == 4) {
+    if (v >= 0 && v < regf_num_variants() && s > 0) {
+      g.tune[key] = TuneEntry{v, s, ms};
+      ++n;
+    }
+  }
+  fclose(f);
+  return n;
+}
 
 static bool devinit(int irank) {
   if (g.devinit) return true;
@@ -326,9 +352,10 @@ static bool devinit(int irank) {
   g.host_direct = g.host_direct_supported;
   if (const char *p = getenv("GPUNB_HOST_DIRECT")) g.host_direct &= (atoi(p) != 0);
   g.devinit = true;
-  if (const char *p = getenv("GPUNB_TUNE_CACHE")) gpunb_tune_load(p);
+  if (const char *p = getenv("GPUNB_TUNE_CACHE")) tune_load(p);
   if (const char *p = getenv("GPUNB_AUTOTUNE")) g.autotune_on = atoi(p);
   if (const char *p = getenv("GPUNB_GRAPHS")) g_use_graphs = atoi(p) != 0;
+  if (const char *p = getenv("GPUNB_RESORT_EVERY")) g.resort_every = std::max(1, atoi(p));
   return true;
 }
 
@@ -352,24 +379,49 @@ static bool ensure_order_scratch(int n) {
          g.ovals_alt.ensure(nn * sizeof(int)) && g.otemp.ensure(order_temp_bytes((int)nn));
 }
 
-static int send_common(int nj, cudaStream_t st) {
+// Whether the next send re-orders the j-set along the Morton curve: when nj
+// differs from the last ordered set's, and on every resort_every-th send.
+// The sends between keep the permutation -- bodies move little between the
+// block times of consecutive sends (intgrt.F:912-944), and the tiles are
+// re-packed from the current positions with their true centres, radii and
+// boxes, so results do not depend on the choice; only the spatial coherence
+// of the tiles, and with it the speed, would decay if bodies travelled far.
+// Taken once per call, outside any captured launch sequence.
+static bool send_resorts(int nj) {
+  return nj != g.sorted_nj || g.resort_every <= 1 || g.sends_since_sort + 1 >= g.resort_every;
+}
+static void send_account(int nj, bool resorted) {
+  if (resorted) {
+    g.sorted_nj = nj;
+    g.sends_since_sort = 0;
+    ++g.sorts;
+  } else {
+    ++g.sends_since_sort;
+  }
+}
+
+static int send_common(int nj, cudaStream_t st, bool resort) {
   const int ntile = (nj + JT - 1) / JT;
-  if (!g.jtiles.ensure((size_t)std::max(ntile, 1) * TILE_BYTES) ||
-      !g.jperm.ensure((size_t)std::max(ntile, 1) * JT * sizeof(int)) || !ensure_order_scratch(nj))
+  const size_t perm_bytes = (size_t)std::max(ntile, 1) * JT * sizeof(int);
+  if (perm_bytes > g.jperm.bytes) resort = true;   // a new permutation buffer
+  if (!g.jtiles.ensure((size_t)std::max(ntile, 1) * TILE_BYTES) || !g.jperm.ensure(perm_bytes) ||
+      !ensure_order_scratch(nj))
     return GPUNB_E_ALLOC;
   double *m = g.jraw.as<double>();
   const double *x = m + nj;
-  // spatial order of the j-set: bounding box, Morton keys, stable sort
-  CUDA_OR(launch_bbox(x, nj, g.bbox.as<int>(), st), GPUNB_E_CUDA);
-  CUDA_OR(launch_order(x, nj, g.bbox.as<int>(), g.okeys.as<unsigned long long>(),
-                       g.okeys_alt.as<unsigned long long>(), g.ovals_alt.as<int>(),
-                       g.jperm.as<int>(), g.otemp.p, g.otemp.bytes, st),
-          GPUNB_E_CUDA);
-  // padding slots of the last tile map to -1 (never a neighbour)
-  if (ntile * JT > nj)
-    CUDA_OR(cudaMemsetAsync(g.jperm.as<int>() + nj, 0xff, (size_t)(ntile * JT - nj) * sizeof(int),
-                            st),
+  if (resort) {
+    // spatial order of the j-set: bounding box, Morton keys, stable sort
+    CUDA_OR(launch_bbox(x, nj, g.bbox.as<int>(), st), GPUNB_E_CUDA);
+    CUDA_OR(launch_order(x, nj, g.bbox.as<int>(), g.okeys.as<unsigned long long>(),
+                         g.okeys_alt.as<unsigned long long>(), g.ovals_alt.as<int>(),
+                         g.jperm.as<int>(), g.otemp.p, g.otemp.bytes, st),
             GPUNB_E_CUDA);
+    // padding slots of the last tile map to -1 (never a neighbour)
+    if (ntile * JT > nj)
+      CUDA_OR(cudaMemsetAsync(g.jperm.as<int>() + nj, 0xff,
+                              (size_t)(ntile * JT - nj) * sizeof(int), st),
+              GPUNB_E_CUDA);
+  }
   CUDA_OR(launch_pack_jtiles(m, x, m + 4 * (size_t)nj, nj, g.jperm.as<int>(),
                              g.jtiles.as<float>(), ntile, g.err.as<int>(), st),
           GPUNB_E_CUDA);
@@ -561,18 +613,28 @@ static void choose_plan(int ni, bool mflag, int &variant, int &S) {
   if (g.force_splits > 0) S = std::min(g.force_splits, std::max(1, js.ntile));
 }
 
-// time every launch shape for (nj, ni) with the given device i-set; keeps
-// the fastest in the cache.
+// Times every launch shape (kernel variant x j-split count around the
+// heuristic's) on the given device i-set -- the caller's own active block --
+// and keeps the fastest in the cache under the (N, ni) bucket.  The time
+// covers the pair kernel and the merge of its split partials (more splits
+// balance the persistent queue better but leave more partials to merge);
+// the merge writes into scratch.  Runs on `st`, synchronously.
 static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out,
-                         float *ms_out) {
+                         float *ms_out, cudaStream_t st) {
   const JSet js = jset();
   const int ni = is.ni;
   int best_v = -1, best_s = 1;
   float best = 1e30f;
-  cudaStream_t st = g.stream;
+  if (!g.outblk.ensure((size_t)7 * ni * sizeof(double) + (size_t)(ni + 2) * sizeof(int)) ||
+      !g.rowlen.ensure((size_t)ni * sizeof(int)))
+    return -1;
+  double *sacc = g.outblk.as<double>();
+  int *snnb = (int *)(sacc + 7 * (size_t)ni);
   for (int v = 0; v < regf_num_variants(); ++v) {
     const long long base = plan_splits(v, ni, js.ntile, mflag);
     const long long cands[5] = {base / 4, base / 2, base, base * 2, base * 4};
+    const int itile = regf_variant(v).itile();
+    const int ni_pad = ((ni + itile - 1) / itile) * itile;
     int last_s = -1;
     for (long long sc : cands) {
       int s = (int)std::max(1ll, std::min<long long>(sc, std::max(1, js.ntile)));
@@ -583,11 +645,18 @@ static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out
       bool ok = true;
       for (int r = 0; r < reps + 1 && ok; ++r) {
         if (run_pair_pass(is, nnbmax, mflag, v, s, st, true) != GPUNB_OK) ok = false;
+        if (ok && launch_regf_merge(g.part.as<double>(), true, s, ni, ni_pad, is.perm,
+                                    g.cnt.as<int>(), nnbmax, sacc, sacc + 3 * (size_t)ni,
+                                    sacc + 6 * (size_t)ni, snnb, g.rowlen.as<int>(),
+                                    st) != cudaSuccess)
+          ok = false;
+        if (ok && cudaEventRecord(g.ek1, st) != cudaSuccess) ok = false;
         if (cudaStreamSynchronize(st) != cudaSuccess) ok = false;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, g.ek0, g.ek1);
         if (r > 0) tot += ms;
       }
+      if (!ok) cudaGetLastError();
       if (!ok) continue;
       const float ms = tot / reps;
       if (ms < best) {
@@ -748,7 +817,7 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   int variant, S;
   if (g.autotune_on && g.precision == 0 && g.force_variant < 0 &&
       g.tune.find(tune_key(g.nj, ni, mflag, 0)) == g.tune.end())
-    autotune_with(is, nnbmax, mflag, nullptr, nullptr);
+    autotune_with(is, nnbmax, mflag, nullptr, nullptr, st);
   choose_plan(ni, mflag, variant, S);
   if (run_pair_pass(is, nnbmax, mflag, variant, S, st, false) != GPUNB_OK) return;
 
@@ -928,6 +997,8 @@ void gpunb_close_(void) {
   g.ovals_alt.release(); g.otemp.release(); g.irec.release();
   g.nbodymax = 0;
   g.nj = 0;
+  g.sorted_nj = -1;
+  g.sends_since_sort = 0;
   g.is_open = false;
 }
 
@@ -942,6 +1013,7 @@ void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
   const double t0 = wtime();
   g.isend++;
   cudaStream_t st = g.stream;
+  const bool resort = send_resorts(n);
   if (g.host_direct) {
     // the device reads the caller's arrays: the whole call is device work,
     // replayed as a CUDA graph per (n, arrays) when graphs are on
@@ -958,7 +1030,7 @@ void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
         jobs.j[2] = HostCopyJob{vj, d + 4 * (size_t)n, 3ll * n, 8};
         CUDA_OR(launch_host_copy(jobs, s), GPUNB_E_CUDA);
       }
-      const int rc = send_common(n, s);
+      const int rc = send_common(n, s, resort);
       if (rc != GPUNB_OK) return rc;
       HostCopyJobs ej;
       ej.count = 1;
@@ -969,11 +1041,13 @@ void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
     int rc;
     if (g_use_graphs && !g.timing)
       rc = run_graphed(dev_graph({2, n, (long long)(uintptr_t)mj, (long long)(uintptr_t)xj,
-                                  (long long)(uintptr_t)vj, (long long)(uintptr_t)st}),
+                                  (long long)(uintptr_t)vj, (long long)(uintptr_t)st,
+                                  resort ? 1 : 0}),
                        true, st, issue);
     else
       rc = issue(st);
     if (rc != GPUNB_OK) return;
+    send_account(n, resort);
     g.nj = n;
     CUDA_OR(cudaStreamSynchronize(st), );
     check_device_error(*herr);
@@ -989,7 +1063,8 @@ void gpunb_send_(int *nj, double mj[], double xj[][3], double vj[][3]) {
     CUDA_OR(cudaMemcpyAsync(g.jraw.p, h, (size_t)n * 7 * sizeof(double), cudaMemcpyHostToDevice,
                             st), );
   }
-  if (send_common(n, st) != GPUNB_OK) return;
+  if (send_common(n, st, resort) != GPUNB_OK) return;
+  send_account(n, resort);
   if (!g.hout.ensure(sizeof(int))) return;
   int *herr = g.hout.as<int>();
   CUDA_OR(cudaMemcpyAsync(herr, g.err.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
@@ -1053,7 +1128,8 @@ void gpupot_(int *irank, int *istart, int *ni, int *n, double m[], double x[][3]
   CUDA_OR(launch_pack_pot(d, d + nn, nn, g.ptiles.as<float>(), ntile, g.err.as<int>(), st), );
   CUDA_OR(launch_pot(g.ptiles.as<float>(), ntile, d + nn, is0, k, gx, S, g.ppart.as<double>(),
                      ni_pad, g.err.as<int>(), st), );
-  CUDA_OR(launch_pot_merge(g.ppart.as<double>(), S, k, ni_pad, g.pout.as<double>(), st), );
+  CUDA_OR(launch_pot_merge(g.ppart.as<double>(), S, k, ni_pad, g.err.as<int>(),
+                           g.pout.as<double>(), st), );
   // results land in the staging buffer (reused: m/x no longer needed)
   CUDA_OR(cudaMemcpyAsync(h, g.pout.p, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, st), );
   int herr = 0;
@@ -1164,30 +1240,37 @@ int gpunb_autotune(int ni, int m_flag, int *splits, float *ms) {
   if (order_iset(is, g.stream) != GPUNB_OK) return -1;
   const int saved = g.precision;
   g.precision = 0;
-  const int v = autotune_with(is, 1024, m_flag != 0, splits, ms);
+  const int v = autotune_with(is, 1024, m_flag != 0, splits, ms, g.stream);
   g.precision = saved;
   return v;
 }
 
+int gpunb_set_resort_interval(int every) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  const int prev = g.resort_every;
+  g.resort_every = std::max(1, every);
+  g.sends_since_sort = 0;
+  g.sorted_nj = -1;   // the next send re-orders
+  return prev;
+}
+
+long long gpunb_sort_count(void) { return g.sorts; }
+
+int gpunb_set_autotune(int flag) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  const int prev = g.autotune_on;
+  g.autotune_on = flag ? 1 : 0;
+  return prev;
+}
+
 int gpunb_tune_load(const char *path) {
-  FILE *f = fopen(path, "r");
-  if (!f) return 0;
-  int n = 0;
-  long long key;
-  int v, s;
-  float ms;
-  while (fscanf(f, "%lld %d %d %f", &key, &v, &s, &ms) == 4) {
-    if (v >= 0 && v < regf_num_variants() && s > 0) {
-      g.tune[key] = TuneEntry{v, s, ms};
-      ++n;
-    }
-  }
-  fclose(f);
-  return n;
+  std::lock_guard<std::mutex> lk(g_mutex);
+  return tune_load(path);
 }
 
 int gpunb_tune_save(const char *path) {
-  FILE *f = fopen(path, "w");
+  std::lock_guard<std::mutex> lk(g_mutex);
+  FILE *f = path ? fopen(path, "w") : nullptr;
   if (!f) return -1;
   int n = 0;
   for (const auto &kv : g.tune) {
@@ -1206,6 +1289,7 @@ int gpunb_send_device(int nj, const double *m, const double *x, const double *v,
     return GPUNB_E_CAPACITY;
   }
   cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  const bool resort = send_resorts(nj);
   auto issue = [&](cudaStream_t s) -> int {
     double *d = g.jraw.as<double>();
     HostCopyJobs jobs;   // one copy kernel for the three arrays
@@ -1214,16 +1298,20 @@ int gpunb_send_device(int nj, const double *m, const double *x, const double *v,
     jobs.j[1] = HostCopyJob{x, d + nj, 3ll * nj, 8};
     jobs.j[2] = HostCopyJob{v, d + 4 * (size_t)nj, 3ll * nj, 8};
     CUDA_OR(launch_host_copy(jobs, s), GPUNB_E_CUDA);
-    return send_common(nj, s);
+    return send_common(nj, s, resort);
   };
   int rc;
   if (g_use_graphs && !g.timing)
     rc = run_graphed(dev_graph({0, nj, (long long)(uintptr_t)m, (long long)(uintptr_t)x,
-                                (long long)(uintptr_t)v, (long long)(uintptr_t)st}),
+                                (long long)(uintptr_t)v, (long long)(uintptr_t)st,
+                                resort ? 1 : 0}),
                      true, st, issue);
   else
     rc = issue(st);
-  if (rc == GPUNB_OK) g.nj = nj;
+  if (rc == GPUNB_OK) {
+    send_account(nj, resort);
+    g.nj = nj;
+  }
   return rc;
 }
 
@@ -1285,6 +1373,16 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
   }
   cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
   const bool mflag = m_flag != 0;
+  if (g.autotune_on && g.precision == 0 && g.force_variant < 0 && g.nj > 0 &&
+      g.tune.find(tune_key(g.nj, ni, mflag, 0)) == g.tune.end()) {
+    // first sight of this (N, ni) bucket: tune on the caller's own block
+    ISet is;
+    is.h2 = h2; is.dtr = dtr; is.x = xi; is.v = vi; is.ni = ni;
+    is.perm = nullptr;
+    is.rec = nullptr;
+    if (order_iset(is, st) != GPUNB_OK) return GPUNB_E_ALLOC;
+    if (autotune_with(is, nnbmax, mflag, nullptr, nullptr, st) < 0) return GPUNB_E_CUDA;
+  }
   int variant, S;
   choose_plan(ni, mflag, variant, S);
   g.num_inter += (long long)ni * g.nj;

@@ -99,7 +99,8 @@ int pot_itile();
 cudaError_t launch_pot(const float *tiles, int ntile, const double *x, int istart0, int ni,
                        int gx, int S, double *part, int ni_pad, int *err, cudaStream_t st);
 int pot_blocks_per_sm();
-cudaError_t launch_pot_merge(const double *part, int S, int ni, int ni_pad, double *pot,
-                             cudaStream_t st);
+// err (may be null): the call's device error word; nonzero -> every pot[i] = NaN
+cudaError_t launch_pot_merge(const double *part, int S, int ni, int ni_pad, const int *err,
+                             double *pot, cudaStream_t st);
 
 }  // namespace gpunb

@@ -123,9 +123,14 @@ __global__ void __launch_bounds__(32 * WI) pot_ds_kernel(const float *__restrict
     }
   }
   if (s_abort) {
+    // Copies for tiles t .. t+PSTAGE-1 may still be in flight, tile t's
+    // included (its wait is the one that gave up): wait for each of them
+    // before the block exits, so that no bulk copy writes into shared memory
+    // the block no longer owns.  The block writes no partial sums; the
+    // merge sees the error word and writes NaN.
     if (tid == 0) {
-      for (int u = t + 1; u < nt && u < t + PSTAGE; ++u)
-        mbar_wait_bounded(&bar[u % PSTAGE], (uint32_t)(u / PSTAGE) & 1u, 1u << 16);
+      for (int u = t; u < nt && u < t + PSTAGE; ++u)
+        mbar_wait_bounded(&bar[u % PSTAGE], (uint32_t)(u / PSTAGE) & 1u, 1u << 20);
       raise_error(err, GPUNB_E_TIMEOUT);
     }
     return;
@@ -135,10 +140,18 @@ __global__ void __launch_bounds__(32 * WI) pot_ds_kernel(const float *__restrict
     if (iloc[k] >= 0) part[(size_t)sy * ni_pad + iloc[k]] = (double)hi[k] + (double)lo[k];
 }
 
+// Sums the S partials of each i in split order.  When an earlier kernel of
+// the call raised an error (a NaN input, a bounded wait that gave up and left
+// its partial sums unwritten), every result is NaN: partial sums left over
+// from an earlier call can never pass for this call's potentials.
 __global__ void pot_merge_kernel(const double *__restrict__ part, int S, int ni, int ni_pad,
-                                 double *__restrict__ pot) {
+                                 const int *__restrict__ err, double *__restrict__ pot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ni) return;
+  if (err && *(volatile const int *)err != 0) {
+    pot[i] = __longlong_as_double(0x7ff8000000000000ll);   // quiet NaN
+    return;
+  }
   double s = 0.0;
   for (int k = 0; k < S; ++k) s += part[(size_t)k * ni_pad + i];
   pot[i] = s;
@@ -173,9 +186,9 @@ cudaError_t launch_pot(const float *tiles, int ntile, const double *x, int istar
   return cudaGetLastError();
 }
 
-cudaError_t launch_pot_merge(const double *part, int S, int ni, int ni_pad, double *pot,
-                             cudaStream_t st) {
-  pot_merge_kernel<<<(ni + 255) / 256, 256, 0, st>>>(part, S, ni, ni_pad, pot);
+cudaError_t launch_pot_merge(const double *part, int S, int ni, int ni_pad, const int *err,
+                             double *pot, cudaStream_t st) {
+  pot_merge_kernel<<<(ni + 255) / 256, 256, 0, st>>>(part, S, ni, ni_pad, err, pot);
   return cudaGetLastError();
 }
 

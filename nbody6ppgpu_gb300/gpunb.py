@@ -68,6 +68,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "gpunb_num_variants": ([], C.c_int),
         "gpunb_variant_info": ([C.c_int, ip, ip, ip], C.c_int),
         "gpunb_autotune": ([C.c_int, C.c_int, ip, _P(C.c_float)], C.c_int),
+        "gpunb_set_autotune": ([C.c_int], C.c_int),
+        "gpunb_set_resort_interval": ([C.c_int], C.c_int),
+        "gpunb_sort_count": ([], C.c_longlong),
         "gpunb_tune_load": ([C.c_char_p], C.c_int),
         "gpunb_tune_save": ([C.c_char_p], C.c_int),
         "gpunb_set_timing": ([C.c_int], None),
@@ -183,6 +186,17 @@ class GpuNb:
         v = self.lib.gpunb_autotune(int(ni), int(m_flag), C.byref(s), C.byref(ms))
         _check(self.lib)
         return v, s.value, ms.value
+
+    def set_autotune(self, on: bool) -> bool:
+        """gpunb_set_autotune: tune each new (N, ni) bucket on its first call's
+        own block; returns the previous setting."""
+        return bool(self.lib.gpunb_set_autotune(1 if on else 0))
+
+    def tune_save(self, path) -> int:
+        return self.lib.gpunb_tune_save(str(path).encode())
+
+    def tune_load(self, path) -> int:
+        return self.lib.gpunb_tune_load(str(path).encode())
 
     def last_launch(self):
         v, s, g = C.c_int(), C.c_int(), C.c_int()

@@ -4,7 +4,7 @@ that set alone, and bit-for-bit repeatability."""
 import numpy as np
 import pytest
 
-from conftest import rel_vec_err, rows_equal
+from conftest import check_split, rows_equal
 from nbody6ppgpu_gb300 import ics
 from oracle import oracle as O
 
@@ -58,14 +58,8 @@ def test_batch_matches_oracle_per_set(batch_case):
             if res.nnb[c][i] > 0:
                 got[i, 1:1 + len(ids)] = ids
         assert rows_equal(got, lst) == [], c
-        ok = lst[:, 0] >= 0
-        ea = rel_vec_err(res.acc[c][ok], acc[ok])
-        ep = np.abs(res.pot[c][ok] - pot[ok]) / pot[ok]
-        na = np.linalg.norm(res.acc[c][ok] - acc[ok], axis=1) / aa[ok]
-        nj = np.linalg.norm(res.jrk[c][ok] - jrk[ok], axis=1) / ja[ok]
-        assert np.percentile(ea, 99) < 1e-6 and ea.max() < 1e-5, (c, ea.max())
-        assert ep.max() < 1e-6, c
-        assert na.max() < 1e-6 and nj.max() < 1e-6, c
+        check_split(res.acc[c], res.jrk[c], res.pot[c], acc, jrk, pot, aa, ja,
+                    ok=lst[:, 0] >= 0)
 
 
 @pytest.mark.parametrize("variant", [2, 4])
@@ -100,3 +94,41 @@ def test_batch_graph_replay_matches_eager(batch_case):
                         assert np.array_equal(a, e)
         finally:
             nb.lib.gpunb_set_graphs(0)
+
+
+def test_batch_autotune_picks_a_shape_on_the_batch_and_keeps_it(batch_case, tmp_path):
+    """gpunb_set_autotune(1): the first call of a batch shape times every
+    (variant, work items per block) on that batch and keeps the fastest; the
+    results stay within the parity bound and equal a second call's bit for
+    bit, and the choice lands in the saved cache under the batch's bucket."""
+    from nbody6ppgpu_gb300.batch import DeviceBatch
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    sets, act, h2s, dtrs = batch_case
+    empty = tmp_path / "empty.txt"
+    empty.write_text("")
+    with GpuNb(1 << 16) as nb:
+        assert nb.tune_load(empty) == 0
+        prev = nb.set_autotune(True)
+        try:
+            b = DeviceBatch(sets, act, NNBMAX)
+            b.set_radii(h2s, dtrs)
+            b.send()
+            b.regf()
+            r1 = b.results()
+            plan1 = b.last_plan()
+            b.regf()
+            r2 = b.results()
+            plan2 = b.last_plan()
+        finally:
+            nb.set_autotune(prev)
+        saved = tmp_path / "tune.txt"
+        assert nb.tune_save(saved) >= 1
+    assert plan1 == plan2 and plan1[0] in (2, 4, 6)
+    key_flags = [int(l.split()[0]) >> 62 for l in saved.read_text().splitlines()]
+    assert 1 in key_flags                       # an entry under the batch flag
+    for c, ((m, x, v), a) in enumerate(zip(sets, act)):
+        assert np.array_equal(r1.acc[c], r2.acc[c]) and np.array_equal(r1.nnb[c], r2.nnb[c])
+        acc, jrk, pot, lst, aa, ja = O.regf_fp64(m, x, v, h2s[c], dtrs[c], x[a], v[a],
+                                                 NNBMAX + 1, NNBMAX, with_abs=True)
+        assert np.array_equal(np.asarray(r1.nnb[c]), lst[:, 0]), c
+        check_split(r1.acc[c], r1.jrk[c], r1.pot[c], acc, jrk, pot, aa, ja, ok=lst[:, 0] >= 0)
