@@ -645,6 +645,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-large", action="store_true", help="skip the N = 2^20 King leg")
     ap.add_argument("--no-irregular", action="store_true", help="skip the irregular-force leg")
+    ap.add_argument("--tune-save", default=None,
+                    help="save the autotuner's cache here at the end (GPUNB_TUNE_CACHE=path "
+                         "loads it in a later run, which then tunes nothing)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     ws, rank, local = dist_env()
@@ -935,6 +938,8 @@ def main():
         line["irregular"] = irr
     line["potential"] = pot
     line["rs_predictor_inference"] = rsp
+    if args.tune_save:
+        lib.gpunb_tune_save(args.tune_save.encode())
     if rank == 0:
         print(json.dumps(line, default=_jsonable), flush=True)
     if dist:

@@ -89,8 +89,70 @@ def run(model="king", n=16384, ticks=64, nnbopt=100, nnbmax=200, levels=6, epoch
     return out
 
 
+def config5(ticks_harvest=48, ticks_eval=48, n_king=1 << 20, n_plummer=65536, nnbopt=100,
+            nnbmax=200, levels=6, epochs=25, q=0.1, band=PRED_BAND, eval_seed=41,
+            max_pairs=2_000_000):
+    """The learned-radius configuration: training pairs harvested with the
+    plain rule on a Plummer/Kroupa cluster of n_plummer bodies (the bench's
+    cluster type) and on a King W0 = 6 model of n_king bodies, pooled (at most
+    max_pairs, drawn evenly), the MLP trained on the GPU kernels, then a
+    further King model of n_king bodies run from the same state with the plain
+    rule and with the predictor (plain-rule fallback outside the band):
+    overflow recomputes after the first block, membership, regular-call time.
+    q < 1/2 starts the clusters cold, so that they contract and lists
+    overflow."""
+    t0 = time.perf_counter()
+    X, Y, sources = [], [], {}
+    for name, model, n, seed in (("plummer", "plummer", n_plummer, 21),
+                                 ("king", "king", n_king, 22)):
+        h = Harness(make(model, n, seed, nnbopt, q), nnbopt, nnbmax, harvest=True, levels=levels,
+                    band=band)
+        h.run(ticks_harvest)
+        x, y = h.dataset()
+        h.close()
+        X.append(x)
+        Y.append(y)
+        sources[name] = {"n": n, "seed": seed, "pairs": int(len(x))}
+    X = np.concatenate(X)
+    Y = np.concatenate(Y)
+    if len(X) > max_pairs:
+        keep = np.linspace(0, len(X) - 1, max_pairs).astype(int)
+        X, Y = X[keep], Y[keep]
+    t_harvest = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mlp = RSMLP(seed=3)
+    losses = mlp.train(X, Y, epochs=epochs)
+    t_train = time.perf_counter() - t0
+    c = make("king", n_king, eval_seed, nnbopt, q)
+    out = {"config": "config 5: King W0=6 evaluation model, pairs from Plummer/Kroupa and King",
+           "n_eval": n_king, "q": q, "ticks_harvest": ticks_harvest, "ticks_eval": ticks_eval,
+           "band": band, "nnbopt": nnbopt, "nnbmax": nnbmax, "levels": levels,
+           "harvest_sources": sources, "train_pairs": int(len(X)),
+           "label_variance": float(Y.var()), "train_mse_first_epoch": losses[0],
+           "train_mse_last_epoch": losses[-1], "harvest_s": t_harvest, "train_s": t_train}
+    for name, pred in (("plain", None), ("predictor", mlp)):
+        t0 = time.perf_counter()
+        h = Harness(c, nnbopt, nnbmax, levels=levels, band=band)
+        s = h.run(ticks_eval, predictor=pred).as_dict()
+        h.close()
+        out[name] = {k: s[k] for k in ("first_call_overflows", "overflow_events",
+                                       "overflow_after_predictor", "active",
+                                       "recompute_rate", "mean_count", "count_p99",
+                                       "regf_seconds", "predict_seconds", "predictor_used",
+                                       "predictor_fallback")}
+        out[name]["wall_s"] = time.perf_counter() - t0
+    p_, q_ = out["plain"]["overflow_events"], out["predictor"]["overflow_events"]
+    out["overflow_recompute_ratio_plain_over_predictor"] = (p_ / q_) if q_ else (
+        None if p_ == 0 else float("inf"))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--config5", action="store_true",
+                    help="the config-5 protocol (pairs from Plummer and King runs, evaluation "
+                         "on a King model of --n bodies)")
+    ap.add_argument("--ticks-harvest", type=int, default=48)
     ap.add_argument("--model", default="king", choices=["king", "plummer"])
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--ticks", type=int, default=64)
@@ -104,6 +166,11 @@ def main():
     ap.add_argument("--band", type=float, nargs=2, default=PRED_BAND,
                     help="accept a prediction whose implied count lies in [lo, hi] x target")
     a = ap.parse_args()
+    if a.config5:
+        print(json.dumps(config5(a.ticks_harvest, a.ticks, n_king=a.n, nnbopt=a.nnbopt,
+                                 nnbmax=a.nnbmax, levels=a.levels, epochs=a.epochs, q=a.q,
+                                 band=tuple(a.band))), flush=True)
+        return
     print(json.dumps(run(a.model, a.n, a.ticks, a.nnbopt, a.nnbmax, a.levels, epochs=a.epochs,
                          q=a.q, rounds=a.rounds, band=tuple(a.band))), flush=True)
 

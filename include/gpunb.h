@@ -267,6 +267,23 @@ int gpunb_rsmlp_backward(int B, const float *X, const float *T, const float *W, 
 int gpunb_rsmlp_adam(float *wf, float *m1, float *m2, const float *grad, float lr, float beta1,
                      float beta2, float eps, int step, void *wq, void *stream);
 
+/* Training labels of the predictor on the device.  For particle i < ni
+ * (position xi, velocity vi, regular step dtr[i], target membership k[i] >=
+ * 1): logr[i] = log R_i with R_i^2 the geometric mean of the k-th and
+ * (k+1)-th smallest keys min(|dx|^2, |dx + dtr dv|^2) over the j-set xj, vj
+ * (the body itself first, key 0) -- the radius at which the regular force's
+ * own membership test admits exactly k[i] bodies besides i.  The keys are
+ * read from rows of the library's neighbour list taken at an enlarged radius
+ * (list_off, list, nnb as written by gpunb_regf_device, ids into xj/vj):
+ * ok[i] = 1 when the row held at least k[i] + 2 members (the label is then
+ * exact), 0 when it held fewer and -1 when it overflowed or held more than
+ * 1024 (retry those rows with a larger / smaller radius).  Device pointers,
+ * asynchronous on `stream`. */
+int gpunb_rsmlp_label_device(int ni, const int *list_off, const int *list, const int *nnb,
+                             const double *xj, const double *vj, const double *xi,
+                             const double *vi, const double *dtr, const int *k, double *logr,
+                             int *ok, void *stream);
+
 /* RS update of an active block on the device (no reference counterpart: the
  * reference runs src/Main/regcor_gpu.F:120-253 on the host, one particle at a
  * time).  Plain rule as regcor_gpu.F (with the few-member rule of
@@ -313,8 +330,12 @@ int gpunb_rs_update_device(int ni, const gpunb_rs_params *p, const double *x, co
  * done here: XTRNLF, FCLOUD, CHECKL, FPCORR and the tidal energy ETIDE.
  * All state arrays are device memory in the Fortran COMMON layout of all
  * NTOT bodies (index I-1; vectors as [NTOT][3]); list is LIST(LMAX,NTOT)
- * as [NTOT][lmax] with 1-based members.  The active bodies must be distinct.
- * Asynchronous on `stream`; returns 0 or GPUNB_E_ARG. */
+ * as [NTOT][lmax] with 1-based members.  The active bodies must be distinct;
+ * the small-step tests read the neighbours' STEP as it was when the call
+ * started (the reference's OpenMP loop leaves open whether a neighbour in
+ * the same block has already changed its own).  Asynchronous on `stream`;
+ * returns 0, GPUNB_E_ARG or GPUNB_E_ALLOC (a grow-only scratch of ni doubles
+ * for the new steps). */
 typedef struct {
   double time;              /* TIME */
   double dtmin, smin, smax; /* DTMIN, SMIN, SMAX */

@@ -31,6 +31,13 @@
 #define GPUNB_NEAR_K2 4.0f
 #endif
 
+// The FP32 chunk sums of the pair loop are folded into the float-float
+// accumulators every GPUNB_FOLD_TILES tiles (64 terms per f32x2 half per
+// tile).
+#ifndef GPUNB_FOLD_TILES
+#define GPUNB_FOLD_TILES 1
+#endif
+
 namespace gpunb {
 
 // ---------------------------------------------------------------------------
@@ -607,17 +614,19 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
                                           out);
         }
       }
-      // fold the tile's FP32 chunk sums into the float-float accumulators
+      // fold the FP32 chunk sums into the float-float accumulators
+      if (GPUNB_FOLD_TILES == 1 || (t + 1) % GPUNB_FOLD_TILES == 0 || t + 1 == nt) {
 #pragma unroll
-      for (int k = 0; k < IPT; ++k) {
+        for (int k = 0; k < IPT; ++k) {
 #pragma unroll
-        for (int c = 0; c < NQ; ++c) {
-          float &hi = ffs[((0 * NQ + c) * IPT + k) * NT + tid];
-          float &lo = ffs[((1 * NQ + c) * IPT + k) * NT + tid];
-          float h = hi, l = lo;
-          ff_accum(h, l, __fadd_rn(q[k][c].x, q[k][c].y));
-          hi = h; lo = l;
-          q[k][c] = make_float2(0.f, 0.f);
+          for (int c = 0; c < NQ; ++c) {
+            float &hi = ffs[((0 * NQ + c) * IPT + k) * NT + tid];
+            float &lo = ffs[((1 * NQ + c) * IPT + k) * NT + tid];
+            float h = hi, l = lo;
+            ff_accum(h, l, __fadd_rn(q[k][c].x, q[k][c].y));
+            hi = h; lo = l;
+            q[k][c] = make_float2(0.f, 0.f);
+          }
         }
       }
       // release the stage; the last warp out refills it with tile t + NSTAGE
@@ -730,14 +739,23 @@ __global__ void __launch_bounds__(128) regf_fp64_kernel(const JSet js, const ISe
         record_neighbour(out, i, jb + jj);
         continue;
       }
-      const double dr2i = 1.0 / r2;
-      const double dr3i = sm[jj] * dr2i * sqrt(dr2i);
+      // 1/r from the FP32 estimate and two Newton steps in FP64 (relative
+      // error below 2^-80 before rounding: FP64-exact to a few ulp) instead of
+      // an FP64 division and square root, which cost about as many FP64
+      // instructions as the rest of the pair on a part whose FP64 pipe runs
+      // at 1/64 of the FP32 rate
+      double y = (double)rsqrt_est((float)r2);
+      y = fma(0.5 * y, fma(-r2 * y, y, 1.0), y);
+      y = fma(0.5 * y, fma(-r2 * y, y, 1.0), y);
+      const double dr2i = y * y;
+      const double mr = sm[jj] * y;              // m/r
+      const double dr3i = mr * dr2i;             // m/r^3
       const double drdp = 3.0 * (dx * dvx + dy * dvy + dz * dvz) * dr2i;
       ax += dx * dr3i; ay += dy * dr3i; az += dz * dr3i;
       jx += (dvx - dx * drdp) * dr3i;
       jy += (dvy - dy * drdp) * dr3i;
       jz += (dvz - dz * drdp) * dr3i;
-      po += dr3i * r2;
+      po += mr;
     }
   }
   if (valid) {

@@ -11,11 +11,14 @@
 // The kernels read the weight matrices from the BF16 copy and the biases
 // from the FP32 copy.  Samples are rows of X[B][8] (normalised features).
 //
-// Kernels use CUDA cores: a 64-wide layer is far below the size at which the
-// tensor-core pipeline (TMEM allocation, descriptors, 128-wide tiles) pays
-// off; one sample per thread with the weights broadcast from shared memory
-// runs a 2^20-sample inference in well under a millisecond.
+// Inference (gpunb_rsmlp_forward) runs its two matrix layers on the tensor
+// cores (mma.sync BF16 tiles of 16 samples, FP32 accumulation, FP32 inputs
+// and activations as two-term BF16 splits); the fused RS update evaluates
+// the network per particle on the CUDA cores (mlp_eval), and training
+// (gpunb_rsmlp_backward) likewise.
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 #include "common.cuh"
 #include "rsrule.cuh"
@@ -81,17 +84,204 @@ __device__ __forceinline__ float mlp_eval(const MlpSmem &s, const float (&x)[MLP
   return out;
 }
 
-__global__ void __launch_bounds__(MLP_THREADS)
-    rsmlp_forward_kernel(int B, const float *__restrict__ X, const __nv_bfloat16 *__restrict__ wq,
-                         const float *__restrict__ wf, float *__restrict__ y) {
-  __shared__ MlpSmem s;
-  stage_params(s, wq, wf);
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  float x[MLP_IN];
+// ---------------------------------------------------------------------------
+// Tensor-core forward pass (mma.sync m16n8k16, BF16 operands, FP32
+// accumulation), 16 samples per warp tile.
+//
+// Layer 1 takes X (16 samples x 8 features, padded to K = 16) as the A
+// operand and W1 (BF16) as B; its D fragments (rows g, g+8 of the tile, two
+// adjacent hidden columns per n8 tile) are laid out exactly as the A
+// fragments of layer 2 (n8 tiles 2s and 2s+1 form k-slice s), so the hidden
+// activations never leave registers.  FP32 values enter as a two-term BF16
+// split, v = hi + lo with hi = bf16(v), lo = bf16(v - hi) (relative error
+// below 2^-17), each term in its own MMA against the exact BF16 weight: the
+// result matches FP32 arithmetic on the same BF16 weights to about 1e-5.
+// Layer 3 (64 -> 1) is a dot product of each lane's hidden columns with W3,
+// reduced over the four lanes of a quad.
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                               uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// two floats as one bf16x2 word (the first in the low half: the lower column)
+__device__ __forceinline__ uint32_t bf16x2_bits(float x, float y) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(x, y);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// the two-term BF16 split of (x, y): hi word and lo word
+__device__ __forceinline__ void split_bf16x2(float x, float y, uint32_t &hi, uint32_t &lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(x, y);
+  const float rx = x - __low2float(h), ry = y - __high2float(h);
+  hi = *reinterpret_cast<const uint32_t *>(&h);
+  lo = bf16x2_bits(rx, ry);
+}
+
+constexpr int TC_WARPS = 4;
+constexpr int W2_STRIDE = MLP_H / 2 + 4;   // bf16x2 words per padded W2 row (conflict-free B loads)
+
+struct MlpTcSmem {
+  uint32_t w1[MLP_H * MLP_IN / 2];     // W1[o][f] as bf16x2 words, 4 per row
+  uint32_t w2[MLP_H * W2_STRIDE];      // W2[o][k] as bf16x2 words, padded rows
+  float b1[MLP_H], b2[MLP_H], w3[MLP_H];
+  float b3;
+};
+
+__global__ void __launch_bounds__(32 * TC_WARPS)
+    rsmlp_forward_tc_kernel(int B, const float *__restrict__ X,
+                            const __nv_bfloat16 *__restrict__ wq, const float *__restrict__ wf,
+                            float *__restrict__ y) {
+  __shared__ __align__(16) MlpTcSmem s;
+  const uint32_t *wq32 = reinterpret_cast<const uint32_t *>(wq);   // OFF_W1, OFF_W2 even
+  for (int k = threadIdx.x; k < MLP_H * MLP_IN / 2; k += blockDim.x)
+    s.w1[k] = wq32[OFF_W1 / 2 + k];
+  for (int k = threadIdx.x; k < MLP_H * MLP_H / 2; k += blockDim.x) {
+    const int o = k / (MLP_H / 2), kk = k % (MLP_H / 2);
+    s.w2[o * W2_STRIDE + kk] = wq32[OFF_W2 / 2 + k];
+  }
+  for (int k = threadIdx.x; k < MLP_H; k += blockDim.x) {
+    s.b1[k] = wf[OFF_B1 + k];
+    s.b2[k] = wf[OFF_B2 + k];
+    s.w3[k] = __bfloat162float(wq[OFF_W3 + k]);
+  }
+  if (threadIdx.x == 0) s.b3 = wf[OFF_B3];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int ntile = (B + 15) / 16;
+  for (int tile = blockIdx.x * TC_WARPS + warp; tile < ntile; tile += gridDim.x * TC_WARPS) {
+    const int r0 = tile * 16 + g, r1 = r0 + 8;
+    float2 x0 = make_float2(0.f, 0.f), x1 = make_float2(0.f, 0.f);
+    if (r0 < B) x0 = *reinterpret_cast<const float2 *>(X + (size_t)r0 * MLP_IN + 2 * t);
+    if (r1 < B) x1 = *reinterpret_cast<const float2 *>(X + (size_t)r1 * MLP_IN + 2 * t);
+    uint32_t xa_hi[4] = {0u, 0u, 0u, 0u}, xa_lo[4] = {0u, 0u, 0u, 0u};
+    split_bf16x2(x0.x, x0.y, xa_hi[0], xa_lo[0]);   // row g, features 2t, 2t+1
+    split_bf16x2(x1.x, x1.y, xa_hi[1], xa_lo[1]);   // row g+8
+    // layer 1 -> the A fragments of layer 2 (k-slice s from n-tiles 2s, 2s+1)
+    uint32_t ha_hi[4][4], ha_lo[4][4];
 #pragma unroll
-  for (int f = 0; f < MLP_IN; ++f) x[f] = X[(size_t)b * MLP_IN + f];
-  y[b] = mlp_eval(s, x);
+    for (int j = 0; j < MLP_H / 8; ++j) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      const uint32_t b0 = s.w1[(8 * j + g) * (MLP_IN / 2) + t];
+      mma_bf16_16816(c, xa_hi, b0, 0u);
+      mma_bf16_16816(c, xa_lo, b0, 0u);
+      const int col = 8 * j + 2 * t;
+      const float h0 = gelu(c[0] + s.b1[col]), h1 = gelu(c[1] + s.b1[col + 1]);
+      const float h2 = gelu(c[2] + s.b1[col]), h3 = gelu(c[3] + s.b1[col + 1]);
+      const int sl = j >> 1, q = (j & 1) * 2;
+      split_bf16x2(h0, h1, ha_hi[sl][q], ha_lo[sl][q]);
+      split_bf16x2(h2, h3, ha_hi[sl][q + 1], ha_lo[sl][q + 1]);
+    }
+    // layers 2 and 3
+    float p0 = 0.f, p1 = 0.f;
+#pragma unroll
+    for (int j = 0; j < MLP_H / 8; ++j) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      const uint32_t *wrow = s.w2 + (8 * j + g) * W2_STRIDE;
+#pragma unroll
+      for (int sl = 0; sl < MLP_H / 16; ++sl) {
+        const uint32_t b0 = wrow[8 * sl + t], b1 = wrow[8 * sl + 4 + t];
+        mma_bf16_16816(c, ha_hi[sl], b0, b1);
+        mma_bf16_16816(c, ha_lo[sl], b0, b1);
+      }
+      const int col = 8 * j + 2 * t;
+      p0 = fmaf(gelu(c[0] + s.b2[col]), s.w3[col], p0);
+      p0 = fmaf(gelu(c[1] + s.b2[col + 1]), s.w3[col + 1], p0);
+      p1 = fmaf(gelu(c[2] + s.b2[col]), s.w3[col], p1);
+      p1 = fmaf(gelu(c[3] + s.b2[col + 1]), s.w3[col + 1], p1);
+    }
+    p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
+    p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
+    p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
+    p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
+    if (t == 0) {
+      if (r0 < B) y[r0] = p0 + s.b3;
+      if (r1 < B) y[r1] = p1 + s.b3;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Training labels on the device.  For particle i with target membership k_i:
+// log R with R^2 the geometric mean of the k-th and (k+1)-th smallest keys
+// q_j = min(|dx|^2, |dx + dtr_i dv|^2) over the j-set (position 0: the body
+// itself, q = 0), dx = x_j - x_i, dv = v_j - v_i -- the radius at which the
+// kernel's own membership test min(r^2, r_p^2) < R^2 admits exactly k_i
+// bodies besides i.  The keys come from the library's own neighbour rows at
+// an enlarged radius (list_off/list of gpunb_regf_device): every key below
+// that radius is in the row, so when the row holds at least k_i + 2 members
+// the two keys are exact.  One warp per row, keys sorted in shared memory.
+constexpr int LABEL_WARPS = 4;
+constexpr int LABEL_MAXROW = 1024;
+
+__global__ void __launch_bounds__(32 * LABEL_WARPS)
+    rsmlp_label_kernel(int ni, const int *__restrict__ list_off, const int *__restrict__ list,
+                       const int *__restrict__ nnb, const double *__restrict__ xj,
+                       const double *__restrict__ vj, const double *__restrict__ xi,
+                       const double *__restrict__ vi, const double *__restrict__ dtr,
+                       const int *__restrict__ k, double *__restrict__ logr,
+                       int *__restrict__ ok) {
+  __shared__ double keys[LABEL_WARPS][LABEL_MAXROW];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * LABEL_WARPS + w;
+  if (i >= ni) return;
+  double *q = keys[w];
+  const int cnt = nnb[i];
+  const int ki = k[i];
+  if (cnt < 0 || cnt > LABEL_MAXROW || ki < 1 || cnt < ki + 2) {
+    if (lane == 0) {
+      ok[i] = cnt < 0 || cnt > LABEL_MAXROW ? -1 : 0;   // -1: too many, 0: too few
+      logr[i] = 0.0;
+    }
+    return;
+  }
+  const int *row = list + list_off[i];
+  const double x0 = xi[3 * (size_t)i], x1 = xi[3 * (size_t)i + 1], x2 = xi[3 * (size_t)i + 2];
+  const double v0 = vi[3 * (size_t)i], v1 = vi[3 * (size_t)i + 1], v2 = vi[3 * (size_t)i + 2];
+  const double d = dtr[i];
+  int n2 = 32;
+  while (n2 < cnt) n2 <<= 1;
+  for (int e = lane; e < n2; e += 32) {
+    double key = INFINITY;
+    if (e < cnt) {
+      const int j = row[e];
+      const double dx = xj[3 * (size_t)j] - x0, dy = xj[3 * (size_t)j + 1] - x1,
+                   dz = xj[3 * (size_t)j + 2] - x2;
+      const double px = dx + d * (vj[3 * (size_t)j] - v0);
+      const double py = dy + d * (vj[3 * (size_t)j + 1] - v1);
+      const double pz = dz + d * (vj[3 * (size_t)j + 2] - v2);
+      key = fmin(dx * dx + dy * dy + dz * dz, px * px + py * py + pz * pz);
+    }
+    q[e] = key;
+  }
+  __syncwarp();
+  // bitonic sort of n2 keys, ascending
+  for (int size = 2; size <= n2; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int e = lane; e < n2; e += 32) {
+        const int p = e ^ stride;
+        if (p > e) {
+          const bool up = (e & size) == 0;
+          const double a = q[e], b = q[p];
+          if ((a > b) == up) {
+            q[e] = b;
+            q[p] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if (lane == 0) {
+    const double lo = fmax(q[ki], 1e-300);
+    const double hi = fmax(q[ki + 1], lo);
+    logr[i] = 0.25 * (log(lo) + log(hi));
+    ok[i] = 1;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -312,8 +502,15 @@ int gpunb_rsmlp_to_bf16(const float *wf, void *wq, void *stream) {
 int gpunb_rsmlp_forward(int B, const float *X, const void *wq, const float *wf, float *y,
                         void *stream) {
   if (B <= 0) return B == 0 ? GPUNB_OK : GPUNB_E_ARG;
-  rsmlp_forward_kernel<<<(B + MLP_THREADS - 1) / MLP_THREADS, MLP_THREADS, 0,
-                         (cudaStream_t)stream>>>(B, X, (const __nv_bfloat16 *)wq, wf, y);
+  // one warp per 16-sample tile, a grid of a few blocks per SM
+  int dev = 0, n_sm = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  const long long tiles = (B + 15) / 16;
+  const long long want = (tiles + TC_WARPS - 1) / TC_WARPS;
+  const int grid = (int)std::max(1ll, std::min(want, 8ll * n_sm));
+  rsmlp_forward_tc_kernel<<<grid, 32 * TC_WARPS, 0, (cudaStream_t)stream>>>(
+      B, X, (const __nv_bfloat16 *)wq, wf, y);
   return cudaGetLastError() == cudaSuccess ? GPUNB_OK : GPUNB_E_CUDA;
 }
 
@@ -339,6 +536,20 @@ int gpunb_rsmlp_adam(float *wf, float *m1, float *m2, const float *grad, float l
   const float bc1 = 1.f - powf(beta1, (float)step), bc2 = 1.f - powf(beta2, (float)step);
   rsmlp_adam_kernel<<<(MLP_P + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
       wf, m1, m2, grad, lr, beta1, beta2, eps, bc1, bc2, (__nv_bfloat16 *)wq);
+  return cudaGetLastError() == cudaSuccess ? GPUNB_OK : GPUNB_E_CUDA;
+}
+
+int gpunb_rsmlp_label_device(int ni, const int *list_off, const int *list, const int *nnb,
+                             const double *xj, const double *vj, const double *xi,
+                             const double *vi, const double *dtr, const int *k, double *logr,
+                             int *ok, void *stream) {
+  if (ni < 0 || (ni > 0 && (!list_off || !list || !nnb || !xj || !vj || !xi || !vi || !dtr ||
+                            !k || !logr || !ok)))
+    return GPUNB_E_ARG;
+  if (ni == 0) return GPUNB_OK;
+  rsmlp_label_kernel<<<(ni + LABEL_WARPS - 1) / LABEL_WARPS, 32 * LABEL_WARPS, 0,
+                       (cudaStream_t)stream>>>(ni, list_off, list, nnb, xj, vj, xi, vi, dtr, k,
+                                               logr, ok);
   return cudaGetLastError() == cudaSuccess ? GPUNB_OK : GPUNB_E_CUDA;
 }
 

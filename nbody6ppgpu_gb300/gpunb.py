@@ -70,6 +70,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "gpunb_autotune": ([C.c_int, C.c_int, ip, _P(C.c_float)], C.c_int),
         "gpunb_set_autotune": ([C.c_int], C.c_int),
         "gpunb_set_resort_interval": ([C.c_int], C.c_int),
+        "gpunb_rsmlp_label_device": ([C.c_int] + [C.c_void_p] * 12, C.c_int),
         "gpunb_sort_count": ([], C.c_longlong),
         "gpunb_tune_load": ([C.c_char_p], C.c_int),
         "gpunb_tune_save": ([C.c_char_p], C.c_int),

@@ -14,7 +14,8 @@ kick-drift-kick leapfrog on the smallest regular step.
 Training pairs: the features of a particle at one regular step, and as label
 log(RS_k / RS), RS_k the radius that gives it exactly k neighbours at its next
 regular step under the kernel's membership test (position or predicted
-position inside RS, `label_log_radius`), k the membership the plain rule aims
+position inside RS; `label_log_radius_gpu` on the device from the library's
+own rows, `label_log_radius` with KD-trees on the host), k the membership the plain rule aims
 at for it (regcor_gpu.F:152-163: NNBOPT-stabilised, tapered outside the
 half-mass radius).  The rule approaches that membership by at
 most 25% in volume per step; the predictor proposes the radius for it
@@ -107,6 +108,76 @@ def label_log_radius(x: np.ndarray, v: np.ndarray, dtr: np.ndarray, idx: np.ndar
     return out
 
 
+LABEL_ROW_MAX = 1024     # longest row the device labeller sorts (gpunb_rsmlp_label_device)
+
+
+def label_log_radius_gpu(nb: GpuNb, x: np.ndarray, v: np.ndarray, dtr: np.ndarray,
+                         idx: np.ndarray, ks: np.ndarray, r_hint: np.ndarray) -> np.ndarray:
+    """The labels of `label_log_radius`, computed on the device from the
+    library's own neighbour rows: the j-set must be the one last sent to `nb`
+    (positions x, velocities v).  Each row is taken at a radius 1.3 r_hint
+    (r_hint: an estimate of R_k, e.g. RS (k+2)^(1/3) / (count+1)^(1/3)),
+    doubled for the rows that hold fewer than k + 2 members and shrunk for
+    those above LABEL_ROW_MAX, until every row qualifies; the keys of a
+    qualifying row are exact, so the labels equal the KD-tree ones."""
+    import torch
+    lib = nb.lib
+    fn = lib.gpunb_rsmlp_label_device
+    dev = torch.device("cuda", 0)
+    xd = torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)
+    vd = torch.as_tensor(np.ascontiguousarray(v), dtype=torch.float64, device=dev)
+    out = np.full(idx.size, np.nan)
+    todo = np.arange(idx.size)
+    scale = np.full(idx.size, 1.3)
+    nnbmax = LABEL_ROW_MAX
+    for _ in range(40):
+        if todo.size == 0:
+            break
+        ii = idx[todo]
+        ni = ii.size
+        r = scale[todo] * r_hint[todo]
+        h2 = torch.as_tensor(r * r, dtype=torch.float64, device=dev)
+        dt = torch.as_tensor(dtr[ii], dtype=torch.float64, device=dev)
+        sel = torch.as_tensor(ii, device=dev)
+        xi = xd[sel].contiguous()
+        vi = vd[sel].contiguous()
+        acc = torch.empty((ni, 3), dtype=torch.float64, device=dev)
+        jrk = torch.empty_like(acc)
+        pot = torch.empty(ni, dtype=torch.float64, device=dev)
+        nnb = torch.empty(ni, dtype=torch.int32, device=dev)
+        off = torch.empty(ni + 1, dtype=torch.int32, device=dev)
+        lst = torch.empty(ni * nnbmax, dtype=torch.int32, device=dev)
+        kd = torch.as_tensor(ks[todo].astype(np.int32), device=dev)
+        logr = torch.empty(ni, dtype=torch.float64, device=dev)
+        ok = torch.empty(ni, dtype=torch.int32, device=dev)
+        torch.cuda.synchronize()
+        rc = lib.gpunb_regf_device(ni, h2.data_ptr(), dt.data_ptr(), xi.data_ptr(),
+                                   vi.data_ptr(), acc.data_ptr(), jrk.data_ptr(), pot.data_ptr(),
+                                   nnb.data_ptr(), off.data_ptr(), lst.data_ptr(), ni * nnbmax,
+                                   nnbmax, 0, None)
+        if rc != 0:
+            raise RuntimeError(f"gpunb_regf_device failed ({rc})")
+        # the regf call ran on the library's own stream: wait for it (and read
+        # its error word) before the labeller runs on the default stream
+        if lib.gpunb_device_status(None) != 0:
+            raise RuntimeError("device error in the regular-force pass of the labeller")
+        rc = fn(ni, off.data_ptr(), lst.data_ptr(), nnb.data_ptr(), xd.data_ptr(), vd.data_ptr(),
+                xi.data_ptr(), vi.data_ptr(), dt.data_ptr(), kd.data_ptr(), logr.data_ptr(),
+                ok.data_ptr(), None)
+        if rc != 0:
+            raise RuntimeError(f"gpunb_rsmlp_label_device failed ({rc})")
+        torch.cuda.synchronize()
+        okh = ok.cpu().numpy()
+        good = okh == 1
+        out[todo[good]] = logr.cpu().numpy()[good]
+        scale[todo[okh == 0]] *= 2.0
+        scale[todo[okh == -1]] *= 0.8
+        todo = todo[~good]
+    if todo.size:
+        raise RuntimeError(f"{todo.size} labels did not converge")
+    return out
+
+
 # accepted range of the count a predicted radius implies at the current
 # density, as a multiple of the plain rule's target (the device update kernel
 # takes the same bounds): 0.5-1.5 by default; WIDE_BAND lowers the floor so
@@ -120,8 +191,9 @@ class Harness:
     def __init__(self, cluster: ics.Cluster, nnbopt: int, nnbmax: int, smax: float = 0.125,
                  levels: int = 4, params: rsrule.RSParams | None = None, rs=None,
                  harvest: bool = False, rs0_factor: float = 1.0,
-                 band: tuple[float, float] = PRED_BAND):
+                 band: tuple[float, float] = PRED_BAND, gpu_labels: bool = True):
         self.c = cluster
+        self.gpu_labels = gpu_labels   # labels from the device labeller (else KD-tree)
         self.band = band
         self.n = cluster.n
         self.nnbopt, self.nnbmax = nnbopt, nnbmax
@@ -252,7 +324,12 @@ class Harness:
         if have.size == 0:
             return
         ks = np.array([int(min(max(round(self.pending[i][2]), 1), self.n - 3)) for i in have])
-        logr = label_log_radius(self.x, self.v, self.stepr, have, ks)
+        if self.gpu_labels and ks.max() + 2 <= LABEL_ROW_MAX:
+            cnt = np.maximum(self.prev_nnb[have], 0) + 1.0
+            hint = self.rs[have] * np.cbrt((ks + 2.0) / cnt)
+            logr = label_log_radius_gpu(self.nb, self.x, self.v, self.stepr, have, ks, hint)
+        else:
+            logr = label_log_radius(self.x, self.v, self.stepr, have, ks)
         for q, i in enumerate(have):
             f, rs_then, _ = self.pending.pop(int(i))
             self.X.append(f)

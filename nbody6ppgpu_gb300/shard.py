@@ -69,17 +69,17 @@ def merge_j_parts(parts: Sequence[RegfResult], joff: Sequence[int], nnbmax: int)
         acc += p.acc
         jrk += p.jrk
         pot += p.pot
-    counts = np.stack([np.abs(p.list[:, 0]) for p in parts])      # [size, ni]
+    counts = np.stack([np.abs(p.list[:, 0]) for p in parts]).astype(np.int64)   # [size, ni]
     total = counts.sum(0)
     over = total > nnbmax
     out = np.zeros((ni, lmax), dtype=np.int32)
     out[:, 0] = np.where(over, -total, total)
-    for i in np.nonzero(~over)[0]:
-        o = 1
-        for r, p in enumerate(parts):
-            c = int(counts[r, i])
-            out[i, o:o + c] = p.list[i, 1:1 + c] + int(joff[r])
-            o += c
+    # rank r's members of row i go to columns 1 + (members of ranks < r) + k
+    prefix = np.cumsum(counts, axis=0) - counts
+    k = np.arange(lmax - 1)
+    for r, p in enumerate(parts):
+        rows, cols = np.nonzero((k[None, :] < counts[r][:, None]) & ~over[:, None])
+        out[rows, 1 + prefix[r, rows] + cols] = p.list[rows, 1 + cols] + int(joff[r])
     return RegfResult(acc=acc, jrk=jrk, pot=pot, list=out)
 
 
@@ -108,21 +108,36 @@ class ShardedRegf:
 
     def i_split(self, h2, dtr, xi, vi, lmax: int, nnbmax: int, m_flag: int = 0) -> RegfResult:
         """Every rank returns all ni rows; rank r computed rows
-        [start[r], start[r] + count[r])."""
+        [start[r], start[r] + count[r]).  The rows travel compact: the forces,
+        the signed counts and the accepted members only (padded to the
+        longest rank's), not lmax-wide rows."""
         ni = len(h2)
         start, count = i_split(ni, self.size)
         s, c = int(start[self.rank]), int(count[self.rank])
         cmax = int(count.max())
-        f = np.zeros((cmax, 7))
-        lst = np.zeros((cmax, lmax), dtype=np.int32)
+        f = np.zeros((cmax, 8))
+        ids = np.zeros(0, dtype=np.int32)
         if c:
             r = self.regf_fn(h2[s:s + c], dtr[s:s + c], xi[s:s + c], vi[s:s + c], lmax, nnbmax,
                              m_flag)
             f[:c, 0:3], f[:c, 3:6], f[:c, 6] = r.acc, r.jrk, r.pot
-            lst[:c] = r.list
-        fs, ls = self._all_gather(f), self._all_gather(lst)
+            f[:c, 7] = r.list[:, 0]
+            n_acc = np.maximum(r.list[:, 0], 0)
+            rows, cols = np.nonzero(np.arange(lmax - 1)[None, :] < n_acc[:, None])
+            ids = r.list[rows, 1 + cols].astype(np.int32)
+        sizes = self._all_gather(np.array([ids.size], dtype=np.int64))
+        width = int(max(int(z[0]) for z in sizes))
+        pad = np.zeros(max(width, 1), dtype=np.int32)
+        pad[:ids.size] = ids
+        fs, idss = self._all_gather(f), self._all_gather(pad)
         F = np.concatenate([fs[q][:count[q]] for q in range(self.size)])
-        L = np.concatenate([ls[q][:count[q]] for q in range(self.size)])
+        nnb = F[:, 7].astype(np.int32)
+        allids = np.concatenate([idss[q][:int(sizes[q][0])] for q in range(self.size)])
+        L = np.zeros((ni, lmax), dtype=np.int32)
+        L[:, 0] = nnb
+        n_acc = np.maximum(nnb, 0)
+        rows, cols = np.nonzero(np.arange(lmax - 1)[None, :] < n_acc[:, None])
+        L[rows, 1 + cols] = allids
         return RegfResult(acc=F[:, 0:3].copy(), jrk=F[:, 3:6].copy(), pot=F[:, 6].copy(), list=L)
 
     def j_split(self, joff: Sequence[int], h2, dtr, xi, vi, lmax: int, nnbmax: int,

@@ -35,11 +35,14 @@ def _pair(xi, vi, xj, vj, mj):
     return [a[k] * dr3i for k in range(3)], [(dv[k] - a[k] * drdp) * dr3i for k in range(3)]
 
 
-def regcor_body(i1, freg, fdr, nlist, s, p, counters):
+def regcor_body(i1, freg, fdr, nlist, s, p, counters, step_entry=None):
     """One body I = i1 (1-based).  freg, fdr: 3-lists (modified as the
     reference modifies FREG, FDR); nlist: Python list in the LISTGP row form
-    [NNB, members...] (modified as NLIST is)."""
+    [NNB, members...] (modified as NLIST is).  step_entry: STEP of all bodies
+    as it was when the block started (default: s["step"]); the small-step
+    tests read the neighbours' STEP from it."""
     i = i1 - 1
+    step_nb = s["step"] if step_entry is None else step_entry
     lmax = p["lmax"]
     ntot = p["ntot"]
     xi = [float(s["x"][i, k]) for k in range(3)]
@@ -152,7 +155,7 @@ def regcor_body(i1, freg, fdr, nlist, s, p, counters):
                     nbloss += 1
                     j = L_[L]
                     jj[nbloss] = j
-                    if s["step"][j - 1] < p["smin"]:
+                    if step_nb[j - 1] < p["smin"]:
                         jmin = j
                     LG -= 1
             if L <= nnb0:                             # label 58
@@ -170,7 +173,7 @@ def regcor_body(i1, freg, fdr, nlist, s, p, counters):
                 if nnb > p["nnbmax"] or i1 > p["n"]:
                     break
                 j = jj[K]
-                skip = (s["step"][j - 1] > p["smin"] or j < p["ifirst"] or j > p["n"])
+                skip = (step_nb[j - 1] > p["smin"] or j < p["ifirst"] or j > p["n"])
                 if not skip:
                     rij2 = sum((xi[k] - s["x"][j - 1, k]) ** 2 for k in range(3))
                     skip = rij2 > 4.0 * rs2
@@ -292,13 +295,16 @@ def regcor_body(i1, freg, fdr, nlist, s, p, counters):
 def regcor_block(iact, freg, fdr, nlist_rows, s, p):
     """All bodies of an active block in order; freg, fdr [ni, 3] and
     nlist_rows [ni, lmax] are modified like the device corrector's inputs.
-    Returns the counters (NBVOID, NBSMIN, NBFLUX, NICONV)."""
+    The neighbours' STEP is read as it was at the start of the block (the
+    reference's OpenMP loop leaves that order open; the device corrector
+    defines it so).  Returns the counters (NBVOID, NBSMIN, NBFLUX, NICONV)."""
     counters = [0, 0, 0, 0]
+    step_entry = s["step"].copy()
     for k, i1 in enumerate(iact):
         fr = [float(v) for v in freg[k]]
         fd = [float(v) for v in fdr[k]]
         row = [int(v) for v in nlist_rows[k, :int(nlist_rows[k, 0]) + 1]]
-        regcor_body(int(i1), fr, fd, row, s, p, counters)
+        regcor_body(int(i1), fr, fd, row, s, p, counters, step_entry)
         freg[k] = fr
         fdr[k] = fd
         nlist_rows[k, :] = 0

@@ -44,7 +44,7 @@ def test_device_corrector_matches_the_host_restatement():
     h2 = c.h2()
     h2_new = h2[act].copy()
     h2_new[::37] = 1e-12                        # empty new lists
-    h2_new[5::41] *= 0.02                       # a few neighbours
+    h2_new[5::23] *= 0.2                        # a few neighbours (~25 x 0.2^1.5)
     h2_old = h2.copy()
     h2_old[act] *= np.exp(rng.normal(0.0, 0.3, act.size))   # gains and losses
     with GpuNb(ntot) as nb:

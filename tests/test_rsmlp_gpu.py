@@ -153,3 +153,23 @@ def test_predictor_cuts_overflow_recomputes():
     assert abs(pred["mean_count"] / plain["mean_count"] - 1.0) < 0.1
     assert pred["count_p99"] <= plain["count_p99"]
     assert pred["predictor_used"] > 0.9 * pred["active"]
+
+
+def test_device_labels_equal_the_kdtree_labels():
+    """The device labeller (the library's own rows at an enlarged radius, keys
+    sorted per row on the GPU) gives the KD-tree labels of the host exactly,
+    over targets from 5 to 200 members and radius hints off by up to 2x."""
+    from nbody6ppgpu_gb300 import ics
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    from nbody6ppgpu_gb300.rsharness import label_log_radius, label_log_radius_gpu
+    pytest.importorskip("scipy")
+    c = ics.plummer(20000, seed=31, masses="kroupa", nb_target=60.0)
+    idx = ics.active_set(c.n, 3000, seed=31)
+    rng = np.random.default_rng(31)
+    ks = rng.integers(5, 200, idx.size)
+    hint = c.rs[idx] * np.cbrt((ks + 2.0) / 61.0) * np.exp(rng.uniform(-0.7, 0.7, idx.size))
+    with GpuNb(c.n) as nb:
+        nb.send(c.m, c.x, c.v)
+        g = label_log_radius_gpu(nb, c.x, c.v, c.dtr, idx, ks, hint)
+    h = label_log_radius(c.x, c.v, c.dtr, idx, ks)
+    assert np.max(np.abs(g - h)) < 1e-12
