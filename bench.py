@@ -409,6 +409,10 @@ def king1m_leg(lib, dev, stream, n_sm: int, peak_mhz: float, steps: int = 2, war
     out = {"workload": "King W0=6, N=2^20, Kroupa, 10% binaries as c.m. bodies, target 100, "
                        "nbmax 1024; one step = send + regf at ni in {1024, 16384, 262144, N}",
            "setup_s": t_ics, "pairs_per_step": pairs}
+    # launch shapes: the library's measured heuristic (its sweeps were taken on
+    # this model); tuning ni = 2^20 on first sight would time ~100 passes of a
+    # one-second kernel
+    autotune_prev = lib.gpunb_set_autotune(0)
     with GpuNb(n) as nb:
         nb.set_precision("split")
         # device-resident steps, graphs on
@@ -482,6 +486,7 @@ def king1m_leg(lib, dev, stream, n_sm: int, peak_mhz: float, steps: int = 2, war
             host_step()
         e2e_s = (time.perf_counter() - t) / steps
         lib.gpunb_set_graphs(0)
+    lib.gpunb_set_autotune(autotune_prev)
     h2d = sum(56 * n + 64 * ni for ni in KING_BLOCKS)
     d2h = sum(60 * ni + 4 * int(np.maximum(outs[ni].list[:, 0], 0).sum()) for ni in KING_BLOCKS)
     a, j, p = got16

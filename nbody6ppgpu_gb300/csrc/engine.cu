@@ -640,8 +640,10 @@ static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out
       int s = (int)std::max(1ll, std::min<long long>(sc, std::max(1, js.ntile)));
       if (s == last_s) continue;
       last_s = s;
+      // one warm-up pass, then three timed ones -- or one when a pass takes
+      // longer than 20 ms (large blocks: the timing is stable, the sweep long)
       float tot = 0.f;
-      const int reps = 3;
+      int reps = 3;
       bool ok = true;
       for (int r = 0; r < reps + 1 && ok; ++r) {
         if (run_pair_pass(is, nnbmax, mflag, v, s, st, true) != GPUNB_OK) ok = false;
@@ -655,6 +657,7 @@ static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out
         float ms = 0.f;
         cudaEventElapsedTime(&ms, g.ek0, g.ek1);
         if (r > 0) tot += ms;
+        if (r == 0 && ms > 20.f) reps = 1;
       }
       if (!ok) cudaGetLastError();
       if (!ok) continue;
