@@ -22,7 +22,11 @@ namespace gpunb {
 //     (for one of them |o| < 2R and R + |o| > 3 d, d the distance to the
 //     tile's box): dx = (hi_j - hi_i) + (lo_j - lo_i), three additions per
 //     component, error 2^-23 |dx|.
-constexpr int JT = 128;
+#ifndef GPUNB_JT
+#define GPUNB_JT 128
+#endif
+constexpr int JT = GPUNB_JT;
+static_assert(JT % 64 == 0 && JT <= 1024, "a tile holds a multiple of 64 bodies");
 enum JField {
   F_XR = 0, F_YR, F_ZR, F_VX, F_VY, F_VZ, F_MN,   // far tiles read these 7
   F_XH, F_YH, F_ZH, F_XL, F_YL, F_ZL,             // near tiles: velocity, mass and these
