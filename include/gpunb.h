@@ -323,7 +323,9 @@ int gpunb_rs_update_device(int ni, const gpunb_rs_params *p, const double *x, co
  * (:120-252), the small-central-mass change for an empty list (:120-143), the
  * force changes of lost and gained neighbours with the retention of old
  * neighbours whose step is below SMIN (:262-460; a retained body is inserted
- * into nlist and the row count updated), the Hermite corrector (:462-552:
+ * into nlist and the row count updated; into an empty list as into any
+ * other, where the reference's insertion loop displaces the first kept body
+ * by the saved last old member), the Hermite corrector (:462-552:
  * XN, XNDOT, FI, FR, FIDOT, FRDOT, D0, D0R..D3R, T0R; tidal FIDOT term for
  * KZ(14) <= 2), the list copy LIST(.,I) = NLIST on a change (:608-616), the
  * new regular step STEPR and the irregular step reduction (:618-800).  Not

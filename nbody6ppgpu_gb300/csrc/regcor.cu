@@ -16,7 +16,11 @@
 //     merged in index order; an old neighbour with a step below SMIN inside
 //     2 RS is kept (its force moves from the regular to the irregular side,
 //     :360-410); the force and derivative of every lost and gained neighbour
-//     form DFIRR, DFD;
+//     form DFIRR, DFD.  One deviation: when the new list is empty, the
+//     reference's insertion loop compares against NLIST(1), which then holds
+//     the saved last old member, so the first kept body is displaced by that
+//     member and the list no longer matches the forces moved (:386-392);
+//     here a kept body enters an empty list like any other;
 //   * the Hermite corrector of the regular polynomial (:462-552): XN, XNDOT,
 //     FI, FR, FIDOT, FRDOT, D0, D0R..D3R, T0R, with the tidal FIDOT term for
 //     KZ(14) <= 2 and the corrector suppression for large step ratios;

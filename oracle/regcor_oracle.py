@@ -1,7 +1,9 @@
 """Host restatement of the reference's regular corrector REGCOR_GPU
 (src/Main/regcor_gpu.F), TEST INFRASTRUCTURE ONLY: the checker of the
 device corrector gpunb_regcor_device.  Plain Python, one body at a time, FP64,
-following the Fortran control flow line by line: the neighbour-radius rule
+following the Fortran control flow line by line (one deviation, marked where
+it occurs: the insertion of a kept neighbour into an empty new list): the
+neighbour-radius rule
 (:120-252), the list comparison with its sentinels and JJLIST bookkeeping
 (:262-330), the retention of small-step neighbours (:332-410), the force
 changes of lost and gained neighbours (:414-460), the corrector (:462-552),
@@ -179,13 +181,17 @@ def regcor_body(i1, freg, fdr, nlist, s, p, counters, step_entry=None):
                     skip = rij2 > 4.0 * rs2
                 if not skip:
                     L = nnb + 1
-                    while True:                       # label 62
+                    # With NNB = 0 the reference's loop starts at L = 1 and
+                    # compares NLIST(1), which then holds the saved last old
+                    # member: the first kept body is displaced by that member
+                    # (:386-392), leaving the list and the force split
+                    # inconsistent.  Here, as on the device, a body is
+                    # inserted into an empty list like into any other.
+                    while L > 1:                      # label 62
                         if NL[L] < j:
                             break
                         NL[L + 1] = NL[L]
                         L -= 1
-                        if not L > 1:
-                            break
                     NL[L + 1] = j                     # label 64
                     nnb += 1
                     nbloss -= 1

@@ -92,3 +92,27 @@ def test_small_step_neighbours_inside_two_radii_are_kept():
                        atol=1e-14)
     assert s["list"][i1 - 1, 0] == 4 and list(s["list"][i1 - 1, 1:5]) == [2, 3, 5, 9]
     assert math.isclose(s["t0r"][i1 - 1], 1.0)
+
+
+def test_kept_neighbours_enter_an_empty_new_list_in_order():
+    """An empty new list with small-step old neighbours inside 2 RS: they are
+    kept in ascending order, and the list matches the forces moved (the
+    reference's loop would displace the first kept body by the last old
+    member here)."""
+    rng = np.random.default_rng(9)
+    n, lmax = 40, 20
+    s = _state(n, lmax, rng)
+    p = _params(n, lmax)
+    i1 = 4
+    xi = s["x"][i1 - 1]
+    s["rs"][i1 - 1] = 0.6
+    old = [2, 3, 5, 8]
+    s["step"][[1, 4]] = 1e-4                 # bodies 2 and 5
+    s["x"][1] = xi + [0.3, 0.0, 0.0]
+    s["x"][4] = xi + [0.0, -0.4, 0.0]
+    s["list"][i1 - 1, :len(old) + 1] = [len(old)] + old
+    row = [0]
+    counters = [0, 0, 0, 0]
+    R.regcor_body(i1, list(s["fr"][i1 - 1]), list(s["frdot"][i1 - 1]), row, s, p, counters)
+    assert row == [2, 2, 5] and counters[1] == 2
+    assert list(s["list"][i1 - 1, :3]) == [2, 2, 5]
