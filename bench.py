@@ -636,7 +636,7 @@ def rs_predictor_leg(dev):
     ms = e0.elapsed_time(e1) / reps
     macs = B * (8 * 64 + 64 * 64 + 64)
     return {"particles": B, "forward_ms": ms, "gmacs_per_s": macs / (ms * 1e-3) / 1e9,
-            "kernel": "rsmlp_forward_kernel (FP32 CUDA cores, BF16 weights)"}
+            "kernel": "rsmlp_forward_tc_kernel (mma.sync BF16 tiles, FP32 accumulation)"}
 
 
 def main():

@@ -11,11 +11,11 @@
 // The kernels read the weight matrices from the BF16 copy and the biases
 // from the FP32 copy.  Samples are rows of X[B][8] (normalised features).
 //
-// Inference (gpunb_rsmlp_forward) runs its two matrix layers on the tensor
-// cores (mma.sync BF16 tiles of 16 samples, FP32 accumulation, FP32 inputs
-// and activations as two-term BF16 splits); the fused RS update evaluates
-// the network per particle on the CUDA cores (mlp_eval), and training
-// (gpunb_rsmlp_backward) likewise.
+// Inference (gpunb_rsmlp_forward) and training (gpunb_rsmlp_backward) run
+// their matrix products on the tensor cores (mma.sync BF16 tiles of 16
+// samples, FP32 accumulation, FP32 inputs and activations as two-term BF16
+// splits); the fused RS update evaluates the network per particle on the
+// CUDA cores (mlp_eval).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -348,101 +348,295 @@ __global__ void __launch_bounds__(MLP_THREADS)
   if (used) used[i] = u;
 }
 
-// Backward pass of the mean of w_b (y_b - t_b)^2 over the batch.  Each block
-// writes the gradient summed over its samples to part[blockIdx][P]; a second
-// kernel sums the block rows in order (deterministic).  Per-sample
-// activations live in dynamic shared memory (rows padded to 65 floats):
-//   sx[T][8], sh1[T][65] h1, sd1[T][65] z1 then dz1, sd2[T][65] z2 then dz2,
-//   sh2[T][65] h2.
-constexpr int LD = MLP_H + 1;
-size_t rsmlp_backward_smem() {
-  return sizeof(float) * ((size_t)MLP_THREADS * MLP_IN + 4ull * MLP_THREADS * LD + MLP_THREADS);
+// Backward pass of the mean of w_b (y_b - t_b)^2 over the batch, on the tensor
+// cores.  One block of 4 warps per 128 samples; each block writes the
+// gradient summed over its samples to part[blockIdx][P] and a second kernel
+// sums the block rows in order, so repeated calls give bit-identical
+// gradients.
+//
+// Per warp, for each of its two 16-sample tiles: the forward pass as in
+// rsmlp_forward_tc_kernel, keeping z1, z2 (D-fragment layout) and the
+// layer-2 A fragments of h1; then dy, dz2 = dy W3 gelu'(z2) and
+// dh1 = dz2 W2 -- again D fragments of one product reused as the A fragments
+// of the next, with W2 transposed in shared memory as the B operand -- and
+// dz1 = dh1 gelu'(z1).  dz2, dz1, h1 and x are staged transposed (feature
+// rows of 128 samples) as two-term BF16 splits, so that the weight gradients
+// dW2 = dz2^T h1 and dW1 = dz1^T x are block GEMMs over the 128 samples (warp
+// w owns rows 16w..16w+15), each product of splits taken as hi*hi + hi*lo +
+// lo*hi.  Bias gradients, dW3, db3 and the loss are column sums reduced over
+// the lanes, then over the warps in order.
+constexpr int BW_WARPS = 4;
+constexpr int BW_SAMPLES = 16 * 2 * BW_WARPS;           // two 16-sample tiles per warp
+constexpr int BT_STRIDE = BW_SAMPLES + 8;               // bf16 per transposed row (padded)
+static_assert(BW_SAMPLES == MLP_THREADS, "one block row of partial sums per 128 samples");
+
+struct MlpBwSmem {
+  uint32_t w1[MLP_H * MLP_IN / 2];       // W1[o][f]  bf16x2 (B of layer 1)
+  uint32_t w2[MLP_H * W2_STRIDE];        // W2[o][k]  bf16x2 (B of layer 2)
+  uint32_t w2t[MLP_H * W2_STRIDE];       // W2[o][k] as [k][o] (B of dh1 = dz2 W2)
+  float b1[MLP_H], b2[MLP_H], w3[MLP_H];
+  float b3;
+  __nv_bfloat16 dz2t[2][MLP_H][BT_STRIDE];   // [hi/lo][o][sample]
+  __nv_bfloat16 h1t[2][MLP_H][BT_STRIDE];    // [hi/lo][k][sample]
+  __nv_bfloat16 dz1t[2][MLP_H][BT_STRIDE];   // [hi/lo][k][sample]
+  __nv_bfloat16 xt[2][MLP_IN][BT_STRIDE];    // [hi/lo][f][sample]
+  float red[BW_WARPS][3][MLP_H];             // per warp: db1, db2, dW3 partial sums
+  float redy[BW_WARPS][2];                   // per warp: db3, loss
+};
+
+template <int ROWS>
+__device__ __forceinline__ void stage_split(__nv_bfloat16 (*t)[ROWS][BT_STRIDE], int row,
+                                            int col, float v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  t[0][row][col] = h;
+  t[1][row][col] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
-__global__ void __launch_bounds__(MLP_THREADS)
-    rsmlp_backward_kernel(int B, const float *__restrict__ X, const float *__restrict__ T,
-                          const float *__restrict__ Wt, const __nv_bfloat16 *__restrict__ wq,
-                          const float *__restrict__ wf, float inv_norm,
-                          float *__restrict__ part, float *__restrict__ loss_part) {
-  __shared__ MlpSmem s;
-  extern __shared__ float dyn[];
-  float *sx = dyn;
-  float *sh1 = sx + MLP_THREADS * MLP_IN;
-  float *sd1 = sh1 + MLP_THREADS * LD;
-  float *sd2 = sd1 + MLP_THREADS * LD;
-  float *sh2 = sd2 + MLP_THREADS * LD;
-  float *sdy = sh2 + MLP_THREADS * LD;
-  __shared__ float sh_red[MLP_THREADS];
-  stage_params(s, wq, wf);
-  const int t = threadIdx.x;
-  const int b = blockIdx.x * blockDim.x + t;
-  const bool valid = b < B;
-#pragma unroll
-  for (int f = 0; f < MLP_IN; ++f) sx[t * MLP_IN + f] = valid ? X[(size_t)b * MLP_IN + f] : 0.f;
-  // layer 1
-  for (int o = 0; o < MLP_H; ++o) {
-    float a = s.b1[o];
-#pragma unroll
-    for (int f = 0; f < MLP_IN; ++f) a = fmaf(s.w1[o * MLP_IN + f], sx[t * MLP_IN + f], a);
-    sd1[t * LD + o] = a;
-    sh1[t * LD + o] = gelu(a);
+__device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16 *p) {
+  return *reinterpret_cast<const uint32_t *>(p);
+}
+
+// column sums of a quad-layout value over the 8 row groups of the warp
+__device__ __forceinline__ float sum_over_rows(float v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 4);
+  v += __shfl_xor_sync(0xffffffffu, v, 8);
+  v += __shfl_xor_sync(0xffffffffu, v, 16);
+  return v;
+}
+
+// adds the warp's column sum of v to row[col] (one lane per column writes)
+__device__ __forceinline__ void add_col_sum(float *row, int col, int g, float v) {
+  v = sum_over_rows(v);
+  if (g == 0) row[col] += v;
+}
+
+__global__ void __launch_bounds__(32 * BW_WARPS)
+    rsmlp_backward_tc_kernel(int B, const float *__restrict__ X, const float *__restrict__ T,
+                             const float *__restrict__ Wt, const __nv_bfloat16 *__restrict__ wq,
+                             const float *__restrict__ wf, float inv_norm,
+                             float *__restrict__ part, float *__restrict__ loss_part) {
+  extern __shared__ __align__(16) unsigned char bw_smem_raw[];
+  MlpBwSmem &s = *reinterpret_cast<MlpBwSmem *>(bw_smem_raw);
+  const uint32_t *wq32 = reinterpret_cast<const uint32_t *>(wq);
+  for (int k = threadIdx.x; k < MLP_H * MLP_IN / 2; k += blockDim.x) s.w1[k] = wq32[OFF_W1 / 2 + k];
+  for (int k = threadIdx.x; k < MLP_H * MLP_H / 2; k += blockDim.x) {
+    const int o = k / (MLP_H / 2), kk = k % (MLP_H / 2);
+    s.w2[o * W2_STRIDE + kk] = wq32[OFF_W2 / 2 + k];
   }
-  // layer 2 and output
-  float out = s.b3;
-  for (int o = 0; o < MLP_H; ++o) {
-    float a = s.b2[o];
-    for (int k = 0; k < MLP_H; ++k) a = fmaf(s.w2[o * MLP_H + k], sh1[t * LD + k], a);
-    const float h2 = gelu(a);
-    sd2[t * LD + o] = a;
-    sh2[t * LD + o] = h2;
-    out = fmaf(s.w3[o], h2, out);
+  for (int e = threadIdx.x; e < MLP_H * MLP_H / 2; e += blockDim.x) {
+    const int k = e / (MLP_H / 2), op = e % (MLP_H / 2);   // row k, pair (2op, 2op+1) of o
+    s.w2t[k * W2_STRIDE + op] =
+        bf16x2_bits(__bfloat162float(wq[OFF_W2 + (2 * op) * MLP_H + k]),
+                    __bfloat162float(wq[OFF_W2 + (2 * op + 1) * MLP_H + k]));
   }
-  const float w = valid ? (Wt ? Wt[b] : 1.0f) : 0.f;
-  const float r = valid ? out - T[b] : 0.f;
-  const float dy = 2.0f * w * r * inv_norm;
-  sdy[t] = dy;
-  sh_red[t] = w * r * r * inv_norm;
-  // dz2 = dy W3 gelu'(z2)
-  for (int o = 0; o < MLP_H; ++o) sd2[t * LD + o] = dy * s.w3[o] * gelu_grad(sd2[t * LD + o]);
-  // dz1 = (W2^T dz2) gelu'(z1)
-  for (int k = 0; k < MLP_H; ++k) {
-    float a = 0.f;
-    for (int o = 0; o < MLP_H; ++o) a = fmaf(s.w2[o * MLP_H + k], sd2[t * LD + o], a);
-    sd1[t * LD + k] = a * gelu_grad(sd1[t * LD + k]);
+  for (int k = threadIdx.x; k < MLP_H; k += blockDim.x) {
+    s.b1[k] = wf[OFF_B1 + k];
+    s.b2[k] = wf[OFF_B2 + k];
+    s.w3[k] = __bfloat162float(wq[OFF_W3 + k]);
+  }
+  if (threadIdx.x == 0) s.b3 = wf[OFF_B3];
+  for (int k = threadIdx.x; k < BW_WARPS * 3 * MLP_H; k += blockDim.x) (&s.red[0][0][0])[k] = 0.f;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int base = blockIdx.x * BW_SAMPLES;
+  float sum_dy = 0.f, sum_loss = 0.f;
+  for (int tl = 0; tl < 2; ++tl) {
+    const int lt = 16 * (2 * warp + tl);             // tile offset within the block
+    const int r0 = base + lt + g, r1 = r0 + 8;
+    const bool v0 = r0 < B, v1 = r1 < B;
+    float2 x0 = make_float2(0.f, 0.f), x1 = make_float2(0.f, 0.f);
+    if (v0) x0 = *reinterpret_cast<const float2 *>(X + (size_t)r0 * MLP_IN + 2 * t);
+    if (v1) x1 = *reinterpret_cast<const float2 *>(X + (size_t)r1 * MLP_IN + 2 * t);
+    uint32_t xa_hi[4] = {0u, 0u, 0u, 0u}, xa_lo[4] = {0u, 0u, 0u, 0u};
+    split_bf16x2(x0.x, x0.y, xa_hi[0], xa_lo[0]);
+    split_bf16x2(x1.x, x1.y, xa_hi[1], xa_lo[1]);
+    stage_split(s.xt, 2 * t, lt + g, x0.x);
+    stage_split(s.xt, 2 * t + 1, lt + g, x0.y);
+    stage_split(s.xt, 2 * t, lt + g + 8, x1.x);
+    stage_split(s.xt, 2 * t + 1, lt + g + 8, x1.y);
+    // forward
+    float z1[8][4], z2[8][4];
+    uint32_t ha_hi[4][4], ha_lo[4][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      const uint32_t b0 = s.w1[(8 * j + g) * (MLP_IN / 2) + t];
+      mma_bf16_16816(c, xa_hi, b0, 0u);
+      mma_bf16_16816(c, xa_lo, b0, 0u);
+      const int col = 8 * j + 2 * t;
+      z1[j][0] = c[0] + s.b1[col]; z1[j][1] = c[1] + s.b1[col + 1];
+      z1[j][2] = c[2] + s.b1[col]; z1[j][3] = c[3] + s.b1[col + 1];
+      const float h0 = gelu(z1[j][0]), h1 = gelu(z1[j][1]);
+      const float h2 = gelu(z1[j][2]), h3 = gelu(z1[j][3]);
+      const int sl = j >> 1, q = (j & 1) * 2;
+      split_bf16x2(h0, h1, ha_hi[sl][q], ha_lo[sl][q]);
+      split_bf16x2(h2, h3, ha_hi[sl][q + 1], ha_lo[sl][q + 1]);
+      stage_split(s.h1t, col, lt + g, h0);
+      stage_split(s.h1t, col + 1, lt + g, h1);
+      stage_split(s.h1t, col, lt + g + 8, h2);
+      stage_split(s.h1t, col + 1, lt + g + 8, h3);
+    }
+    float p0 = 0.f, p1 = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      const uint32_t *wrow = s.w2 + (8 * j + g) * W2_STRIDE;
+#pragma unroll
+      for (int sl = 0; sl < 4; ++sl) {
+        const uint32_t b0 = wrow[8 * sl + t], b1 = wrow[8 * sl + 4 + t];
+        mma_bf16_16816(c, ha_hi[sl], b0, b1);
+        mma_bf16_16816(c, ha_lo[sl], b0, b1);
+      }
+      const int col = 8 * j + 2 * t;
+      z2[j][0] = c[0] + s.b2[col]; z2[j][1] = c[1] + s.b2[col + 1];
+      z2[j][2] = c[2] + s.b2[col]; z2[j][3] = c[3] + s.b2[col + 1];
+      p0 = fmaf(gelu(z2[j][0]), s.w3[col], p0);
+      p0 = fmaf(gelu(z2[j][1]), s.w3[col + 1], p0);
+      p1 = fmaf(gelu(z2[j][2]), s.w3[col], p1);
+      p1 = fmaf(gelu(z2[j][3]), s.w3[col + 1], p1);
+    }
+    p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
+    p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
+    p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
+    p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
+    // residuals of rows g and g + 8 (every lane of the quad holds them)
+    const float w0 = v0 ? (Wt ? Wt[r0] : 1.0f) : 0.f, w1 = v1 ? (Wt ? Wt[r1] : 1.0f) : 0.f;
+    const float e0 = v0 ? p0 + s.b3 - T[r0] : 0.f, e1 = v1 ? p1 + s.b3 - T[r1] : 0.f;
+    const float dy0 = 2.0f * w0 * e0 * inv_norm, dy1 = 2.0f * w1 * e1 * inv_norm;
+    if (t == 0) {
+      sum_dy += dy0 + dy1;
+      sum_loss += w0 * e0 * e0 * inv_norm + w1 * e1 * e1 * inv_norm;
+    }
+    // dz2 = dy W3 gelu'(z2) -> A fragments of dh1 = dz2 W2
+    uint32_t da_hi[4][4], da_lo[4][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int col = 8 * j + 2 * t;
+      const float d0 = dy0 * s.w3[col] * gelu_grad(z2[j][0]);
+      const float d1 = dy0 * s.w3[col + 1] * gelu_grad(z2[j][1]);
+      const float d2 = dy1 * s.w3[col] * gelu_grad(z2[j][2]);
+      const float d3 = dy1 * s.w3[col + 1] * gelu_grad(z2[j][3]);
+      add_col_sum(s.red[warp][1], col, g, d0 + d2);
+      add_col_sum(s.red[warp][1], col + 1, g, d1 + d3);
+      add_col_sum(s.red[warp][2], col, g, dy0 * gelu(z2[j][0]) + dy1 * gelu(z2[j][2]));
+      add_col_sum(s.red[warp][2], col + 1, g, dy0 * gelu(z2[j][1]) + dy1 * gelu(z2[j][3]));
+      const int sl = j >> 1, q = (j & 1) * 2;
+      split_bf16x2(d0, d1, da_hi[sl][q], da_lo[sl][q]);
+      split_bf16x2(d2, d3, da_hi[sl][q + 1], da_lo[sl][q + 1]);
+      stage_split(s.dz2t, col, lt + g, d0);
+      stage_split(s.dz2t, col + 1, lt + g, d1);
+      stage_split(s.dz2t, col, lt + g + 8, d2);
+      stage_split(s.dz2t, col + 1, lt + g + 8, d3);
+    }
+    // dh1 = dz2 W2 (B from W2 transposed), dz1 = dh1 gelu'(z1)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      const uint32_t *wrow = s.w2t + (8 * j + g) * W2_STRIDE;
+#pragma unroll
+      for (int sl = 0; sl < 4; ++sl) {
+        const uint32_t b0 = wrow[8 * sl + t], b1 = wrow[8 * sl + 4 + t];
+        mma_bf16_16816(c, da_hi[sl], b0, b1);
+        mma_bf16_16816(c, da_lo[sl], b0, b1);
+      }
+      const int col = 8 * j + 2 * t;
+      const float d0 = c[0] * gelu_grad(z1[j][0]), d1 = c[1] * gelu_grad(z1[j][1]);
+      const float d2 = c[2] * gelu_grad(z1[j][2]), d3 = c[3] * gelu_grad(z1[j][3]);
+      add_col_sum(s.red[warp][0], col, g, d0 + d2);
+      add_col_sum(s.red[warp][0], col + 1, g, d1 + d3);
+      stage_split(s.dz1t, col, lt + g, d0);
+      stage_split(s.dz1t, col + 1, lt + g, d1);
+      stage_split(s.dz1t, col, lt + g + 8, d2);
+      stage_split(s.dz1t, col + 1, lt + g + 8, d3);
+    }
+  }
+  sum_dy += __shfl_xor_sync(0xffffffffu, sum_dy, 4);
+  sum_dy += __shfl_xor_sync(0xffffffffu, sum_dy, 8);
+  sum_dy += __shfl_xor_sync(0xffffffffu, sum_dy, 16);
+  sum_loss += __shfl_xor_sync(0xffffffffu, sum_loss, 4);
+  sum_loss += __shfl_xor_sync(0xffffffffu, sum_loss, 8);
+  sum_loss += __shfl_xor_sync(0xffffffffu, sum_loss, 16);
+  if (lane == 0) {
+    s.redy[warp][0] = sum_dy;
+    s.redy[warp][1] = sum_loss;
   }
   __syncthreads();
-  // block sums over the samples, each output by one thread in sample order
+  // weight gradients over the block's samples: warp w owns rows 16w..16w+15
   float *pb = part + (size_t)blockIdx.x * MLP_P;
-  for (int e = t; e < MLP_H * MLP_H; e += MLP_THREADS) {     // dW2[o][k]
-    const int o = e / MLP_H, k = e % MLP_H;
-    float a = 0.f;
-    for (int u = 0; u < MLP_THREADS; ++u) a = fmaf(sd2[u * LD + o], sh1[u * LD + k], a);
-    pb[OFF_W2 + e] = a;
-  }
-  for (int e = t; e < MLP_H * MLP_IN; e += MLP_THREADS) {    // dW1[k][f]
-    const int k = e / MLP_IN, f = e % MLP_IN;
-    float a = 0.f;
-    for (int u = 0; u < MLP_THREADS; ++u) a = fmaf(sd1[u * LD + k], sx[u * MLP_IN + f], a);
-    pb[OFF_W1 + e] = a;
-  }
-  if (t < MLP_H) {                                           // dW3, db2, db1
-    float a = 0.f, c = 0.f, d = 0.f;
-    for (int u = 0; u < MLP_THREADS; ++u) {
-      a = fmaf(sdy[u], sh2[u * LD + t], a);
-      c += sd2[u * LD + t];
-      d += sd1[u * LD + t];
+  {
+    const int m0 = 16 * warp;
+    float acc[8][4], acc1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int n = 0; n < 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+#pragma unroll 2
+    for (int ks = 0; ks < BW_SAMPLES / 16; ++ks) {
+      const int kc = 16 * ks + 2 * t;
+      uint32_t ah[4], al[4], zh[4], zl[4];
+#pragma unroll
+      for (int hl = 0; hl < 2; ++hl) {
+        uint32_t *a = hl ? al : ah, *z = hl ? zl : zh;
+        a[0] = ld_pair(&s.dz2t[hl][m0 + g][kc]);
+        a[1] = ld_pair(&s.dz2t[hl][m0 + g + 8][kc]);
+        a[2] = ld_pair(&s.dz2t[hl][m0 + g][kc + 8]);
+        a[3] = ld_pair(&s.dz2t[hl][m0 + g + 8][kc + 8]);
+        z[0] = ld_pair(&s.dz1t[hl][m0 + g][kc]);
+        z[1] = ld_pair(&s.dz1t[hl][m0 + g + 8][kc]);
+        z[2] = ld_pair(&s.dz1t[hl][m0 + g][kc + 8]);
+        z[3] = ld_pair(&s.dz1t[hl][m0 + g + 8][kc + 8]);
+      }
+      const uint32_t (&ahr)[4] = *reinterpret_cast<const uint32_t(*)[4]>(ah);
+      const uint32_t (&alr)[4] = *reinterpret_cast<const uint32_t(*)[4]>(al);
+      const uint32_t (&zhr)[4] = *reinterpret_cast<const uint32_t(*)[4]>(zh);
+      const uint32_t (&zlr)[4] = *reinterpret_cast<const uint32_t(*)[4]>(zl);
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        const uint32_t bh0 = ld_pair(&s.h1t[0][8 * n + g][kc]);
+        const uint32_t bh1 = ld_pair(&s.h1t[0][8 * n + g][kc + 8]);
+        const uint32_t bl0 = ld_pair(&s.h1t[1][8 * n + g][kc]);
+        const uint32_t bl1 = ld_pair(&s.h1t[1][8 * n + g][kc + 8]);
+        mma_bf16_16816(acc[n], ahr, bh0, bh1);
+        mma_bf16_16816(acc[n], ahr, bl0, bl1);
+        mma_bf16_16816(acc[n], alr, bh0, bh1);
+      }
+      const uint32_t xh0 = ld_pair(&s.xt[0][g][kc]), xh1 = ld_pair(&s.xt[0][g][kc + 8]);
+      const uint32_t xl0 = ld_pair(&s.xt[1][g][kc]), xl1 = ld_pair(&s.xt[1][g][kc + 8]);
+      mma_bf16_16816(acc1, zhr, xh0, xh1);
+      mma_bf16_16816(acc1, zhr, xl0, xl1);
+      mma_bf16_16816(acc1, zlr, xh0, xh1);
     }
-    pb[OFF_W3 + t] = a;
-    pb[OFF_B2 + t] = c;
-    pb[OFF_B1 + t] = d;
-  } else if (t == MLP_H) {                                   // db3
-    float a = 0.f;
-    for (int u = 0; u < MLP_THREADS; ++u) a += sdy[u];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const int k = 8 * n + 2 * t;
+      pb[OFF_W2 + (m0 + g) * MLP_H + k] = acc[n][0];
+      pb[OFF_W2 + (m0 + g) * MLP_H + k + 1] = acc[n][1];
+      pb[OFF_W2 + (m0 + g + 8) * MLP_H + k] = acc[n][2];
+      pb[OFF_W2 + (m0 + g + 8) * MLP_H + k + 1] = acc[n][3];
+    }
+    pb[OFF_W1 + (m0 + g) * MLP_IN + 2 * t] = acc1[0];
+    pb[OFF_W1 + (m0 + g) * MLP_IN + 2 * t + 1] = acc1[1];
+    pb[OFF_W1 + (m0 + g + 8) * MLP_IN + 2 * t] = acc1[2];
+    pb[OFF_W1 + (m0 + g + 8) * MLP_IN + 2 * t + 1] = acc1[3];
+  }
+  const int tid = threadIdx.x;
+  if (tid < MLP_H) {
+    float a = 0.f, b = 0.f, c = 0.f;
+    for (int w = 0; w < BW_WARPS; ++w) {
+      a += s.red[w][0][tid];
+      b += s.red[w][1][tid];
+      c += s.red[w][2][tid];
+    }
+    pb[OFF_B1 + tid] = a;
+    pb[OFF_B2 + tid] = b;
+    pb[OFF_W3 + tid] = c;
+  } else if (tid == MLP_H) {
+    float a = 0.f, l = 0.f;
+    for (int w = 0; w < BW_WARPS; ++w) {
+      a += s.redy[w][0];
+      l += s.redy[w][1];
+    }
     pb[OFF_B3] = a;
-  } else if (t == MLP_H + 1) {                               // loss
-    float a = 0.f;
-    for (int u = 0; u < MLP_THREADS; ++u) a += sh_red[u];
-    loss_part[blockIdx.x] = a;
+    loss_part[blockIdx.x] = l;
   }
 }
 
@@ -521,12 +715,12 @@ int gpunb_rsmlp_backward(int B, const float *X, const float *T, const float *W, 
   const int nb = (B + MLP_THREADS - 1) / MLP_THREADS;
   float *loss_part = part + (size_t)nb * MLP_P;
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t smem = rsmlp_backward_smem();
-  if (cudaFuncSetAttribute(rsmlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const size_t smem = sizeof(MlpBwSmem);
+  if (cudaFuncSetAttribute(rsmlp_backward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return GPUNB_E_CUDA;
-  rsmlp_backward_kernel<<<nb, MLP_THREADS, smem, st>>>(B, X, T, W, (const __nv_bfloat16 *)wq, wf,
-                                                       1.0f / (float)B, part, loss_part);
+  rsmlp_backward_tc_kernel<<<nb, 32 * BW_WARPS, smem, st>>>(
+      B, X, T, W, (const __nv_bfloat16 *)wq, wf, 1.0f / (float)B, part, loss_part);
   rsmlp_reduce_kernel<<<(MLP_P + 255) / 256, 256, 0, st>>>(nb, part, loss_part, grad, loss);
   return cudaGetLastError() == cudaSuccess ? GPUNB_OK : GPUNB_E_CUDA;
 }

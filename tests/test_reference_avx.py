@@ -32,7 +32,7 @@ def test_port_keeps_pace_with_the_reference_cpu_path():
     reference's x86 AVX source does not build) runs within 1.35x of the
     reference's own reg.avx.cpp on the same host threads: best of five
     interleaved runs of a 4096-particle block against N = 65536, in the
-    caller's chunks of 1024 (measured here: 1.2x).  Its lists equal the
+    caller's chunks of 1024 (measured here: 1.0x to 1.2x).  Its lists equal the
     reference's except in rows holding a pair whose criterion value lies
     within FP32 rounding of h2 (at most two here)."""
     import time
