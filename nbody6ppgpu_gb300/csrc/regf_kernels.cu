@@ -250,10 +250,11 @@ __device__ __forceinline__ void load_istate(IState &I, const float4 *__restrict_
 
 // Exact FP64 decision for a pair whose FP32 criterion value fell inside the
 // error band (very rare): kept out of line so that the common path carries
-// no call frame.
+// no call frame.  slot: the j's tile slot (padding slots are never members).
 template <bool MFLAG>
-__device__ __noinline__ bool decide_pair_fp64(const ISet &is, int i, const JSet &js, int jg) {
-  return nb_test_fp64(is, i, js, jg, MFLAG);
+__device__ __noinline__ bool decide_pair_fp64(const ISet &is, int i, const JSet &js, int slot) {
+  const int jo = js.perm[slot];
+  return jo >= 0 && nb_test_fp64(is, i, js, jo, MFLAG);
 }
 
 // Decide one candidate pair (rare path).  FP32 decision, FP64 re-test when
@@ -265,7 +266,7 @@ __device__ __noinline__ bool decide_pair_fp64(const ISet &is, int i, const JSet 
 // radius).
 template <bool MFLAG>
 __device__ __forceinline__ bool decide_pair(const IState &I, const ISet &is, const JSet &js,
-                                            int jg, float dx, float dy, float dz, float dvx,
+                                            int slot, float dx, float dy, float dz, float dvx,
                                             float dvy, float dvz, float r2, float mneg_half,
                                             float R) {
   const float px = fmaf(I.dtrf, dvx, dx);
@@ -278,13 +279,62 @@ __device__ __forceinline__ bool decide_pair(const IState &I, const ISet &is, con
   const float dv1 = fabsf(dvx) + fabsf(dvy) + fabsf(dvz);
   const float w = 2.0f * fabsf(I.dtrf) * (I.va + dv1);
   const float band = 0x1p-14f * (fabsf(crit) + r2 + w * w) + 0x1p-18f * R * (sqrtf(r2) + w);
-  if (fabsf(r2min - crit) <= band) in = decide_pair_fp64<MFLAG>(is, I.i, js, jg);
+  if (fabsf(r2min - crit) <= band) in = decide_pair_fp64<MFLAG>(is, I.i, js, slot);
   return in;
 }
 
-__device__ __forceinline__ void record_neighbour(const RegfOut &out, int i, int j) {
-  const int slot = atomicAdd(out.cnt + i, 1);
-  if (slot < out.cap) out.rows[(size_t)i * out.cap + slot] = j;
+// Accepted neighbours of one (thread, i) pending in shared memory: the tile
+// slots, NBUF at most, entry e at buf[e * stride].  The pair loop only writes
+// them there; a flush maps the slots to the caller's ids, reserves room in
+// the row with one atomic per thread and stores them.  Flushes are
+// warp-collective (when a lane of the warp could overflow its buffer, and at
+// the end of each work item), so the loads and atomics of the lanes overlap
+// and the pair loop never waits on global memory.  Row order does not matter:
+// the rows are sorted when they are gathered.
+#ifndef GPUNB_NBUF
+#define GPUNB_NBUF 32
+#endif
+constexpr int NBUF = GPUNB_NBUF;
+static_assert(NBUF >= 8 && NBUF % 4 == 0, "a pair group adds up to 8 entries");
+
+struct NbRec {
+  int *buf;
+  int stride;
+  int n;
+};
+
+__device__ __forceinline__ void nb_flush(NbRec &r, int i, int jbase, const int *__restrict__ perm,
+                                         const RegfOut &out) {
+  if (r.n > 0) {
+    int valid = 0;
+    for (int e0 = 0; e0 < r.n; e0 += 4) {
+      int jo[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) jo[u] = e0 + u < r.n ? __ldg(perm + r.buf[(e0 + u) * r.stride]) : -1;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (e0 + u < r.n) r.buf[(e0 + u) * r.stride] = jo[u];
+        valid += jo[u] >= 0;
+      }
+    }
+    if (valid > 0) {
+      int slot = atomicAdd(out.cnt + i, valid);
+      for (int e = 0; e < r.n; ++e) {
+        const int jo = r.buf[e * r.stride];
+        if (jo >= 0) {
+          if (slot < out.cap) out.rows[(size_t)i * out.cap + slot] = jo - jbase;
+          ++slot;
+        }
+      }
+    }
+    r.n = 0;
+  }
+}
+
+// warp-collective: make room for the up to 8 entries of one pair group
+__device__ __forceinline__ void nb_room(NbRec &r, int i, int jbase, const JSet &js,
+                                        const RegfOut &out) {
+  if (__any_sync(0xffffffffu, r.n > NBUF - 8)) nb_flush(r, i, jbase, js.perm, out);
 }
 
 // Two j (one f32x2 lane pair) against one i.  The per-pair computation is
@@ -345,30 +395,23 @@ __device__ __forceinline__ bool pair_maybe(const PairGeo &g, float H) {
   return (g.r2.x < H) | (g.r2.y < H);
 }
 
-// Candidates of one lane pair (rare path): decide, record, and drop the
-// neighbours from the sums.  perm maps a tile slot to the index into the sent
-// arrays; padding slots hold -1 and never qualify.  Ids are reported relative
-// to the owning j-set (jbase), in the caller's numbering.
+// Candidates of one lane pair (rare path): decide, record the tile slot, and
+// drop the neighbours from the sums.  Padding slots (massless, at 1e15) are
+// filtered when the slots are mapped to ids (nb_flush).
 template <bool MFLAG>
 __device__ __forceinline__ void pair_candidates(const IState &I, const TileCtx &C, PairGeo &g,
-                                                int jg0, int jbase, const JSet &js,
-                                                const ISet &is, const RegfOut &out) {
+                                                int jg0, const JSet &js, const ISet &is,
+                                                NbRec &rec) {
   const float H = C.H;
-  if (g.r2.x < H) {
-    const int jo = js.perm[jg0];
-    if (jo >= 0 && decide_pair<MFLAG>(I, is, js, jo, g.dx.x, g.dy.x, g.dz.x, g.dvx.x, g.dvy.x,
-                                      g.dvz.x, g.r2.x, g.mn.x, C.R)) {
-      record_neighbour(out, I.i, jo - jbase);
-      g.z.x = 0.f;
-    }
+  if (g.r2.x < H && decide_pair<MFLAG>(I, is, js, jg0, g.dx.x, g.dy.x, g.dz.x, g.dvx.x, g.dvy.x,
+                                       g.dvz.x, g.r2.x, g.mn.x, C.R)) {
+    rec.buf[rec.n++ * rec.stride] = jg0;
+    g.z.x = 0.f;
   }
-  if (g.r2.y < H) {
-    const int jo = js.perm[jg0 + 1];
-    if (jo >= 0 && decide_pair<MFLAG>(I, is, js, jo, g.dx.y, g.dy.y, g.dz.y, g.dvx.y, g.dvy.y,
-                                      g.dvz.y, g.r2.y, g.mn.y, C.R)) {
-      record_neighbour(out, I.i, jo - jbase);
-      g.z.y = 0.f;
-    }
+  if (g.r2.y < H && decide_pair<MFLAG>(I, is, js, jg0 + 1, g.dx.y, g.dy.y, g.dz.y, g.dvx.y,
+                                       g.dvy.y, g.dvz.y, g.r2.y, g.mn.y, C.R)) {
+    rec.buf[rec.n++ * rec.stride] = jg0 + 1;
+    g.z.y = 0.f;
   }
 }
 
@@ -390,13 +433,15 @@ __device__ __forceinline__ void pair_acc(const PairGeo &g, f2 (&q)[NQ]) {
 template <bool MFLAG, bool REL>
 __device__ __forceinline__ void pair4(const IState &I, const TileCtx &C, const JPair &p0,
                                       const JPair &p1, f2 (&q)[NQ], int jg0, int jbase,
-                                      const JSet &js, const ISet &is, const RegfOut &out) {
+                                      const JSet &js, const ISet &is, const RegfOut &out,
+                                      NbRec &rec) {
   PairGeo g0, g1;
   pair_geo<REL>(I, C, p0, g0);
   pair_geo<REL>(I, C, p1, g1);
   if (__any_sync(0xffffffffu, pair_maybe(g0, C.H) | pair_maybe(g1, C.H))) {
-    pair_candidates<MFLAG>(I, C, g0, jg0, jbase, js, is, out);
-    pair_candidates<MFLAG>(I, C, g1, jg0 + 2, jbase, js, is, out);
+    nb_room(rec, I.i, jbase, js, out);
+    pair_candidates<MFLAG>(I, C, g0, jg0, js, is, rec);
+    pair_candidates<MFLAG>(I, C, g1, jg0 + 2, js, is, rec);
   }
   pair_acc(g0, q);
   pair_acc(g1, q);
@@ -406,7 +451,7 @@ __device__ __forceinline__ void pair4(const IState &I, const TileCtx &C, const J
 template <bool MFLAG, bool REL>
 __device__ __forceinline__ void pair8(const IState &I, const TileCtx &C, const JPair (&p)[4],
                                       f2 (&q)[NQ], int jg0, int jbase, const JSet &js,
-                                      const ISet &is, const RegfOut &out) {
+                                      const ISet &is, const RegfOut &out, NbRec &rec) {
   PairGeo g[4];
 #pragma unroll
   for (int u = 0; u < 4; ++u) pair_geo<REL>(I, C, p[u], g[u]);
@@ -414,9 +459,9 @@ __device__ __forceinline__ void pair8(const IState &I, const TileCtx &C, const J
   const bool any = pair_maybe(g[0], H) | pair_maybe(g[1], H) | pair_maybe(g[2], H) |
                    pair_maybe(g[3], H);
   if (__any_sync(0xffffffffu, any)) {
+    nb_room(rec, I.i, jbase, js, out);
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
-      pair_candidates<MFLAG>(I, C, g[u], jg0 + 2 * u, jbase, js, is, out);
+    for (int u = 0; u < 4; ++u) pair_candidates<MFLAG>(I, C, g[u], jg0 + 2 * u, js, is, rec);
   }
 #pragma unroll
   for (int u = 0; u < 4; ++u) pair_acc(g[u], q);
@@ -429,7 +474,7 @@ template <bool MFLAG, bool REL, int JV, int JW>
 __device__ __forceinline__ void tile_pairs(const IState &I, const TileCtx &C,
                                            const float *__restrict__ T, int jbeg, f2 (&q)[NQ],
                                            int jg_tile, int jbase, const JSet &js,
-                                           const ISet &is, const RegfOut &out) {
+                                           const ISet &is, const RegfOut &out, NbRec &rec) {
   constexpr int F0 = REL ? 0 : F_VX;
   constexpr int F1 = REL ? NFIELD_REL : NFIELD;
   if (JV == 8) {
@@ -444,7 +489,7 @@ __device__ __forceinline__ void tile_pairs(const IState &I, const TileCtx &C,
         p[2].v[f] = make_float2(w4.x, w4.y);
         p[3].v[f] = make_float2(w4.z, w4.w);
       }
-      pair8<MFLAG, REL>(I, C, p, q, jg_tile + jj, jbase, js, is, out);
+      pair8<MFLAG, REL>(I, C, p, q, jg_tile + jj, jbase, js, is, out, rec);
     }
   } else {
     for (int jj = jbeg; jj < jbeg + JW; jj += 4) {
@@ -463,7 +508,7 @@ __device__ __forceinline__ void tile_pairs(const IState &I, const TileCtx &C,
           p1.v[f] = make_float2(u.z, u.w);
         }
       }
-      pair4<MFLAG, REL>(I, C, p0, p1, q, jg_tile + jj, jbase, js, is, out);
+      pair4<MFLAG, REL>(I, C, p0, p1, q, jg_tile + jj, jbase, js, is, out, rec);
     }
   }
 }
@@ -502,6 +547,7 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
   extern __shared__ __align__(128) float smem[];
   float *ring = smem;                                   // NSTAGE * TILE_FLOATS
   float *ffs = smem + NSTAGE * TILE_FLOATS;             // [2][NQ][IPT][NT] float-float
+  int *nbuf = reinterpret_cast<int *>(ffs + 2 * NQ * IPT * NT);   // [NBUF][IPT][NT]
   __shared__ __align__(8) uint64_t bar[NSTAGE];
   __shared__ int s_rel[NSTAGE];                         // warps done with the stage
   __shared__ int s_iss[NSTAGE];                         // copies issued into the stage
@@ -553,8 +599,12 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
 
     IState I[IPT];
     f2 q[IPT][NQ];
+    NbRec rec[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
+      rec[k].buf = nbuf + k * NT + tid;
+      rec[k].stride = IPT * NT;
+      rec[k].n = 0;
       const int slot = slot0 + wi * 32 * IPT + k * 32 + lane;
       load_istate(I[k], is.rec, slot, slot < slot_end);
 #pragma unroll
@@ -608,10 +658,10 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
           C.nxh = mk2(I[k].nxh); C.nyh = mk2(I[k].nyh); C.nzh = mk2(I[k].nzh);
           C.nxl = mk2(I[k].nxl); C.nyl = mk2(I[k].nyl); C.nzl = mk2(I[k].nzl);
           tile_pairs<MFLAG, false, JV, JW>(I[k], C, T, jbeg, q[k], (t0 + t) * JT, jbase, js, is,
-                                           out);
+                                           out, rec[k]);
         } else {
           tile_pairs<MFLAG, true, JV, JW>(I[k], C, T, jbeg, q[k], (t0 + t) * JT, jbase, js, is,
-                                          out);
+                                          out, rec[k]);
         }
       }
       // fold the FP32 chunk sums into the float-float accumulators
@@ -645,6 +695,8 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
         }
       }
     }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) nb_flush(rec[k], I[k].i, jbase, js.perm, out);
     g += nt;
     __syncthreads();
     if (s_abort) break;
@@ -687,6 +739,11 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
       if (s_iss[u] > 0) mbar_wait_bounded(&bar[u], (uint32_t)(s_iss[u] - 1) & 1u, 1u << 16);
     raise_error(out.err, GPUNB_E_TIMEOUT);
   }
+}
+
+__device__ __forceinline__ void record_neighbour(const RegfOut &out, int i, int j) {
+  const int slot = atomicAdd(out.cnt + i, 1);
+  if (slot < out.cap) out.rows[(size_t)i * out.cap + slot] = j;
 }
 
 // ---------------------------------------------------------------------------
@@ -1213,7 +1270,8 @@ VariantDesc regf_variant(int v) { return kVariants[v]; }
 
 size_t regf_ds_smem(int v) {
   const VariantDesc d = kVariants[v];
-  return (size_t)NSTAGE * TILE_BYTES + 2u * NQ * d.ipt * d.threads() * sizeof(float);
+  return (size_t)NSTAGE * TILE_BYTES + 2u * NQ * d.ipt * d.threads() * sizeof(float) +
+         (size_t)NBUF * d.ipt * d.threads() * sizeof(int);
 }
 
 typedef void (*regf_fn)(JSet, ISet, RegfOut, RegfWork);
