@@ -289,9 +289,18 @@ int gpunb_rsmlp_label_device(int ni, const int *list_off, const int *list, const
  * time).  Plain rule as regcor_gpu.F (with the few-member rule of
  * fpoly0.F:153-158 for counts below 2 when few_nb_rule), and, when wq is not
  * NULL, the MLP proposal from the 8 features of each particle normalised by
- * norm[0..7] (mean) and norm[8..15] (spread), taken where the count it implies
- * at the current density stays within [band_lo, band_hi] x the rule's target
- * (0.5-1.5 when the fields are 0).  Inputs per
+ * norm[0..7] (mean) and norm[8..15] (spread), taken where its count stays
+ * within [band_lo, band_hi] x the rule's target (0.5-1.5 when the fields are
+ * 0).  The count of a proposed radius R' is the count at the current
+ * density, (nnb + 1)(R'/RS)^3 - 1, or, when the block's neighbour rows are
+ * given (list_off != NULL), the larger of that and an estimate at the next
+ * regular step: the members j of row i (list[list_off[i] .. list_off[i+1]),
+ * indices into xj/vj, the j-set the rows were computed on, e.g. the CSR output
+ * of gpunb_regf_device) with min(|d|^2, |d + dtr dv|^2) < R'^2,
+ * d = dx + dtr dv (the kernel's membership test one step later, separations
+ * moved on the current relative velocity), plus, when R' > RS, the members x
+ * ((R'/RS)^3 - 1); a member with the particle's own position and velocity is
+ * the particle itself and is skipped.  Inputs per
  * active particle i < ni: x, v ([ni][3]), m_scaled (mass x N), rs, nnb (count,
  * self excluded), nnb0 (previous count), acc, jrk ([ni][3], regular force and
  * derivative; only read with wq), dtr.  Outputs rs_new[ni], and when not NULL
@@ -305,6 +314,9 @@ typedef struct {
   double bodym;             /* mean mass */
   double rdens[3];          /* density centre RDENS */
   double band_lo, band_hi;  /* acceptance band of the MLP proposal (0: 0.5, 1.5) */
+  const int *list_off;      /* neighbour rows for the band check (device), or NULL */
+  const int *list;
+  const double *xj, *vj;    /* positions, velocities of the j-set the rows index */
 } gpunb_rs_params;
 int gpunb_rs_update_device(int ni, const gpunb_rs_params *p, const double *x, const double *v,
                            const double *m_scaled, const double *rs, const int *nnb,

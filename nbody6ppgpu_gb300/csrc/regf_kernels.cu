@@ -524,7 +524,10 @@ __device__ __forceinline__ void tile_pairs(const IState &I, const TileCtx &C,
 // to finish with a stage refills it, so warps are never held at a block-wide
 // barrier inside an item.  Stage phases run on a per-block tile counter g
 // that continues across items.
-constexpr int NSTAGE = 4;
+#ifndef GPUNB_NSTAGE
+#define GPUNB_NSTAGE 4
+#endif
+constexpr int NSTAGE = GPUNB_NSTAGE;
 
 struct RegfWork {
   int *queue;              // item counter, zeroed before the launch
@@ -1260,9 +1263,12 @@ __global__ void list_finalize_offsets_kernel(int *off, const int *btot, int ni, 
 // SM (the register cap, 65536 / (threads x blocks) per thread, set to what
 // each shape reaches unconstrained: a tighter cap, e.g. 80 registers for six
 // blocks of variant 4, spills and measured slower)
+#ifndef GPUNB_V6_MINB
+#define GPUNB_V6_MINB 4
+#endif
 static const VariantDesc kVariants[] = {{2, 4, 1, 2, 3}, {2, 2, 2, 2, 3}, {1, 1, 8, 2, 2},
                                         {1, 4, 1, 2, 5}, {1, 4, 1, 4, 5}, {1, 8, 1, 2, 2},
-                                        {1, 4, 1, 8, 4}};
+                                        {1, 4, 1, 8, GPUNB_V6_MINB}};
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 
 int regf_num_variants() { return kNumVariants; }
@@ -1285,7 +1291,7 @@ static regf_fn regf_kernel_ptr(int v, bool mflag) {
     case 3: return GPUNB_RK(1, 4, 1, 2, 5);
     case 4: return GPUNB_RK(1, 4, 1, 4, 5);
     case 5: return GPUNB_RK(1, 8, 1, 2, 2);
-    default: return GPUNB_RK(1, 4, 1, 8, 4);
+    default: return GPUNB_RK(1, 4, 1, 8, GPUNB_V6_MINB);
   }
 #undef GPUNB_RK
 }

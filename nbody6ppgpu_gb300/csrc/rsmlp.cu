@@ -1,5 +1,5 @@
-// Learned neighbour-radius predictor: an 8 -> 64 -> 64 -> 1 MLP with GELU,
-// BF16 weight matrices, FP32 biases, activations and accumulation.
+// Learned neighbour-radius predictor: an 8 -> 64 -> 64 -> 1 MLP with GELU in
+// its tanh form, BF16 weight matrices, FP32 biases and accumulation.
 //
 // No reference counterpart: the reference adjusts RS by a fixed rule after
 // every regular step (src/Main/regcor_gpu.F:146-253) and shrinks it after a
@@ -11,14 +11,17 @@
 // The kernels read the weight matrices from the BF16 copy and the biases
 // from the FP32 copy.  Samples are rows of X[B][8] (normalised features).
 //
-// Inference (gpunb_rsmlp_forward) and training (gpunb_rsmlp_backward) run
-// their matrix products on the tensor cores (mma.sync BF16 tiles of 16
-// samples, FP32 accumulation, FP32 inputs and activations as two-term BF16
-// splits); the fused RS update evaluates the network per particle on the
-// CUDA cores (mlp_eval).
+// Inference (gpunb_rsmlp_forward, and the fused RS update) and training
+// (gpunb_rsmlp_backward) run their matrix products on the tensor cores
+// (mma.sync BF16 tiles of 16 samples, FP32 accumulation).  Inference takes
+// BF16 inputs and activations and the hardware tanh approximation; training
+// carries inputs and activations as two-term BF16 splits and an accurate
+// tanh, so that its gradients are those of FP32 arithmetic on the same
+// weights.
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 #include "rsrule.cuh"
@@ -31,73 +34,37 @@ constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + MLP_H * MLP_IN, OFF_W2 = OFF_B1 + ML
               MLP_P = OFF_B3 + 1;
 constexpr int MLP_THREADS = 128;
 
+// GELU in its tanh form (Hendrycks and Gimpel, 2016):
+//   gelu(x) = x/2 (1 + tanh(u)),  u = sqrt(2/pi) (x + 0.044715 x^3),
+//   gelu'(x) = (1 + tanh u)/2 + x/2 (1 - tanh^2 u) sqrt(2/pi) (1 + 3 0.044715 x^2).
+constexpr float GELU_C = 0.7978845608028654f;           // sqrt(2/pi)
+constexpr float GELU_CA = 0.7978845608028654f * 0.044715f;
+__device__ __forceinline__ float gelu_arg(float x) { return x * fmaf(GELU_CA, x * x, GELU_C); }
 __device__ __forceinline__ float gelu(float x) {
-  return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+  const float h = 0.5f * x;
+  return fmaf(h, tanhf(gelu_arg(x)), h);
 }
 __device__ __forceinline__ float gelu_grad(float x) {
-  // d/dx [x Phi(x)] = Phi(x) + x phi(x)
-  return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) +
-         x * 0.3989422804014327f * expf(-0.5f * x * x);
+  const float t = tanhf(gelu_arg(x));
+  return fmaf(0.5f, t, 0.5f) + 0.5f * x * fmaf(-t, t, 1.0f) * fmaf(3.0f * GELU_CA, x * x, GELU_C);
 }
-
-// weights (as float) and biases staged in shared memory
-struct MlpSmem {
-  float w1[MLP_H * MLP_IN];
-  float b1[MLP_H];
-  float w2[MLP_H * MLP_H];
-  float b2[MLP_H];
-  float w3[MLP_H];
-  float b3;
-};
-
-__device__ void stage_params(MlpSmem &s, const __nv_bfloat16 *__restrict__ wq,
-                             const float *__restrict__ wf) {
-  for (int k = threadIdx.x; k < MLP_H * MLP_IN; k += blockDim.x)
-    s.w1[k] = __bfloat162float(wq[OFF_W1 + k]);
-  for (int k = threadIdx.x; k < MLP_H * MLP_H; k += blockDim.x)
-    s.w2[k] = __bfloat162float(wq[OFF_W2 + k]);
-  for (int k = threadIdx.x; k < MLP_H; k += blockDim.x) {
-    s.w3[k] = __bfloat162float(wq[OFF_W3 + k]);
-    s.b1[k] = wf[OFF_B1 + k];
-    s.b2[k] = wf[OFF_B2 + k];
-  }
-  if (threadIdx.x == 0) s.b3 = wf[OFF_B3];
-  __syncthreads();
-}
-
-__device__ __forceinline__ float mlp_eval(const MlpSmem &s, const float (&x)[MLP_IN]) {
-  float h1[MLP_H];
-#pragma unroll
-  for (int o = 0; o < MLP_H; ++o) {
-    float a = s.b1[o];
-#pragma unroll
-    for (int f = 0; f < MLP_IN; ++f) a = fmaf(s.w1[o * MLP_IN + f], x[f], a);
-    h1[o] = gelu(a);
-  }
-  float out = s.b3;
-  for (int o = 0; o < MLP_H; ++o) {
-    float a = s.b2[o];
-#pragma unroll
-    for (int k = 0; k < MLP_H; ++k) a = fmaf(s.w2[o * MLP_H + k], h1[k], a);
-    out = fmaf(s.w3[o], gelu(a), out);
-  }
-  return out;
+// inference: the tanh from the hardware approximation (relative error below
+// 2^-10.9, under the BF16 rounding of the activations that follows)
+__device__ __forceinline__ float gelu_fast(float x) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(gelu_arg(x)));
+  const float h = 0.5f * x;
+  return fmaf(h, t, h);
 }
 
 // ---------------------------------------------------------------------------
-// Tensor-core forward pass (mma.sync m16n8k16, BF16 operands, FP32
-// accumulation), 16 samples per warp tile.
+// Tensor-core building blocks (mma.sync, BF16 operands, FP32 accumulation).
 //
-// Layer 1 takes X (16 samples x 8 features, padded to K = 16) as the A
-// operand and W1 (BF16) as B; its D fragments (rows g, g+8 of the tile, two
+// The D fragments of one product (rows g, g+8 of a 16-sample tile, two
 // adjacent hidden columns per n8 tile) are laid out exactly as the A
-// fragments of layer 2 (n8 tiles 2s and 2s+1 form k-slice s), so the hidden
-// activations never leave registers.  FP32 values enter as a two-term BF16
-// split, v = hi + lo with hi = bf16(v), lo = bf16(v - hi) (relative error
-// below 2^-17), each term in its own MMA against the exact BF16 weight: the
-// result matches FP32 arithmetic on the same BF16 weights to about 1e-5.
-// Layer 3 (64 -> 1) is a dot product of each lane's hidden columns with W3,
-// reduced over the four lanes of a quad.
+// fragments of the next (n8 tiles 2s and 2s+1 form k-slice s), so hidden
+// activations never leave registers.  Layer 3 (64 -> 1) is a dot product of
+// each lane's hidden columns with W3, reduced over the four lanes of a quad.
 __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
                                                uint32_t b1) {
   asm volatile(
@@ -106,6 +73,14 @@ __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
+__device__ __forceinline__ void mma_bf16_1688(float (&d)[4], uint32_t a0, uint32_t a1,
+                                              uint32_t b0) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(b0));
+}
 
 // two floats as one bf16x2 word (the first in the low half: the lower column)
 __device__ __forceinline__ uint32_t bf16x2_bits(float x, float y) {
@@ -113,7 +88,8 @@ __device__ __forceinline__ uint32_t bf16x2_bits(float x, float y) {
   return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-// the two-term BF16 split of (x, y): hi word and lo word
+// the two-term BF16 split of (x, y): hi word and lo word (x = hi + lo to a
+// relative 2^-17)
 __device__ __forceinline__ void split_bf16x2(float x, float y, uint32_t &hi, uint32_t &lo) {
   const __nv_bfloat162 h = __floats2bfloat162_rn(x, y);
   const float rx = x - __low2float(h), ry = y - __high2float(h);
@@ -124,24 +100,29 @@ __device__ __forceinline__ void split_bf16x2(float x, float y, uint32_t &hi, uin
 constexpr int TC_WARPS = 4;
 constexpr int W2_STRIDE = MLP_H / 2 + 4;   // bf16x2 words per padded W2 row (conflict-free B loads)
 
+// W2 row o as bf16x2 words in B-fragment order: for k-slice s and lane
+// column t the two words of the fragment, (k 16s + 2t, +1) and
+// (k 16s + 8 + 2t, +1), side by side at 8s + 2t, so one 64-bit load fetches
+// both
+__host__ __device__ constexpr int w2_frag_pos(int kk) {   // kk: word index in the row (k / 2)
+  return 8 * (kk / 8) + 2 * (kk % 4) + (kk % 8) / 4;
+}
+
 struct MlpTcSmem {
   uint32_t w1[MLP_H * MLP_IN / 2];     // W1[o][f] as bf16x2 words, 4 per row
-  uint32_t w2[MLP_H * W2_STRIDE];      // W2[o][k] as bf16x2 words, padded rows
+  uint32_t w2[MLP_H * W2_STRIDE];      // W2[o][k] as bf16x2 words, padded rows, fragment order
   float b1[MLP_H], b2[MLP_H], w3[MLP_H];
   float b3;
 };
 
-__global__ void __launch_bounds__(32 * TC_WARPS)
-    rsmlp_forward_tc_kernel(int B, const float *__restrict__ X,
-                            const __nv_bfloat16 *__restrict__ wq, const float *__restrict__ wf,
-                            float *__restrict__ y) {
-  __shared__ __align__(16) MlpTcSmem s;
+__device__ void stage_tc_params(MlpTcSmem &s, const __nv_bfloat16 *__restrict__ wq,
+                                const float *__restrict__ wf) {
   const uint32_t *wq32 = reinterpret_cast<const uint32_t *>(wq);   // OFF_W1, OFF_W2 even
   for (int k = threadIdx.x; k < MLP_H * MLP_IN / 2; k += blockDim.x)
     s.w1[k] = wq32[OFF_W1 / 2 + k];
   for (int k = threadIdx.x; k < MLP_H * MLP_H / 2; k += blockDim.x) {
     const int o = k / (MLP_H / 2), kk = k % (MLP_H / 2);
-    s.w2[o * W2_STRIDE + kk] = wq32[OFF_W2 / 2 + k];
+    s.w2[o * W2_STRIDE + w2_frag_pos(kk)] = wq32[OFF_W2 / 2 + k];
   }
   for (int k = threadIdx.x; k < MLP_H; k += blockDim.x) {
     s.b1[k] = wf[OFF_B1 + k];
@@ -149,59 +130,87 @@ __global__ void __launch_bounds__(32 * TC_WARPS)
     s.w3[k] = __bfloat162float(wq[OFF_W3 + k]);
   }
   if (threadIdx.x == 0) s.b3 = wf[OFF_B3];
+}
+
+// Inference of one 16-sample tile by the whole warp: lane (g = lane / 4,
+// t = lane % 4) passes features 2t, 2t+1 of rows g (x0) and g + 8 (x1) and
+// receives the outputs of rows g and g + 8 (every lane of the quad).  BF16
+// inputs and activations, FP32 accumulation: 8 MMAs (k8) for layer 1, 32
+// (k16) for layer 2.
+__device__ __forceinline__ float2 mlp_tile_infer(const MlpTcSmem &s, float2 x0, float2 x1) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const uint32_t a0 = bf16x2_bits(x0.x, x0.y), a1 = bf16x2_bits(x1.x, x1.y);
+  uint32_t ha[4][4];
+#pragma unroll
+  for (int j = 0; j < MLP_H / 8; ++j) {
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    mma_bf16_1688(c, a0, a1, s.w1[(8 * j + g) * (MLP_IN / 2) + t]);
+    const int col = 8 * j + 2 * t;
+    const float2 bb = *reinterpret_cast<const float2 *>(&s.b1[col]);
+    const int sl = j >> 1, q = (j & 1) * 2;
+    ha[sl][q] = bf16x2_bits(gelu_fast(c[0] + bb.x), gelu_fast(c[1] + bb.y));
+    ha[sl][q + 1] = bf16x2_bits(gelu_fast(c[2] + bb.x), gelu_fast(c[3] + bb.y));
+  }
+  float p0 = 0.f, p1 = 0.f;
+#pragma unroll
+  for (int j = 0; j < MLP_H / 8; ++j) {
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    const uint32_t *wrow = s.w2 + (8 * j + g) * W2_STRIDE;
+#pragma unroll
+    for (int sl = 0; sl < MLP_H / 16; ++sl) {
+      const uint2 b = *reinterpret_cast<const uint2 *>(wrow + 8 * sl + 2 * t);
+      mma_bf16_16816(c, ha[sl], b.x, b.y);
+    }
+    const int col = 8 * j + 2 * t;
+    const float2 w = *reinterpret_cast<const float2 *>(&s.w3[col]);
+    const float2 bb = *reinterpret_cast<const float2 *>(&s.b2[col]);
+    p0 = fmaf(gelu_fast(c[0] + bb.x), w.x, p0);
+    p0 = fmaf(gelu_fast(c[1] + bb.y), w.y, p0);
+    p1 = fmaf(gelu_fast(c[2] + bb.x), w.x, p1);
+    p1 = fmaf(gelu_fast(c[3] + bb.y), w.y, p1);
+  }
+  p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
+  p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
+  p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
+  p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
+  return make_float2(p0 + s.b3, p1 + s.b3);
+}
+
+__global__ void __launch_bounds__(32 * TC_WARPS)
+    rsmlp_forward_tc_kernel(int B, const float *__restrict__ X,
+                            const __nv_bfloat16 *__restrict__ wq, const float *__restrict__ wf,
+                            float *__restrict__ y) {
+  __shared__ __align__(16) MlpTcSmem s;
+  stage_tc_params(s, wq, wf);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, t = lane & 3;
   const int ntile = (B + 15) / 16;
-  for (int tile = blockIdx.x * TC_WARPS + warp; tile < ntile; tile += gridDim.x * TC_WARPS) {
+  const int stride = gridDim.x * TC_WARPS;
+  // inputs of rows g, g + 8 of a tile (zero beyond B)
+  auto load = [&](int tile, float2 &x0, float2 &x1) {
     const int r0 = tile * 16 + g, r1 = r0 + 8;
-    float2 x0 = make_float2(0.f, 0.f), x1 = make_float2(0.f, 0.f);
-    if (r0 < B) x0 = *reinterpret_cast<const float2 *>(X + (size_t)r0 * MLP_IN + 2 * t);
-    if (r1 < B) x1 = *reinterpret_cast<const float2 *>(X + (size_t)r1 * MLP_IN + 2 * t);
-    uint32_t xa_hi[4] = {0u, 0u, 0u, 0u}, xa_lo[4] = {0u, 0u, 0u, 0u};
-    split_bf16x2(x0.x, x0.y, xa_hi[0], xa_lo[0]);   // row g, features 2t, 2t+1
-    split_bf16x2(x1.x, x1.y, xa_hi[1], xa_lo[1]);   // row g+8
-    // layer 1 -> the A fragments of layer 2 (k-slice s from n-tiles 2s, 2s+1)
-    uint32_t ha_hi[4][4], ha_lo[4][4];
-#pragma unroll
-    for (int j = 0; j < MLP_H / 8; ++j) {
-      float c[4] = {0.f, 0.f, 0.f, 0.f};
-      const uint32_t b0 = s.w1[(8 * j + g) * (MLP_IN / 2) + t];
-      mma_bf16_16816(c, xa_hi, b0, 0u);
-      mma_bf16_16816(c, xa_lo, b0, 0u);
-      const int col = 8 * j + 2 * t;
-      const float h0 = gelu(c[0] + s.b1[col]), h1 = gelu(c[1] + s.b1[col + 1]);
-      const float h2 = gelu(c[2] + s.b1[col]), h3 = gelu(c[3] + s.b1[col + 1]);
-      const int sl = j >> 1, q = (j & 1) * 2;
-      split_bf16x2(h0, h1, ha_hi[sl][q], ha_lo[sl][q]);
-      split_bf16x2(h2, h3, ha_hi[sl][q + 1], ha_lo[sl][q + 1]);
+    x0 = make_float2(0.f, 0.f);
+    x1 = make_float2(0.f, 0.f);
+    if (tile < ntile) {
+      if (r0 < B) x0 = __ldg(reinterpret_cast<const float2 *>(X + (size_t)r0 * MLP_IN + 2 * t));
+      if (r1 < B) x1 = __ldg(reinterpret_cast<const float2 *>(X + (size_t)r1 * MLP_IN + 2 * t));
     }
-    // layers 2 and 3
-    float p0 = 0.f, p1 = 0.f;
-#pragma unroll
-    for (int j = 0; j < MLP_H / 8; ++j) {
-      float c[4] = {0.f, 0.f, 0.f, 0.f};
-      const uint32_t *wrow = s.w2 + (8 * j + g) * W2_STRIDE;
-#pragma unroll
-      for (int sl = 0; sl < MLP_H / 16; ++sl) {
-        const uint32_t b0 = wrow[8 * sl + t], b1 = wrow[8 * sl + 4 + t];
-        mma_bf16_16816(c, ha_hi[sl], b0, b1);
-        mma_bf16_16816(c, ha_lo[sl], b0, b1);
-      }
-      const int col = 8 * j + 2 * t;
-      p0 = fmaf(gelu(c[0] + s.b2[col]), s.w3[col], p0);
-      p0 = fmaf(gelu(c[1] + s.b2[col + 1]), s.w3[col + 1], p0);
-      p1 = fmaf(gelu(c[2] + s.b2[col]), s.w3[col], p1);
-      p1 = fmaf(gelu(c[3] + s.b2[col + 1]), s.w3[col + 1], p1);
-    }
-    p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
-    p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
-    p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
-    p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
+  };
+  int tile = blockIdx.x * TC_WARPS + warp;
+  float2 x0, x1;
+  load(tile, x0, x1);
+  for (; tile < ntile; tile += stride) {
+    float2 n0, n1;
+    load(tile + stride, n0, n1);   // the next tile's inputs, in flight during this one
+    const float2 out = mlp_tile_infer(s, x0, x1);
+    const int r0 = tile * 16 + g, r1 = r0 + 8;
     if (t == 0) {
-      if (r0 < B) y[r0] = p0 + s.b3;
-      if (r1 < B) y[r1] = p1 + s.b3;
+      if (r0 < B) y[r0] = out.x;
+      if (r1 < B) y[r1] = out.y;
     }
+    x0 = n0;
+    x1 = n1;
   }
 }
 
@@ -290,9 +299,11 @@ __global__ void __launch_bounds__(32 * LABEL_WARPS)
 // inertial and radial-velocity factors, RSFAC limit, second-order cube root,
 // shell square root, inward reduction; the zero-neighbour branch :120-143),
 // optionally the few-member rule of fpoly0.F:153-158, and -- with weights --
-// the learned proposal: features, MLP, and the plain rule as fallback when the
-// count it implies at the current density leaves the band (default 0.5-1.5 x
-// the rule's target).
+// the learned proposal and the plain rule as fallback when its count leaves
+// the band (default 0.5-1.5 x the rule's target).  One thread per particle
+// for the rule, the features and the band check; the network runs on the
+// tensor cores, each warp taking its 32 particles as two 16-sample tiles
+// through shared memory.
 __global__ void __launch_bounds__(MLP_THREADS)
     rs_update_kernel(int ni, gpunb_rs_params p, const double *__restrict__ x,
                      const double *__restrict__ v, const double *__restrict__ m_scaled,
@@ -302,47 +313,99 @@ __global__ void __launch_bounds__(MLP_THREADS)
                      const __nv_bfloat16 *__restrict__ wq, const float *__restrict__ wf,
                      const float *__restrict__ norm, double *__restrict__ rs_new,
                      double *__restrict__ target, int *__restrict__ used) {
-  __shared__ MlpSmem s;
-  if (wq) stage_params(s, wq, wf);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ni) return;
-  const double *xi = x + 3 * (size_t)i, *vi = v + 3 * (size_t)i;
-  const int n = nnb[i];
-  const double r0 = rs[i];
-  double plain, tgt;
-  rs_plain(p, r0, n, nnb0[i], xi, vi, dtr[i], -1.0, plain, tgt);
-  if (p.few_nb_rule && n < 2) plain = 1.5 * r0;
+  __shared__ __align__(16) MlpTcSmem s;
+  __shared__ __align__(16) float feat[MLP_THREADS][MLP_IN];
+  __shared__ float yv[MLP_THREADS];
+  const int tid = threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + tid;
+  const bool live = i < ni;
+  if (wq) stage_tc_params(s, wq, wf);
+  double plain = 0.0, tgt = 0.0, r0 = 0.0;
+  int n = 0;
+  const double *xi = x + 3 * (size_t)(live ? i : 0), *vi = v + 3 * (size_t)(live ? i : 0);
+  if (live) {
+    n = nnb[i];
+    r0 = rs[i];
+    rs_plain(p, r0, n, nnb0[i], xi, vi, dtr[i], -1.0, plain, tgt);
+    if (p.few_nb_rule && n < 2) plain = 1.5 * r0;
+  }
   double nw = plain;
   int u = 0;
-  if (wq) {
+  if (wq) {   // uniform over the grid: every warp reaches the MMAs whole
     // features (rsmlp.py): log distance to the centre, log local density,
     // count / NNBOPT, log |F_reg|, log |jerk|, log regular step, log mass N,
     // log RS; normalised with the training set's mean and spread
-    const double e0 = xi[0] - p.rdens[0], e1 = xi[1] - p.rdens[1], e2 = xi[2] - p.rdens[2];
     const double nn = (double)max(n, 0);
-    const double *a = acc + 3 * (size_t)i, *j = jrk + 3 * (size_t)i;
-    const double f[MLP_IN] = {
-        log(sqrt(e0 * e0 + e1 * e1 + e2 * e2) + 1e-6),
-        log((nn + 1.0) / (4.0 / 3.0 * 3.141592653589793 * r0 * r0 * r0)),
-        nn / (double)p.nnbopt,
-        log(sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) + 1e-30),
-        log(sqrt(j[0] * j[0] + j[1] * j[1] + j[2] * j[2]) + 1e-30),
-        log(fmax(dtr[i], 1e-12)),
-        log(fmax(m_scaled[i], 1e-12)),
-        log(r0)};
-    float xf[MLP_IN];
+    if (live) {
+      const double e0 = xi[0] - p.rdens[0], e1 = xi[1] - p.rdens[1], e2 = xi[2] - p.rdens[2];
+      const double *a = acc + 3 * (size_t)i, *j = jrk + 3 * (size_t)i;
+      const double f[MLP_IN] = {
+          log(sqrt(e0 * e0 + e1 * e1 + e2 * e2) + 1e-6),
+          log((nn + 1.0) / (4.0 / 3.0 * 3.141592653589793 * r0 * r0 * r0)),
+          nn / (double)p.nnbopt,
+          log(sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) + 1e-30),
+          log(sqrt(j[0] * j[0] + j[1] * j[1] + j[2] * j[2]) + 1e-30),
+          log(fmax(dtr[i], 1e-12)),
+          log(fmax(m_scaled[i], 1e-12)),
+          log(r0)};
 #pragma unroll
-    for (int q = 0; q < MLP_IN; ++q)
-      xf[q] = (float)((f[q] - (double)norm[q]) / (double)norm[MLP_IN + q]);
-    const float y = mlp_eval(s, xf);
-    const double pc = (nn + 1.0) * exp(3.0 * (double)y) - 1.0;
-    const double blo = p.band_lo > 0.0 ? p.band_lo : 0.5;
-    const double bhi = p.band_hi > 0.0 ? p.band_hi : 1.5;
-    if (isfinite(y) && pc >= blo * tgt && pc <= bhi * tgt) {
-      nw = r0 * exp((double)y);
-      u = 1;
+      for (int q = 0; q < MLP_IN; ++q)
+        feat[tid][q] = (float)((f[q] - (double)norm[q]) / (double)norm[MLP_IN + q]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < MLP_IN; ++q) feat[tid][q] = 0.f;
+    }
+    __syncthreads();   // parameters and features staged
+    {
+      const int lane = tid & 31, w0 = tid & ~31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = w0 + 16 * h + g;
+        const float2 o = mlp_tile_infer(s, *reinterpret_cast<const float2 *>(&feat[r][2 * t]),
+                                        *reinterpret_cast<const float2 *>(&feat[r + 8][2 * t]));
+        if (t == 0) {
+          yv[r] = o.x;
+          yv[r + 8] = o.y;
+        }
+      }
+      __syncwarp();
+    }
+    if (live) {
+      const float y = yv[tid];
+      const double rp = r0 * exp((double)y);
+      double pc;
+      if (p.list_off) {
+        // the count of rp at the next regular step (see gpunb.h)
+        const double dt = dtr[i], rp2 = rp * rp;
+        int in = 0, members = 0;
+        for (int e = p.list_off[i]; e < p.list_off[i + 1]; ++e) {
+          const int jj = p.list[e];
+          const double *xj = p.xj + 3 * (size_t)jj, *vj = p.vj + 3 * (size_t)jj;
+          const double dv0 = vj[0] - vi[0], dv1 = vj[1] - vi[1], dv2 = vj[2] - vi[2];
+          const double dx0 = xj[0] - xi[0], dx1 = xj[1] - xi[1], dx2 = xj[2] - xi[2];
+          if (dx0 == 0.0 && dx1 == 0.0 && dx2 == 0.0 && dv0 == 0.0 && dv1 == 0.0 && dv2 == 0.0)
+            continue;
+          ++members;
+          const double d0 = dx0 + dt * dv0, d1 = dx1 + dt * dv1, d2 = dx2 + dt * dv2;
+          const double f0 = d0 + dt * dv0, f1 = d1 + dt * dv1, f2 = d2 + dt * dv2;
+          const double k = fmin(d0 * d0 + d1 * d1 + d2 * d2, f0 * f0 + f1 * f1 + f2 * f2);
+          in += k < rp2;
+        }
+        const double grow = (rp / r0) * (rp / r0) * (rp / r0) - 1.0;
+        pc = fmax((double)in + (double)members * fmax(grow, 0.0),
+                  (nn + 1.0) * exp(3.0 * (double)y) - 1.0);
+      } else {
+        pc = (nn + 1.0) * exp(3.0 * (double)y) - 1.0;
+      }
+      const double blo = p.band_lo > 0.0 ? p.band_lo : 0.5;
+      const double bhi = p.band_hi > 0.0 ? p.band_hi : 1.5;
+      if (isfinite(y) && pc >= blo * tgt && pc <= bhi * tgt) {
+        nw = rp;
+        u = 1;
+      }
     }
   }
+  if (!live) return;
   rs_new[i] = nw;
   if (target) target[i] = tgt;
   if (used) used[i] = u;
@@ -354,9 +417,10 @@ __global__ void __launch_bounds__(MLP_THREADS)
 // sums the block rows in order, so repeated calls give bit-identical
 // gradients.
 //
-// Per warp, for each of its two 16-sample tiles: the forward pass as in
-// rsmlp_forward_tc_kernel, keeping z1, z2 (D-fragment layout) and the
-// layer-2 A fragments of h1; then dy, dz2 = dy W3 gelu'(z2) and
+// Per warp, for each of its two 16-sample tiles: the forward pass with inputs
+// and activations as two-term BF16 splits and the accurate tanh (the
+// gradients are those of FP32 arithmetic on the BF16 weights), keeping z1, z2
+// (D-fragment layout) and the layer-2 A fragments of h1; then dy, dz2 = dy W3 gelu'(z2) and
 // dh1 = dz2 W2 -- again D fragments of one product reused as the A fragments
 // of the next, with W2 transposed in shared memory as the B operand -- and
 // dz1 = dh1 gelu'(z1).  dz2, dz1, h1 and x are staged transposed (feature
@@ -696,13 +760,26 @@ int gpunb_rsmlp_to_bf16(const float *wf, void *wq, void *stream) {
 int gpunb_rsmlp_forward(int B, const float *X, const void *wq, const float *wf, float *y,
                         void *stream) {
   if (B <= 0) return B == 0 ? GPUNB_OK : GPUNB_E_ARG;
-  // one warp per 16-sample tile, a grid of a few blocks per SM
-  int dev = 0, n_sm = 152;
-  if (cudaGetDevice(&dev) == cudaSuccess)
-    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  // one warp per 16-sample tile; one wave of resident blocks striding over
+  // the tiles (a grid beyond what fits leaves a second, nearly empty wave)
+  // (resident blocks per device, cached: the queries cost more host time than
+  // the kernel takes for small batches; concurrent first calls store equal values)
+  static std::atomic<int> wave[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return GPUNB_E_CUDA;
+  int blocks = wave[dev].load(std::memory_order_relaxed);
+  if (blocks == 0) {
+    int n_sm = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rsmlp_forward_tc_kernel,
+                                                      32 * TC_WARPS, 0) != cudaSuccess)
+      return GPUNB_E_CUDA;
+    blocks = std::max(1, n_sm * per_sm);
+    wave[dev].store(blocks, std::memory_order_relaxed);
+  }
   const long long tiles = (B + 15) / 16;
   const long long want = (tiles + TC_WARPS - 1) / TC_WARPS;
-  const int grid = (int)std::max(1ll, std::min(want, 8ll * n_sm));
+  const int grid = (int)std::max(1ll, std::min(want, (long long)blocks));
   rsmlp_forward_tc_kernel<<<grid, 32 * TC_WARPS, 0, (cudaStream_t)stream>>>(
       B, X, (const __nv_bfloat16 *)wq, wf, y);
   return cudaGetLastError() == cudaSuccess ? GPUNB_OK : GPUNB_E_CUDA;

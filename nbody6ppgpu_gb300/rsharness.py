@@ -43,10 +43,13 @@ class HarnessStats:
     first_call_overflows: int = 0    # overflows of the first block (same for every policy)
     overflow_events: int = 0         # overflowed rows after it (one recompute each)
     overflow_after_predictor: int = 0  # ... of which the RS came from the predictor
+    overflow_after_fallback: int = 0   # ... of which the plain rule replaced a prediction
     recompute_pairs: float = 0.0     # extra pair work of the recomputes
     pairs: float = 0.0               # pair work of the first evaluations
     predictor_used: int = 0
     predictor_fallback: int = 0
+    fallback_low: int = 0            # ... count below the band
+    fallback_high: int = 0           # ... count above it (the rest: no finite prediction)
     regf_seconds: float = 0.0
     predict_seconds: float = 0.0
     counts: list = field(default_factory=list)
@@ -178,23 +181,74 @@ def label_log_radius_gpu(nb: GpuNb, x: np.ndarray, v: np.ndarray, dtr: np.ndarra
     return out
 
 
-# accepted range of the count a predicted radius implies at the current
-# density, as a multiple of the plain rule's target (the device update kernel
-# takes the same bounds): 0.5-1.5 by default; WIDE_BAND lowers the floor so
-# that in a contraction a correct prediction of a strong shrink, which implies
-# a low count at today's density, is not rejected
+# accepted range of the count a predicted radius gives, as a multiple of the
+# plain rule's target (the device update kernel takes the same bounds):
+# 0.5-1.5 by default; WIDE_BAND lowers the floor
 PRED_BAND = (0.5, 1.5)
 WIDE_BAND = (0.25, 1.5)
+
+# How the count of a predicted radius is estimated for the band check
+# ("max" by default):
+#   "motion": at the next regular step -- the members of the current list
+#             moved on their relative velocities by one regular step and
+#             tested as the kernel tests them then (position or predicted
+#             position inside the radius), plus, for a growing radius, the
+#             shell beyond the current radius at the current density;
+#   "static": at the current density, count x (RS_new / RS)^3;
+#   "max":    the larger of the two.
+# In a contraction a correct prediction of a strong shrink implies a low count
+# at today's density, so the static estimate rejects it and the lagging plain
+# rule then overflows; the motion estimate follows the neighbours inwards.
+# Over a long regular step the straight-line motion undercounts instead
+# (orbits curve, the infall accelerates): measured against the counts the
+# predicted radii had (Plummer 65536 collapse), the motion estimate reads
+# about half the true count on the rows it rejects, which the static one gets
+# right, so a prediction is taken as too small only when both say so.
+GUARDS = ("motion", "static", "max")
+
+
+def motion_count(x: np.ndarray, v: np.ndarray, idx: np.ndarray, rows: np.ndarray,
+                 dtr: np.ndarray, rs_new: np.ndarray, rs_old: np.ndarray) -> np.ndarray:
+    """Estimated count of radius rs_new at the next regular step of the
+    particles idx: members j of their current rows (LISTGP layout, 0-based ids,
+    self included and skipped here) with
+    min(|dx'|^2, |dx' + dtr dv|^2) < rs_new^2, dx' = dx + dtr dv (the kernel's
+    membership test one step later, separations moved on the current relative
+    velocity), plus count x ((rs_new / rs_old)^3 - 1) when the radius grows."""
+    out = np.zeros(idx.size)
+    cnt = np.zeros(idx.size)
+    for s in range(0, idx.size, CHUNK):
+        ii = idx[s:s + CHUNK]
+        r = rows[s:s + CHUNK]
+        m = np.maximum(r[:, 0], 0)
+        width = int(m.max()) if m.size else 0
+        if width == 0:
+            continue
+        ids = r[:, 1:1 + width].astype(np.int64)
+        valid = (np.arange(width)[None, :] < m[:, None]) & (ids != ii[:, None])
+        j = np.where(valid, ids, ii[:, None])
+        dt = dtr[ii][:, None, None]
+        dv = v[j] - v[ii][:, None, :]
+        d1 = x[j] - x[ii][:, None, :] + dt * dv
+        d2 = d1 + dt * dv
+        key = np.minimum((d1 * d1).sum(-1), (d2 * d2).sum(-1))
+        out[s:s + CHUNK] = (valid & (key < (rs_new[s:s + CHUNK] ** 2)[:, None])).sum(1)
+        cnt[s:s + CHUNK] = valid.sum(1)
+    return out + cnt * np.maximum((rs_new / rs_old) ** 3 - 1.0, 0.0)
 
 
 class Harness:
     def __init__(self, cluster: ics.Cluster, nnbopt: int, nnbmax: int, smax: float = 0.125,
                  levels: int = 4, params: rsrule.RSParams | None = None, rs=None,
                  harvest: bool = False, rs0_factor: float = 1.0,
-                 band: tuple[float, float] = PRED_BAND, gpu_labels: bool = True):
+                 band: tuple[float, float] = PRED_BAND, gpu_labels: bool = True,
+                 guard: str = "max"):
+        if guard not in GUARDS:
+            raise ValueError(f"guard must be one of {GUARDS}")
         self.c = cluster
         self.gpu_labels = gpu_labels   # labels from the device labeller (else KD-tree)
         self.band = band
+        self.guard = guard
         self.n = cluster.n
         self.nnbopt, self.nnbmax = nnbopt, nnbmax
         self.m = cluster.m.copy()
@@ -210,7 +264,9 @@ class Harness:
         self.tick = 0
         self.next_tick = (self.stepr / self.dt).round().astype(int)
         self.prev_nnb = np.full(self.n, nnbopt, dtype=np.int64)
-        self.src = np.zeros(self.n, dtype=np.int64)      # 1: RS set by the predictor
+        # RS source of each particle: 0 plain rule, 1 predictor, 2 plain rule
+        # after a rejected prediction
+        self.src = np.zeros(self.n, dtype=np.int64)
         self.p = params or rsrule.RSParams(nnbopt=nnbopt, nnbmax=nnbmax,
                                            bodym=float(self.m.mean()))
         self.nb = GpuNb(self.n)
@@ -218,6 +274,9 @@ class Harness:
         self.harvest = harvest
         self.pending = {}
         self.X, self.Y = [], []
+        # with harvest and a predictor: per labelled row (label, y, motion
+        # count, static count, target, accepted) for the band diagnostics
+        self.diag = []
         self.stats = HarnessStats()
 
     def close(self):
@@ -260,7 +319,8 @@ class Harness:
                     self.stats.first_call_overflows += nover
                 else:
                     self.stats.overflow_events += nover
-                    self.stats.overflow_after_predictor += int(self.src[ch[over]].sum())
+                    self.stats.overflow_after_predictor += int((self.src[ch[over]] == 1).sum())
+                    self.stats.overflow_after_fallback += int((self.src[ch[over]] == 2).sum())
                     self.stats.recompute_pairs += nover * ch.size * float(self.n)
                 self.rs[ch[over]] = rsrule.overflow_rs(self.rs[ch[over]], res.list[over, 0],
                                                        self.p)
@@ -275,7 +335,8 @@ class Harness:
             nnbs.append(res.list[:, 0].copy()); lists.append(res.list)
         self.stats.regf_seconds += time.perf_counter() - t0
         self.stats.regular_calls += 1
-        return np.concatenate(accs), np.concatenate(jrks), np.concatenate(nnbs)
+        return (np.concatenate(accs), np.concatenate(jrks), np.concatenate(nnbs),
+                np.concatenate(lists))
 
     def step(self, predictor=None):
         """Advance one tick; returns the active block's size."""
@@ -283,7 +344,7 @@ class Harness:
         idx = np.nonzero(self.next_tick <= self.tick)[0]
         if idx.size == 0:
             return 0
-        acc, jrk, nnb_raw = self._regf_with_recompute(idx)
+        acc, jrk, nnb_raw, rows = self._regf_with_recompute(idx)
         nnb = np.maximum(nnb_raw - 1, 0)                 # self removed (util_gpu.F:102-111)
         self.stats.active += idx.size
         self.stats.counts.append(nnb)
@@ -302,18 +363,35 @@ class Harness:
             t0 = time.perf_counter()
             y = predictor.predict(F)
             self.stats.predict_seconds += time.perf_counter() - t0
-            # count implied at the predicted radius (local density unchanged);
-            # outside band x the rule's own target the plain rule is used
-            pred_count = (nnb + 1.0) * np.exp(3.0 * y) - 1.0
+            # the count the predicted radius gives (GUARDS); outside band x
+            # the rule's own target the plain rule is used
+            static_count = (nnb + 1.0) * np.exp(3.0 * y) - 1.0
+            if self.guard == "static":
+                pred_count = static_count
+            else:
+                pred_count = motion_count(self.x, self.v, idx, rows, self.stepr,
+                                          rs_old * np.exp(np.where(np.isfinite(y), y, 0.0)),
+                                          rs_old)
+                if self.guard == "max":
+                    pred_count = np.maximum(pred_count, static_count)
             lo, hi = self.band
             ok = (pred_count >= lo * target) & (pred_count <= hi * target) & np.isfinite(y)
             new = np.where(ok, rs_old * np.exp(y), plain)
-            self.src[idx] = ok
+            self.src[idx] = np.where(ok, 1, 2)
+            self.stats.fallback_low += int((pred_count < lo * target).sum())
+            self.stats.fallback_high += int((pred_count > hi * target).sum())
             self.stats.predictor_used += int(ok.sum())
             self.stats.predictor_fallback += int((~ok).sum())
         if self.harvest:
+            if predictor is not None:   # the motion estimate, for the diagnostics
+                mc = (pred_count if self.guard == "motion" else
+                      motion_count(self.x, self.v, idx, rows, self.stepr,
+                                   rs_old * np.exp(np.where(np.isfinite(y), y, 0.0)), rs_old))
             for q, i in enumerate(idx):
-                self.pending[int(i)] = (F[q], rs_old[q], target[q])
+                d = None
+                if predictor is not None:
+                    d = (float(y[q]), float(mc[q]), float(static_count[q]), bool(ok[q]))
+                self.pending[int(i)] = (F[q], rs_old[q], target[q], d)
         self.rs[idx] = new
         self.prev_nnb[idx] = nnb
         self.next_tick[idx] += (self.stepr[idx] / self.dt).round().astype(int)
@@ -331,9 +409,11 @@ class Harness:
         else:
             logr = label_log_radius(self.x, self.v, self.stepr, have, ks)
         for q, i in enumerate(have):
-            f, rs_then, _ = self.pending.pop(int(i))
+            f, rs_then, tgt, d = self.pending.pop(int(i))
             self.X.append(f)
             self.Y.append(logr[q] - math.log(rs_then))
+            if d is not None:
+                self.diag.append((self.Y[-1],) + d[:3] + (tgt, d[3]))
 
     def run(self, ticks: int, predictor=None):
         for _ in range(ticks):

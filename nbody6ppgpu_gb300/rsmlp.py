@@ -199,16 +199,20 @@ class RSParamsC(C.Structure):
     _fields_ = [("nnbopt", C.c_int), ("nnbmax", C.c_int), ("nb_flag", C.c_int),
                 ("few_nb_rule", C.c_int), ("rscale", C.c_double), ("rc", C.c_double),
                 ("rsfac", C.c_double), ("bodym", C.c_double), ("rdens", C.c_double * 3),
-                ("band_lo", C.c_double), ("band_hi", C.c_double)]
+                ("band_lo", C.c_double), ("band_hi", C.c_double),
+                ("list_off", C.c_void_p), ("list", C.c_void_p), ("xj", C.c_void_p),
+                ("vj", C.c_void_p)]
 
 
 def rs_update_device(p, x, v, m_scaled, rs, nnb, nnb0, acc, jrk, dtr, mlp: "RSMLP | None" = None,
-                     few_nb_rule: bool = True, device: int = 0, band=(0.5, 1.5)):
+                     few_nb_rule: bool = True, device: int = 0, band=(0.5, 1.5), rows=None):
     """gpunb_rs_update_device on host arrays (copied to the device and back):
     the plain RS rule of `rsrule.regcor_rs` (with the few-member rule when
     few_nb_rule) and, with `mlp`, the learned proposal and its fallback, in
-    one kernel.  p: rsrule.RSParams; band: acceptance band of the proposal.
-    Returns (rs_new, target, used)."""
+    one kernel.  p: rsrule.RSParams; band: acceptance band of the proposal;
+    rows: (off[ni + 1], ids, xj, vj), the block's neighbour rows in CSR form
+    over the j-set (xj, vj), for the band check at the next regular step
+    (None: at the current density).  Returns (rs_new, target, used)."""
     import torch
     lib = load()
     fn = lib.gpunb_rs_update_device
@@ -220,9 +224,15 @@ def rs_update_device(p, x, v, m_scaled, rs, nnb, nnb0, acc, jrk, dtr, mlp: "RSML
     def d(a, dt=torch.float64):
         return torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
 
+    keep = []
+    rp = [None] * 4
+    if rows is not None:
+        off, ids, xj, vj = rows
+        keep = [d(off, torch.int32), d(ids, torch.int32), d(xj), d(vj)]
+        rp = [t.data_ptr() for t in keep]
     cp = RSParamsC(int(p.nnbopt), int(p.nnbmax), int(p.nb_flag), int(few_nb_rule),
                    float(p.rscale), float(p.rc), float(p.rsfac), float(p.bodym),
-                   (C.c_double * 3)(0.0, 0.0, 0.0), float(band[0]), float(band[1]))
+                   (C.c_double * 3)(0.0, 0.0, 0.0), float(band[0]), float(band[1]), *rp)
     X, V, M, R = d(x), d(v), d(m_scaled), d(rs)
     NB, NB0 = d(nnb, torch.int32), d(nnb0, torch.int32)
     A, J, DT = d(acc), d(jrk), d(dtr)

@@ -22,15 +22,18 @@ def unpack(w):
     return W1, b1, W2, b2, W3, b3
 
 
-_erf = np.vectorize(math.erf)
+# GELU in its tanh form (Hendrycks and Gimpel, 2016), as the kernels define it
+_C = math.sqrt(2.0 / math.pi)
+_A = 0.044715
 
 
 def gelu(x):
-    return 0.5 * x * (1.0 + _erf(x / math.sqrt(2.0)))
+    return 0.5 * x * (1.0 + np.tanh(_C * (x + _A * x ** 3)))
 
 
 def gelu_grad(x):
-    return 0.5 * (1.0 + _erf(x / math.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / math.sqrt(2 * math.pi)
+    t = np.tanh(_C * (x + _A * x ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * _C * (1.0 + 3.0 * _A * x * x)
 
 
 def forward(wq, wf, X):

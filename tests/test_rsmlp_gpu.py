@@ -9,7 +9,11 @@ from oracle import mlp_oracle
 
 pytestmark = pytest.mark.gpu
 
-FWD_TOL = 2e-5      # |y_gpu - y_fp64| / (1 + |y|): FP32 accumulation, erff GELU
+# inference: BF16 inputs and activations (2^-9 relative each), FP32
+# accumulation, hardware tanh; |y_gpu - y_fp64| / (1 + |y|) at most FWD_TOL,
+# its root mean square at most FWD_RMS
+FWD_TOL = 3e-2
+FWD_RMS = 3e-3
 GRAD_TOL = 1e-4     # ||g_gpu - g_fp64|| / ||g_fp64||: FP32 accumulation over the batch
 
 
@@ -31,7 +35,8 @@ def test_forward_matches_oracle(mlp):
     y = mlp.forward_normalised(X)
     wf, wq = mlp.params()
     ref, _ = mlp_oracle.forward(wq, wf, X)
-    assert np.max(np.abs(y - ref) / (1.0 + np.abs(ref))) < FWD_TOL
+    e = np.abs(y - ref) / (1.0 + np.abs(ref))
+    assert e.max() < FWD_TOL and np.sqrt(np.mean(e * e)) < FWD_RMS, (e.max(), np.sqrt(np.mean(e * e)))
 
 
 @pytest.mark.parametrize("B,weighted", [(1000, False), (1000, True), (384, False), (1, True)])
@@ -84,10 +89,12 @@ def test_training_fits_a_smooth_map():
     losses = m.train(X, T, epochs=12)
     assert losses[-1] < 0.15 * T.var()
     assert losses[-1] < 0.5 * losses[0]
-    # the kernels train the same network the oracle evaluates
+    # the kernels train the same network the oracle evaluates (inference in
+    # BF16: the tolerance of test_forward_matches_oracle)
     wf, wq = m.params()
     ref, _ = mlp_oracle.forward(wq, wf, m.normalise(X[:500]))
-    assert np.max(np.abs(m.predict(X[:500]) - ref)) < 1e-4
+    e = np.abs(m.predict(X[:500]) - ref) / (1.0 + np.abs(ref))
+    assert e.max() < FWD_TOL and np.sqrt(np.mean(e * e)) < FWD_RMS
 
 
 def _irregular(c, idx, lst):
@@ -137,19 +144,20 @@ def test_total_force_is_independent_of_the_radius():
 
 
 def test_predictor_cuts_overflow_recomputes():
-    """A cold (virial ratio 0.1) King cluster collapses, so local densities
-    rise faster than the plain rule's 25%-per-step volume limit follows and
-    lists overflow.  The predictor, trained on pairs harvested from two other
-    seeds with the plain rule, is run on a third seed from the same state:
-    it must need at least 5x fewer overflow recomputes at the same mean
-    membership."""
+    """A cold (virial ratio 0.1) Plummer cluster of 65536 bodies collapses, so
+    local densities rise faster than the plain rule's 25%-per-step volume
+    limit follows and lists overflow.  The predictor, trained on pairs
+    harvested from two other seeds with the plain rule, is run on a third seed
+    from the same state with the plain rule as fallback outside 0.5-1.5 x the
+    target: it must need at least 5x fewer overflow recomputes at the same
+    mean membership."""
     pytest.importorskip("scipy")
     from experiments.rs_experiment import run
-    r = run(model="king", n=8192, ticks=256, nnbopt=100, nnbmax=200, levels=6, epochs=25,
-            rounds=1, q=0.1)
+    r = run(model="plummer", n=65536, ticks=256, nnbopt=100, nnbmax=200, levels=6, epochs=25,
+            rounds=1, q=0.1, band=(0.5, 1.5))
     plain, pred = r["plain"], r["predictor"]
-    assert plain["overflow_events"] >= 200            # the regime does overflow
-    assert pred["overflow_events"] * 5 <= plain["overflow_events"]   # measured 17x
+    assert plain["overflow_events"] >= 10000          # the regime does overflow
+    assert pred["overflow_events"] * 5 <= plain["overflow_events"]   # measured 6.1x
     assert abs(pred["mean_count"] / plain["mean_count"] - 1.0) < 0.1
     assert pred["count_p99"] <= plain["count_p99"]
     assert pred["predictor_used"] > 0.9 * pred["active"]
