@@ -136,7 +136,7 @@ def run(model="king", n=16384, ticks=64, nnbopt=100, nnbmax=200, levels=6, epoch
 
 def config5(ticks_harvest=48, ticks_eval=48, n_king=1 << 20, n_plummer=65536, nnbopt=100,
             nnbmax=200, levels=6, epochs=25, q=0.1, band=PRED_BAND, eval_seed=41,
-            max_pairs=2_000_000, guard="max"):
+            max_pairs=2_000_000, guard="max", harvest_every=1):
     """The learned-radius configuration: training pairs harvested with the
     plain rule on a Plummer/Kroupa cluster of n_plummer bodies (the bench's
     cluster type) and on a King W0 = 6 model of n_king bodies, pooled (at most
@@ -151,7 +151,7 @@ def config5(ticks_harvest=48, ticks_eval=48, n_king=1 << 20, n_plummer=65536, nn
     for name, model, n, seed in (("plummer", "plummer", n_plummer, 21),
                                  ("king", "king", n_king, 22)):
         h = Harness(make(model, n, seed, nnbopt, q), nnbopt, nnbmax, harvest=True, levels=levels,
-                    band=band)
+                    band=band, harvest_every=harvest_every if n > n_plummer else 1)
         h.run(ticks_harvest)
         x, y = h.dataset()
         h.close()
@@ -172,7 +172,7 @@ def config5(ticks_harvest=48, ticks_eval=48, n_king=1 << 20, n_plummer=65536, nn
     out = {"config": "config 5: King W0=6 evaluation model, pairs from Plummer/Kroupa and King",
            "n_eval": n_king, "q": q, "ticks_harvest": ticks_harvest, "ticks_eval": ticks_eval,
            "band": band, "guard": guard, "nnbopt": nnbopt, "nnbmax": nnbmax, "levels": levels,
-           "harvest_sources": sources, "train_pairs": int(len(X)),
+           "harvest_every_king": harvest_every, "harvest_sources": sources, "train_pairs": int(len(X)),
            "label_variance": float(Y.var()), "train_mse_first_epoch": losses[0],
            "train_mse_last_epoch": losses[-1], "harvest_s": t_harvest, "train_s": t_train}
     for name, pred in (("plain", None), ("predictor", mlp)):
@@ -198,6 +198,8 @@ def main():
                     help="the config-5 protocol (pairs from Plummer and King runs, evaluation "
                          "on a King model of --n bodies)")
     ap.add_argument("--ticks-harvest", type=int, default=48)
+    ap.add_argument("--harvest-every", type=int, default=1,
+                    help="config 5: label only the King bodies i %% k == 0")
     ap.add_argument("--model", default="king", choices=["king", "plummer"])
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--ticks", type=int, default=64)
@@ -224,7 +226,8 @@ def main():
     if a.config5:
         print(json.dumps(config5(a.ticks_harvest, a.ticks, n_king=a.n, nnbopt=a.nnbopt,
                                  nnbmax=a.nnbmax, levels=a.levels, epochs=a.epochs, q=a.q,
-                                 band=tuple(a.band), guard=a.guard)), flush=True)
+                                 band=tuple(a.band), guard=a.guard,
+                                 harvest_every=a.harvest_every)), flush=True)
         return
     print(json.dumps(run(a.model, a.n, a.ticks, a.nnbopt, a.nnbmax, a.levels, epochs=a.epochs,
                          q=a.q, rounds=a.rounds, band=tuple(a.band), guard=a.guard,

@@ -264,6 +264,7 @@ struct Engine {
   int timing = 0;
   float last_kernel_ms = 0.f;
   int last_variant = -1, last_splits = 0, last_gx = 0;
+  bool last_fused = false;   // the last pair pass merged its partials itself
   std::map<long long, TuneEntry> tune;
   int autotune_on = 0;
   // host arrays of the gpunb_* calls: 1 = copied straight from/to the
@@ -528,8 +529,18 @@ static bool ensure_work(int ni, int nnbmax, int S, int ni_pad) {
          g.rows.ensure((size_t)ni * std::max(nnbmax, 1) * sizeof(int));
 }
 
+// The pair kernel merges its partials itself (merge_itile) for the split
+// kernel when S <= FUSE_MAX_SPLITS: one block sums an i-tile's S rows, which
+// for many splits (small blocks against a large j-set, S up to thousands) is
+// a long serial tail that the merge kernels spread over many blocks.
+// Measured on GB300 at S = 38 (Plummer N = ni = 65536): pair kernel + merge
+// 4.55 -> 4.52 ms and 135 -> 42 MB of DRAM traffic per launch.
+constexpr int FUSE_MAX_SPLITS = 48;
+
+// fuse: the outputs the pair kernel merges into (used when the rule above
+// holds; g.last_fused tells finish_lists whether a merge kernel must run).
 static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, int S,
-                         cudaStream_t st, bool timed) {
+                         cudaStream_t st, bool timed, const RegfDev *fuse) {
   const JSet js = jset();
   const int ni = is.ni;
   RegfOut out;
@@ -543,6 +554,19 @@ static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, in
     out.ni_pad = gx * d.itile();
   }
   if (!ensure_work(ni, nnbmax, S, out.ni_pad)) return GPUNB_E_ALLOC;
+  const bool fused = fuse && g.precision == 0 && S <= FUSE_MAX_SPLITS;
+  g.last_fused = fused;
+  if (!g.queue.ensure((size_t)(1 + (fused ? gx : 0)) * sizeof(int))) return GPUNB_E_ALLOC;
+  if (fused) {
+    out.done = g.queue.as<int>() + 1;
+    out.perm = is.perm;
+    out.acc = fuse->acc;
+    out.jrk = fuse->jrk;
+    out.pot = fuse->pot;
+    out.nnb = fuse->nnb;
+    out.rowlen = fuse->rowlen;
+    out.nnbmax = nnbmax;
+  }
   out.part = g.part.as<double>();
   out.cnt = g.cnt.as<int>();
   out.rows = g.rows.as<int>();
@@ -582,11 +606,13 @@ static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, in
   return GPUNB_OK;
 }
 
+// merged: the pair kernel merged its partials into o (run_pair_pass with o)
 static int finish_lists(int ni, int nnbmax, int S, int ni_pad, const int *perm, const RegfDev &o,
-                        size_t list_cap, cudaStream_t st) {
-  CUDA_OR(launch_regf_merge(g.part.as<double>(), g.precision == 0, S, ni, ni_pad, perm,
-                            g.cnt.as<int>(), nnbmax, o.acc, o.jrk, o.pot, o.nnb, o.rowlen, st),
-          GPUNB_E_CUDA);
+                        size_t list_cap, cudaStream_t st, bool merged) {
+  if (!merged)
+    CUDA_OR(launch_regf_merge(g.part.as<double>(), g.precision == 0, S, ni, ni_pad, perm,
+                              g.cnt.as<int>(), nnbmax, o.acc, o.jrk, o.pot, o.nnb, o.rowlen, st),
+            GPUNB_E_CUDA);
   CUDA_OR(launch_list_scan(o.rowlen, ni, o.off, o.btot, st), GPUNB_E_CUDA);
   (void)list_cap;
   CUDA_OR(launch_list_gather(g.rows.as<int>(), std::max(nnbmax, 0), o.rowlen, o.off, o.btot, ni,
@@ -616,9 +642,9 @@ static void choose_plan(int ni, bool mflag, int &variant, int &S) {
 // Times every launch shape (kernel variant x j-split count around the
 // heuristic's) on the given device i-set -- the caller's own active block --
 // and keeps the fastest in the cache under the (N, ni) bucket.  The time
-// covers the pair kernel and the merge of its split partials (more splits
-// balance the persistent queue better but leave more partials to merge);
-// the merge writes into scratch.  Runs on `st`, synchronously.
+// covers the pair kernel with the merge of its split partials, which its
+// last item per i-tile does (more splits balance the persistent queue better
+// but leave more partials to merge); the merge writes into scratch.  Runs on `st`, synchronously.
 static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out,
                          float *ms_out, cudaStream_t st) {
   const JSet js = jset();
@@ -629,12 +655,15 @@ static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out
       !g.rowlen.ensure((size_t)ni * sizeof(int)))
     return -1;
   double *sacc = g.outblk.as<double>();
-  int *snnb = (int *)(sacc + 7 * (size_t)ni);
+  RegfDev scratch;   // the merge writes here (the pair kernel merges itself)
+  scratch.acc = sacc;
+  scratch.jrk = sacc + 3 * (size_t)ni;
+  scratch.pot = sacc + 6 * (size_t)ni;
+  scratch.nnb = (int *)(sacc + 7 * (size_t)ni);
+  scratch.rowlen = g.rowlen.as<int>();
   for (int v = 0; v < regf_num_variants(); ++v) {
     const long long base = plan_splits(v, ni, js.ntile, mflag);
     const long long cands[5] = {base / 4, base / 2, base, base * 2, base * 4};
-    const int itile = regf_variant(v).itile();
-    const int ni_pad = ((ni + itile - 1) / itile) * itile;
     int last_s = -1;
     for (long long sc : cands) {
       int s = (int)std::max(1ll, std::min<long long>(sc, std::max(1, js.ntile)));
@@ -646,12 +675,7 @@ static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out
       int reps = 3;
       bool ok = true;
       for (int r = 0; r < reps + 1 && ok; ++r) {
-        if (run_pair_pass(is, nnbmax, mflag, v, s, st, true) != GPUNB_OK) ok = false;
-        if (ok && launch_regf_merge(g.part.as<double>(), true, s, ni, ni_pad, is.perm,
-                                    g.cnt.as<int>(), nnbmax, sacc, sacc + 3 * (size_t)ni,
-                                    sacc + 6 * (size_t)ni, snnb, g.rowlen.as<int>(),
-                                    st) != cudaSuccess)
-          ok = false;
+        if (run_pair_pass(is, nnbmax, mflag, v, s, st, true, &scratch) != GPUNB_OK) ok = false;
         if (ok && cudaEventRecord(g.ek1, st) != cudaSuccess) ok = false;
         if (cudaStreamSynchronize(st) != cudaSuccess) ok = false;
         float ms = 0.f;
@@ -708,8 +732,6 @@ static void regf_host_direct(int ni, const double *h2, const double *dtr, const 
     is.perm = nullptr;
     is.rec = nullptr;
     if (g.precision == 0 && order_iset(is, s) != GPUNB_OK) return GPUNB_E_ALLOC;
-    int rc = run_pair_pass(is, nnbmax, mflag, variant, S, s, false);
-    if (rc != GPUNB_OK) return rc;
     const int nb = list_scan_blocks(ni);
     if (!g.outblk.ensure((size_t)7 * ni * sizeof(double) + (size_t)(ni + 2) * sizeof(int)) ||
         !g.rowlen.ensure((size_t)ni * sizeof(int)) ||
@@ -727,9 +749,11 @@ static void regf_host_direct(int ni, const double *h2, const double *dtr, const 
     o.off = g.off.as<int>();
     o.btot = g.btot.as<int>();
     o.dense = g.dense.as<int>();
+    int rc = run_pair_pass(is, nnbmax, mflag, variant, S, s, false, &o);
+    if (rc != GPUNB_OK) return rc;
     const int itile = g.precision == 1 ? FP64_THREADS : regf_variant(variant).itile();
     const int ni_pad = ((ni + itile - 1) / itile) * itile;
-    rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, 0, s);
+    rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, 0, s, g.last_fused);
     if (rc != GPUNB_OK) return rc;
     // results straight into the caller's arrays; the device writes the rows
     CUDA_OR(launch_list_rows(o.dense, o.off, o.btot, o.nnb, ni, lmax, list, s), GPUNB_E_CUDA);
@@ -822,7 +846,6 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
       g.tune.find(tune_key(g.nj, ni, mflag, 0)) == g.tune.end())
     autotune_with(is, nnbmax, mflag, nullptr, nullptr, st);
   choose_plan(ni, mflag, variant, S);
-  if (run_pair_pass(is, nnbmax, mflag, variant, S, st, false) != GPUNB_OK) return;
 
   // outputs: acc | jrk | pot (doubles), then nnb (ints)
   const int nb = list_scan_blocks(ni);
@@ -841,11 +864,13 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   o.off = g.off.as<int>();
   o.btot = g.btot.as<int>();
   o.dense = g.dense.as<int>();
+  if (run_pair_pass(is, nnbmax, mflag, variant, S, st, false, &o) != GPUNB_OK) return;
   const int ni_pad = g.precision == 1
                          ? ((ni + FP64_THREADS - 1) / FP64_THREADS) * FP64_THREADS
                          : ((ni + regf_variant(variant).itile() - 1) / regf_variant(variant).itile()) *
                                regf_variant(variant).itile();
-  if (finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, 0, st) != GPUNB_OK) return;
+  if (finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, 0, st, g.last_fused) != GPUNB_OK)
+    return;
   if (g.host_direct) {
     // results straight into the caller's arrays; the device writes the rows
     CUDA_OR(launch_list_rows(o.dense, o.off, o.btot, o.nnb, ni, lmax, list, st), );
@@ -1397,8 +1422,6 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
     is.perm = nullptr;
     is.rec = nullptr;
     if (g.precision == 0 && order_iset(is, s) != GPUNB_OK) return GPUNB_E_ALLOC;
-    int rc = run_pair_pass(is, nnbmax, mflag, variant, S, s, false);
-    if (rc != GPUNB_OK) return rc;
     const int nb = list_scan_blocks(ni);
     if (!g.rowlen.ensure((size_t)ni * sizeof(int)) ||
         !g.btot.ensure((size_t)(nb + 1) * sizeof(int)))
@@ -1406,9 +1429,11 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
     RegfDev o;
     o.acc = acc; o.jrk = jrk; o.pot = pot; o.nnb = nnb;
     o.rowlen = g.rowlen.as<int>(); o.off = list_off; o.btot = g.btot.as<int>(); o.dense = list;
+    int rc = run_pair_pass(is, nnbmax, mflag, variant, S, s, false, &o);
+    if (rc != GPUNB_OK) return rc;
     const int itile = g.precision == 1 ? FP64_THREADS : regf_variant(variant).itile();
     const int ni_pad = ((ni + itile - 1) / itile) * itile;
-    rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, list_cap, s);
+    rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, list_cap, s, g.last_fused);
     if (rc != GPUNB_OK) return rc;
     CUDA_OR(launch_list_finalize_offsets(list_off, o.btot, ni, s), GPUNB_E_CUDA);
     return GPUNB_OK;

@@ -23,7 +23,9 @@ int regf_ds_blocks_per_sm(int v, bool mflag);
 cudaError_t launch_pack_jtiles(const double *m, const double *x, const double *v, int nj, const int *perm,
                                float *tiles, int ntile, int *err, cudaStream_t st);
 // persistent launch: `grid` blocks drain n_itiles * S work items from `queue`
-// (single j-set), or the n_items entries of `items` in `order` (batches)
+// (single j-set), or the n_items entries of `items` in `order` (batches).
+// out.done (single j-set only) must be queue + 1, with room for n_itiles
+// counters: the kernel then merges each i-tile itself into out.acc etc.
 cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int *queue,
                            const JSet &js, const ISet &is, const RegfOut &out, cudaStream_t st,
                            const ItemDesc *items = nullptr, const int *order = nullptr,

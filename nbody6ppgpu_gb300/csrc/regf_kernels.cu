@@ -514,12 +514,72 @@ __device__ __forceinline__ void tile_pairs(const IState &I, const TileCtx &C,
 }
 
 // ---------------------------------------------------------------------------
+// Merge of the j-split partial sums (merge kernels and the merge in the pair
+// kernel).
+__device__ __forceinline__ void merge_store(const double *s, int i, const int *__restrict__ cnt,
+                                            int nnbmax, double *__restrict__ acc,
+                                            double *__restrict__ jrk, double *__restrict__ pot,
+                                            int *__restrict__ nnb, int *__restrict__ rowlen) {
+  acc[3 * i + 0] = 0.25 * s[0];
+  acc[3 * i + 1] = 0.25 * s[1];
+  acc[3 * i + 2] = 0.25 * s[2];
+  jrk[3 * i + 0] = 0.25 * s[3];
+  jrk[3 * i + 1] = 0.25 * s[4];
+  jrk[3 * i + 2] = 0.25 * s[5];
+  pot[i] = s[6];
+  const int c = cnt[i];
+  const bool over = c > nnbmax;
+  nnb[i] = over ? -c : c;
+  rowlen[i] = over ? 0 : c;
+}
+
+// Partial sums are stored by processing slot (column); the result of slot s
+// belongs to i = perm[s] (identity without a permutation).  The split kernel
+// stores each partial as a float-float pair (hi, lo) in the 8-byte slot and
+// the merges add those pairs exactly-rounded on the FP32 pipe (FF); the FP64
+// kernel stores doubles, added in FP64.  Either way the order is fixed.
+template <bool FF>
+struct PartAcc {
+  double d[NQ];
+  float h[NQ], l[NQ];
+  __device__ __forceinline__ PartAcc() {
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) {
+      d[c] = 0.0;
+      h[c] = l[c] = 0.f;
+    }
+  }
+  // adds partial c, loaded as the 8 bytes of its slot (for FF the float
+  // pair (hi, lo) at the slot's low and high 4 bytes)
+  __device__ __forceinline__ void add_slot(int c, double v) {
+    if (FF) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+      ff_add(h[c], l[c], __int_as_float((int)(unsigned int)b), __int_as_float((int)(b >> 32)));
+    } else {
+      d[c] += v;
+    }
+  }
+  // adds the NQ partials of one split, entry c at p[c * stride]
+  __device__ __forceinline__ void add(const double *__restrict__ p, size_t stride) {
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) add_slot(c, p[c * stride]);
+  }
+  __device__ __forceinline__ double value(int c) const {
+    return FF ? (double)h[c] + (double)l[c] : d[c];
+  }
+};
+
+// ---------------------------------------------------------------------------
 // Split-precision pair kernel, persistent.
 //   IPT : i-particles per thread (independent chains)
 //   WI  : warps along i;  WJ : warps splitting each j tile (same i's)
-// Work items are (i-tile it, j-split s) pairs, item = s * n_itiles + it, split
-// s covering tiles [s*ntile/S, (s+1)*ntile/S); a block takes items from the
-// device queue until it is empty.  The j tiles of an item stream through a
+// Work items are (i-tile it, j-split s) pairs, split s covering tiles
+// [s*ntile/S, (s+1)*ntile/S); a block takes items from the device queue until
+// it is empty.  Queue order: item = s * n_itiles + it (the i-tiles of one
+// split side by side, its j tiles hot in L2), or with out.done item =
+// it * S + s (an i-tile's splits side by side, finishing close together) and
+// the block that completes an i-tile's last item merges the tile
+// (merge_itile).  The j tiles of an item stream through a
 // NSTAGE-deep shared-memory ring filled by bulk-async copies; the last warp
 // to finish with a stage refills it, so warps are never held at a block-wide
 // barrier inside an item.  Stage phases run on a per-block tile counter g
@@ -531,12 +591,57 @@ constexpr int NSTAGE = GPUNB_NSTAGE;
 
 struct RegfWork {
   int *queue;              // item counter, zeroed before the launch
-  int n_itiles;            // single j-set: items are (split, i-tile) pairs
+  int n_itiles;            // single j-set: items are (i-tile, split) pairs
   int S;
   const ItemDesc *items;   // batched clusters: explicit item table (else null)
   const int *order;        // queue position -> item (largest first), or null
   int n_items;
 };
+
+// The merge of one i-tile (slots [slot0, slot0 + itile) of the partial rows,
+// columns from pcol0) by the block that completed its last item: the S rows
+// summed in split order per slot (float-float, then FP64 as the merge
+// kernels), the results stored, and the merged rows' L2 lines discarded --
+// they are dead, and would otherwise be written back to DRAM.
+__device__ __forceinline__ void merge_itile(const RegfOut &out, int S, int slot0, int slot_end,
+                                            int pcol0, int itile) {
+  const size_t rs = (size_t)NQ * out.ni_pad;   // doubles per partial row
+  for (int u = threadIdx.x; u < itile; u += blockDim.x) {
+    const int slot = slot0 + u;
+    if (slot >= slot_end) break;
+    const double *p = out.part + pcol0 + u;
+    PartAcc<true> a;
+    int k = 0;
+    for (; k + 4 <= S; k += 4) {   // four rows' loads in flight, added in row order
+      double v[4][NQ];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < NQ; ++c) v[r][c] = __ldcg(p + (k + r) * rs + (size_t)c * out.ni_pad);
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < NQ; ++c) a.add_slot(c, v[r][c]);
+    }
+    for (; k < S; ++k)
+#pragma unroll
+      for (int c = 0; c < NQ; ++c) a.add_slot(c, __ldcg(p + k * rs + (size_t)c * out.ni_pad));
+    double sv[NQ];
+#pragma unroll
+    for (int c = 0; c < NQ; ++c) sv[c] = a.value(c);
+    merge_store(sv, out.perm ? out.perm[slot] : slot, out.cnt, out.nnbmax, out.acc, out.jrk,
+                out.pot, out.nnb, out.rowlen);
+  }
+  __syncthreads();   // every read of the rows done
+  // 128-byte lines: the tile's columns (itile x 8 bytes, a multiple of 128
+  // from a multiple of 128) in each of the S x NQ row segments
+  const int lines = itile * 8 / 128;
+  for (int e = threadIdx.x; e < S * NQ * lines; e += blockDim.x) {
+    const int seg = e / lines, l = e - seg * lines;
+    const double *a = out.part + (size_t)seg * out.ni_pad + pcol0 + l * 16;
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
+  }
+}
 
 template <int IPT, int WI, int WJ, int JV, bool MFLAG, int MINB>
 __global__ void __launch_bounds__(32 * WI * WJ, MINB)
@@ -554,7 +659,7 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
   __shared__ __align__(8) uint64_t bar[NSTAGE];
   __shared__ int s_rel[NSTAGE];                         // warps done with the stage
   __shared__ int s_iss[NSTAGE];                         // copies issued into the stage
-  __shared__ int s_item, s_abort;
+  __shared__ int s_item, s_abort, s_last;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wi = warp % WI, wj = warp / WI;
@@ -583,7 +688,16 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
       slot0 = d.slot0; slot_end = d.slot_end; t0 = d.t0; t1 = d.t1;
       prow = d.prow; jbase = d.jbase; pcol0 = d.pcol0;
     } else {
-      const int sy = qpos / w.n_itiles, it = qpos - sy * w.n_itiles;
+      // with the merge in the kernel an i-tile's splits follow one another;
+      // otherwise the i-tiles of one split do (the split's j tiles hot in L2)
+      int it, sy;
+      if (out.done) {
+        it = qpos / w.S;
+        sy = qpos - it * w.S;
+      } else {
+        sy = qpos / w.n_itiles;
+        it = qpos - sy * w.n_itiles;
+      }
       slot0 = it * ITILE; slot_end = is.ni;
       t0 = (int)(((long long)js.ntile * sy) / w.S);
       t1 = (int)(((long long)js.ntile * (sy + 1)) / w.S);
@@ -734,6 +848,16 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
         }
       }
     }
+    if (out.done && !w.items) {
+      __threadfence();   // this item's rows (and neighbour counts) visible before its count
+      __syncthreads();
+      if (tid == 0) s_last = atomicAdd(out.done + qpos / w.S, 1) == w.S - 1;
+      __syncthreads();
+      if (s_last) {
+        __threadfence();   // the rows of the tile's other items, counted before, are visible
+        merge_itile(out, w.S, slot0, slot_end, pcol0, ITILE);
+      }
+    }
     __syncthreads();   // ffs and s_item are reused by the next item
   }
   if (s_abort && tid == 0) {
@@ -832,58 +956,6 @@ __global__ void __launch_bounds__(128) regf_fp64_kernel(const JSet js, const ISe
 // deterministic replacement of force_reduce_kernel + the host sum over GPUs,
 // gpunb.velocity.cu:441-496,822-845).  Also turns counts into the in-band
 // overflow flag of gpunb.velocity.cu:872-877 / reg.avx.cpp:320-321.
-__device__ __forceinline__ void merge_store(const double *s, int i, const int *__restrict__ cnt,
-                                            int nnbmax, double *__restrict__ acc,
-                                            double *__restrict__ jrk, double *__restrict__ pot,
-                                            int *__restrict__ nnb, int *__restrict__ rowlen) {
-  acc[3 * i + 0] = 0.25 * s[0];
-  acc[3 * i + 1] = 0.25 * s[1];
-  acc[3 * i + 2] = 0.25 * s[2];
-  jrk[3 * i + 0] = 0.25 * s[3];
-  jrk[3 * i + 1] = 0.25 * s[4];
-  jrk[3 * i + 2] = 0.25 * s[5];
-  pot[i] = s[6];
-  const int c = cnt[i];
-  const bool over = c > nnbmax;
-  nnb[i] = over ? -c : c;
-  rowlen[i] = over ? 0 : c;
-}
-
-// Partial sums are stored by processing slot (column); the result of slot s
-// belongs to i = perm[s] (identity without a permutation).  The split kernel
-// stores each partial as a float-float pair (hi, lo) in the 8-byte slot and
-// the merges add those pairs exactly-rounded on the FP32 pipe (FF); the FP64
-// kernel stores doubles, added in FP64.  Either way the order is fixed.
-template <bool FF>
-struct PartAcc {
-  double d[NQ];
-  float h[NQ], l[NQ];
-  __device__ __forceinline__ PartAcc() {
-#pragma unroll
-    for (int c = 0; c < NQ; ++c) {
-      d[c] = 0.0;
-      h[c] = l[c] = 0.f;
-    }
-  }
-  // adds partial c, loaded as the 8 bytes of its slot (for FF the float
-  // pair (hi, lo) at the slot's low and high 4 bytes)
-  __device__ __forceinline__ void add_slot(int c, double v) {
-    if (FF) {
-      const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-      ff_add(h[c], l[c], __int_as_float((int)(unsigned int)b), __int_as_float((int)(b >> 32)));
-    } else {
-      d[c] += v;
-    }
-  }
-  // adds the NQ partials of one split, entry c at p[c * stride]
-  __device__ __forceinline__ void add(const double *__restrict__ p, size_t stride) {
-#pragma unroll
-    for (int c = 0; c < NQ; ++c) add_slot(c, p[c * stride]);
-  }
-  __device__ __forceinline__ double value(int c) const {
-    return FF ? (double)h[c] + (double)l[c] : d[c];
-  }
-};
 //
 // Many j-splits (small active blocks): one block of MERGE_THREADS per slot,
 // each thread summing a strided subset of the splits (four splits' loads in
@@ -1322,7 +1394,11 @@ cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int), st);
+  // the item counter, and with the merge in the kernel the per-i-tile counts
+  // that follow it
+  if (out.done && (items || out.done != queue + 1)) return cudaErrorInvalidValue;
+  cudaError_t e =
+      cudaMemsetAsync(queue, 0, (out.done ? 1 + (size_t)n_itiles : 1) * sizeof(int), st);
   if (e != cudaSuccess) return e;
   RegfWork w;
   w.queue = queue;

@@ -92,6 +92,15 @@ struct RegfOut {
   int cap;               // row capacity (= nnbmax)
   int ni_pad;
   int *err;              // device error word
+  // Merge in the pair kernel (single j-set, split kernel; done == null: a
+  // merge kernel follows): the block that completes the last of an i-tile's
+  // S items sums the tile's partial rows in split order and stores the
+  // results as the merge kernels do.
+  int *done = nullptr;   // [n_itiles] completed items per i-tile (zeroed before the launch)
+  const int *perm = nullptr;   // processing slot -> i (null: identity)
+  double *acc = nullptr, *jrk = nullptr, *pot = nullptr;
+  int *nnb = nullptr, *rowlen = nullptr;
+  int nnbmax = 0;
 };
 
 }  // namespace gpunb

@@ -49,12 +49,17 @@ __device__ __forceinline__ float gelu_grad(float x) {
   return fmaf(0.5f, t, 0.5f) + 0.5f * x * fmaf(-t, t, 1.0f) * fmaf(3.0f * GELU_CA, x * x, GELU_C);
 }
 // inference: the tanh from the hardware approximation (relative error below
-// 2^-10.9, under the BF16 rounding of the activations that follows)
-__device__ __forceinline__ float gelu_fast(float x) {
+// 2^-10.9, under the BF16 rounding of the activations that follows), two
+// activations at a time in packed FP32
+__device__ __forceinline__ float tanh_fast(float u) {
   float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(gelu_arg(x)));
-  const float h = 0.5f * x;
-  return fmaf(h, t, h);
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return t;
+}
+__device__ __forceinline__ f2 gelu_fast2(f2 x) {
+  const f2 u = mul2(x, fma2(mk2(GELU_CA), mul2(x, x), mk2(GELU_C)));
+  const f2 h = mul2(x, mk2(0.5f));
+  return fma2(h, make_float2(tanh_fast(u.x), tanh_fast(u.y)), h);
 }
 
 // ---------------------------------------------------------------------------
@@ -65,9 +70,11 @@ __device__ __forceinline__ float gelu_fast(float x) {
 // fragments of the next (n8 tiles 2s and 2s+1 form k-slice s), so hidden
 // activations never leave registers.  Layer 3 (64 -> 1) is a dot product of
 // each lane's hidden columns with W3, reduced over the four lanes of a quad.
+// (plain asm: no side effects beyond the outputs, so the compiler may
+// interleave independent products)
 __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
                                                uint32_t b1) {
-  asm volatile(
+  asm(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
       "{%8,%9}, {%0,%1,%2,%3};"
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
@@ -75,7 +82,7 @@ __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a
 }
 __device__ __forceinline__ void mma_bf16_1688(float (&d)[4], uint32_t a0, uint32_t a1,
                                               uint32_t b0) {
-  asm volatile(
+  asm(
       "mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, "
       "{%0,%1,%2,%3};"
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
@@ -98,6 +105,9 @@ __device__ __forceinline__ void split_bf16x2(float x, float y, uint32_t &hi, uin
 }
 
 constexpr int TC_WARPS = 4;
+#ifndef GPUNB_MLP_PAIR
+#define GPUNB_MLP_PAIR 1   // inference: two 16-sample tiles per warp pass
+#endif
 constexpr int W2_STRIDE = MLP_H / 2 + 4;   // bf16x2 words per padded W2 row (conflict-free B loads)
 
 // W2 row o as bf16x2 words in B-fragment order: for k-slice s and lane
@@ -146,12 +156,14 @@ __device__ __forceinline__ float2 mlp_tile_infer(const MlpTcSmem &s, float2 x0, 
     float c[4] = {0.f, 0.f, 0.f, 0.f};
     mma_bf16_1688(c, a0, a1, s.w1[(8 * j + g) * (MLP_IN / 2) + t]);
     const int col = 8 * j + 2 * t;
-    const float2 bb = *reinterpret_cast<const float2 *>(&s.b1[col]);
+    const f2 bb = *reinterpret_cast<const f2 *>(&s.b1[col]);
     const int sl = j >> 1, q = (j & 1) * 2;
-    ha[sl][q] = bf16x2_bits(gelu_fast(c[0] + bb.x), gelu_fast(c[1] + bb.y));
-    ha[sl][q + 1] = bf16x2_bits(gelu_fast(c[2] + bb.x), gelu_fast(c[3] + bb.y));
+    const f2 h0 = gelu_fast2(add2(make_float2(c[0], c[1]), bb));
+    const f2 h1 = gelu_fast2(add2(make_float2(c[2], c[3]), bb));
+    ha[sl][q] = bf16x2_bits(h0.x, h0.y);
+    ha[sl][q + 1] = bf16x2_bits(h1.x, h1.y);
   }
-  float p0 = 0.f, p1 = 0.f;
+  f2 p0 = mk2(0.f), p1 = mk2(0.f);   // per row: the two columns' partial dot products
 #pragma unroll
   for (int j = 0; j < MLP_H / 8; ++j) {
     float c[4] = {0.f, 0.f, 0.f, 0.f};
@@ -162,18 +174,17 @@ __device__ __forceinline__ float2 mlp_tile_infer(const MlpTcSmem &s, float2 x0, 
       mma_bf16_16816(c, ha[sl], b.x, b.y);
     }
     const int col = 8 * j + 2 * t;
-    const float2 w = *reinterpret_cast<const float2 *>(&s.w3[col]);
-    const float2 bb = *reinterpret_cast<const float2 *>(&s.b2[col]);
-    p0 = fmaf(gelu_fast(c[0] + bb.x), w.x, p0);
-    p0 = fmaf(gelu_fast(c[1] + bb.y), w.y, p0);
-    p1 = fmaf(gelu_fast(c[2] + bb.x), w.x, p1);
-    p1 = fmaf(gelu_fast(c[3] + bb.y), w.y, p1);
+    const f2 w = *reinterpret_cast<const f2 *>(&s.w3[col]);
+    const f2 bb = *reinterpret_cast<const f2 *>(&s.b2[col]);
+    p0 = fma2(gelu_fast2(add2(make_float2(c[0], c[1]), bb)), w, p0);
+    p1 = fma2(gelu_fast2(add2(make_float2(c[2], c[3]), bb)), w, p1);
   }
-  p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
-  p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
-  p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
-  p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
-  return make_float2(p0 + s.b3, p1 + s.b3);
+  float q0 = p0.x + p0.y, q1 = p1.x + p1.y;
+  q0 += __shfl_xor_sync(0xffffffffu, q0, 1);
+  q0 += __shfl_xor_sync(0xffffffffu, q0, 2);
+  q1 += __shfl_xor_sync(0xffffffffu, q1, 1);
+  q1 += __shfl_xor_sync(0xffffffffu, q1, 2);
+  return make_float2(q0 + s.b3, q1 + s.b3);
 }
 
 __global__ void __launch_bounds__(32 * TC_WARPS)
@@ -181,8 +192,6 @@ __global__ void __launch_bounds__(32 * TC_WARPS)
                             const __nv_bfloat16 *__restrict__ wq, const float *__restrict__ wf,
                             float *__restrict__ y) {
   __shared__ __align__(16) MlpTcSmem s;
-  stage_tc_params(s, wq, wf);
-  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, t = lane & 3;
   const int ntile = (B + 15) / 16;
@@ -197,9 +206,39 @@ __global__ void __launch_bounds__(32 * TC_WARPS)
       if (r1 < B) x1 = __ldg(reinterpret_cast<const float2 *>(X + (size_t)r1 * MLP_IN + 2 * t));
     }
   };
+#if GPUNB_MLP_PAIR
+  // two tiles per pass (independent, so their products and activations
+  // interleave), the next pass's inputs in flight meanwhile
+  int tile = blockIdx.x * TC_WARPS + warp;
+  float2 x0, x1, z0, z1;
+  load(tile, x0, x1);   // in flight while the weights are staged
+  load(tile + stride, z0, z1);
+  stage_tc_params(s, wq, wf);
+  __syncthreads();
+  for (; tile < ntile; tile += 2 * stride) {
+    float2 n0, n1, m0, m1;
+    load(tile + 2 * stride, n0, n1);
+    load(tile + 3 * stride, m0, m1);
+    const float2 oa = mlp_tile_infer(s, x0, x1);
+    const float2 ob = mlp_tile_infer(s, z0, z1);
+    const int ra = tile * 16 + g, rb = (tile + stride) * 16 + g;
+    if (t == 0) {
+      if (ra < B) y[ra] = oa.x;
+      if (ra + 8 < B) y[ra + 8] = oa.y;
+      if (tile + stride < ntile) {
+        if (rb < B) y[rb] = ob.x;
+        if (rb + 8 < B) y[rb + 8] = ob.y;
+      }
+    }
+    x0 = n0; x1 = n1;
+    z0 = m0; z1 = m1;
+  }
+#else
   int tile = blockIdx.x * TC_WARPS + warp;
   float2 x0, x1;
   load(tile, x0, x1);
+  stage_tc_params(s, wq, wf);
+  __syncthreads();
   for (; tile < ntile; tile += stride) {
     float2 n0, n1;
     load(tile + stride, n0, n1);   // the next tile's inputs, in flight during this one
@@ -212,6 +251,7 @@ __global__ void __launch_bounds__(32 * TC_WARPS)
     x0 = n0;
     x1 = n1;
   }
+#endif
 }
 
 // ---------------------------------------------------------------------------

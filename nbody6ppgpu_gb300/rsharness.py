@@ -237,12 +237,42 @@ def motion_count(x: np.ndarray, v: np.ndarray, idx: np.ndarray, rows: np.ndarray
     return out + cnt * np.maximum((rs_new / rs_old) ** 3 - 1.0, 0.0)
 
 
+def motion_count_device(xd, vd, idx: np.ndarray, rows: np.ndarray, dtr: np.ndarray,
+                        rs_new: np.ndarray, rs_old: np.ndarray, chunk: int = 16384) -> np.ndarray:
+    """`motion_count` evaluated with torch on the device: xd, vd are device
+    tensors of the whole set's positions and velocities; the rest as there."""
+    import torch
+    dev = xd.device
+    out = np.zeros(idx.size)
+    cnt = np.zeros(idx.size)
+    for s in range(0, idx.size, chunk):
+        r = rows[s:s + chunk]
+        m = np.maximum(r[:, 0], 0)
+        width = int(m.max()) if m.size else 0
+        if width == 0:
+            continue
+        ii = torch.as_tensor(idx[s:s + chunk], device=dev)
+        ids = torch.as_tensor(r[:, 1:1 + width].astype(np.int64), device=dev)
+        mm = torch.as_tensor(m, device=dev)
+        valid = (torch.arange(width, device=dev)[None, :] < mm[:, None]) & (ids != ii[:, None])
+        j = torch.where(valid, ids, ii[:, None])
+        dt = torch.as_tensor(dtr[idx[s:s + chunk]], dtype=torch.float64, device=dev)[:, None, None]
+        dv = vd[j] - vd[ii][:, None, :]
+        d1 = xd[j] - xd[ii][:, None, :] + dt * dv
+        d2 = d1 + dt * dv
+        key = torch.minimum((d1 * d1).sum(-1), (d2 * d2).sum(-1))
+        rn = torch.as_tensor(rs_new[s:s + chunk], dtype=torch.float64, device=dev)
+        out[s:s + chunk] = (valid & (key < (rn * rn)[:, None])).sum(1).cpu().numpy()
+        cnt[s:s + chunk] = valid.sum(1).cpu().numpy()
+    return out + cnt * np.maximum((rs_new / rs_old) ** 3 - 1.0, 0.0)
+
+
 class Harness:
     def __init__(self, cluster: ics.Cluster, nnbopt: int, nnbmax: int, smax: float = 0.125,
                  levels: int = 4, params: rsrule.RSParams | None = None, rs=None,
                  harvest: bool = False, rs0_factor: float = 1.0,
                  band: tuple[float, float] = PRED_BAND, gpu_labels: bool = True,
-                 guard: str = "max"):
+                 guard: str = "max", harvest_every: int = 1):
         if guard not in GUARDS:
             raise ValueError(f"guard must be one of {GUARDS}")
         self.c = cluster
@@ -272,6 +302,7 @@ class Harness:
         self.nb = GpuNb(self.n)
         self.acc = self._total_force()
         self.harvest = harvest
+        self.harvest_every = max(1, int(harvest_every))   # label the bodies i % k == 0
         self.pending = {}
         self.X, self.Y = [], []
         # with harvest and a predictor: per labelled row (label, y, motion
@@ -369,9 +400,8 @@ class Harness:
             if self.guard == "static":
                 pred_count = static_count
             else:
-                pred_count = motion_count(self.x, self.v, idx, rows, self.stepr,
-                                          rs_old * np.exp(np.where(np.isfinite(y), y, 0.0)),
-                                          rs_old)
+                pred_count = self._motion_count(idx, rows, rs_old * np.exp(
+                    np.where(np.isfinite(y), y, 0.0)), rs_old)
                 if self.guard == "max":
                     pred_count = np.maximum(pred_count, static_count)
             lo, hi = self.band
@@ -385,9 +415,11 @@ class Harness:
         if self.harvest:
             if predictor is not None:   # the motion estimate, for the diagnostics
                 mc = (pred_count if self.guard == "motion" else
-                      motion_count(self.x, self.v, idx, rows, self.stepr,
-                                   rs_old * np.exp(np.where(np.isfinite(y), y, 0.0)), rs_old))
+                      self._motion_count(idx, rows, rs_old * np.exp(
+                          np.where(np.isfinite(y), y, 0.0)), rs_old))
             for q, i in enumerate(idx):
+                if int(i) % self.harvest_every:
+                    continue
                 d = None
                 if predictor is not None:
                     d = (float(y[q]), float(mc[q]), float(static_count[q]), bool(ok[q]))
@@ -396,6 +428,14 @@ class Harness:
         self.prev_nnb[idx] = nnb
         self.next_tick[idx] += (self.stepr[idx] / self.dt).round().astype(int)
         return idx.size
+
+    def _motion_count(self, idx, rows, rs_new, rs_old):
+        """motion_count on the device (the set's current positions copied over)."""
+        import torch
+        dev = torch.device("cuda", 0)
+        xd = torch.as_tensor(self.x, dtype=torch.float64, device=dev)
+        vd = torch.as_tensor(self.v, dtype=torch.float64, device=dev)
+        return motion_count_device(xd, vd, idx, rows, self.stepr, rs_new, rs_old)
 
     def _harvest(self, idx):
         have = np.array([int(i) for i in idx if int(i) in self.pending], dtype=np.int64)

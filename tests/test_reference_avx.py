@@ -30,8 +30,8 @@ def test_fresh_inputs_against_reference(seed, n, target, m_flag):
 def test_port_keeps_pace_with_the_reference_cpu_path():
     """The FP32 port (the CPU baseline on the aarch64 GPU host, where the
     reference's x86 AVX source does not build) runs within 1.35x of the
-    reference's own reg.avx.cpp on the same host threads: best of five
-    interleaved runs of a 4096-particle block against N = 65536, in the
+    reference's own reg.avx.cpp on the same host threads: best of seven
+    interleaved runs (after one untimed pass) of a 4096-particle block against N = 65536, in the
     caller's chunks of 1024 (measured here: 1.0x to 1.2x).  Its lists equal the
     reference's except in rows holding a pair whose criterion value lies
     within FP32 rounding of h2 (at most two here)."""
@@ -42,13 +42,14 @@ def test_port_keeps_pace_with_the_reference_cpu_path():
     ref, port = O.RefAVX(1 << 17), O.Port()
     best = {"ref": 1e9, "port": 1e9}
     lists = {}
-    for _ in range(5):
+    for rep in range(8):   # the first pass warms both up and is not timed
         for name, impl in (("ref", ref), ("port", port)):
             impl.send(c.m, c.x, c.v)
             t = time.perf_counter()
             out = [impl.regf(h2[act[k:k + 1024]], c.dtr[act[k:k + 1024]], c.x[act[k:k + 1024]],
                              c.v[act[k:k + 1024]], 513, 512) for k in range(0, act.size, 1024)]
-            best[name] = min(best[name], time.perf_counter() - t)
+            if rep > 0:
+                best[name] = min(best[name], time.perf_counter() - t)
             lists[name] = np.concatenate([o[3] for o in out])
     ref.close()
     assert len(rows_equal(lists["port"], lists["ref"])) <= 2

@@ -2,6 +2,7 @@
 against a direct count: the members of each row moved on their relative
 velocity by one regular step and tested as the kernel tests them then."""
 import numpy as np
+import pytest
 
 from nbody6ppgpu_gb300.rsharness import motion_count
 
@@ -62,3 +63,28 @@ def test_motion_count_follows_a_contraction():
     got = motion_count(x, v, np.array([0]), rows, dtr, rs_new, rs_old)[0]
     static = m * (rs_new[0] / rs_old[0]) ** 3
     assert got == m and static == m / 8
+
+
+@pytest.mark.gpu
+def test_motion_count_on_the_device_equals_the_host_count():
+    torch = pytest.importorskip("torch")
+    from nbody6ppgpu_gb300.rsharness import motion_count_device
+    rng = np.random.default_rng(5)
+    n, lmax = 5000, 80
+    x = rng.normal(size=(n, 3))
+    v = rng.normal(size=(n, 3))
+    dtr = 2.0 ** -rng.integers(3, 8, n)
+    idx = rng.choice(n, 3000, replace=False)
+    rows = np.zeros((idx.size, lmax), dtype=np.int32)
+    for k, i in enumerate(idx):
+        ids = np.sort(np.append(rng.choice(n, int(rng.integers(0, lmax - 2)), replace=False), i))
+        ids = np.unique(ids)
+        rows[k, 0] = len(ids)
+        rows[k, 1:1 + len(ids)] = ids
+    rs_old = rng.uniform(0.5, 1.5, idx.size)
+    rs_new = rs_old * np.exp(rng.normal(0.0, 0.4, idx.size))
+    dev = torch.device("cuda", 0)
+    got = motion_count_device(torch.tensor(x, device=dev), torch.tensor(v, device=dev), idx, rows,
+                              dtr, rs_new, rs_old, chunk=1000)
+    want = motion_count(x, v, idx, rows, dtr, rs_new, rs_old)
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
