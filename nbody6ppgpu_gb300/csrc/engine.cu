@@ -651,6 +651,10 @@ static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out
   const int ni = is.ni;
   int best_v = -1, best_s = 1;
   float best = 1e30f;
+  // the fastest plan whose pair kernel merges itself (its partial rows stay
+  // in L2): taken when within 1% of the fastest overall
+  int fused_v = -1, fused_s = 1;
+  float fused_best = 1e30f;
   if (!g.outblk.ensure((size_t)7 * ni * sizeof(double) + (size_t)(ni + 2) * sizeof(int)) ||
       !g.rowlen.ensure((size_t)ni * sizeof(int)))
     return -1;
@@ -691,7 +695,17 @@ static int autotune_with(const ISet &is, int nnbmax, bool mflag, int *splits_out
         best_v = v;
         best_s = s;
       }
+      if (s <= FUSE_MAX_SPLITS && ms < fused_best) {
+        fused_best = ms;
+        fused_v = v;
+        fused_s = s;
+      }
     }
+  }
+  if (fused_v >= 0 && fused_best <= 1.01f * best) {
+    best = fused_best;
+    best_v = fused_v;
+    best_s = fused_s;
   }
   if (best_v >= 0) g.tune[tune_key(g.nj, ni, mflag, 0)] = TuneEntry{best_v, best_s, best};
   if (splits_out) *splits_out = best_s;
