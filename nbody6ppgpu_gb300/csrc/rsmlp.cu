@@ -191,7 +191,7 @@ __device__ __forceinline__ float2 mlp_tile_infer(const MlpTcSmem &s, float2 x0, 
 }
 
 #ifndef GPUNB_MLP_MINB
-#define GPUNB_MLP_MINB 1   // uncapped (126 registers, 4 blocks per SM): 3% faster than 96 / 5
+#define GPUNB_MLP_MINB 1   // uncapped: 184 registers, 2 blocks per SM, 3% faster than 96 / 5
 #endif
 __global__ void __launch_bounds__(32 * TC_WARPS, GPUNB_MLP_MINB)
     rsmlp_forward_tc_kernel(int B, const float *__restrict__ X,
