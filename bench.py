@@ -141,6 +141,24 @@ def fp32_peak_tflops(n_sm: int, mhz: float) -> float:
     return n_sm * 128 * 2 * mhz * 1e6 / 1e12
 
 
+def fp64_peak_tflops(n_sm: int, mhz: float) -> float:
+    # 2 FP64 FMAs per SM per cycle on GB300 (ncu: dfma peak 2 per cycle per SM)
+    return n_sm * 2 * 2 * mhz * 1e6 / 1e12
+
+
+def hbm_gbs() -> float:
+    """Measured copy bandwidth of the GB300s (MEASURED_PEAKS.json), else 6800."""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0
+
+
+# j-tile bytes per body (TILE_BYTES / JT of the library: 12 fields + metadata, 128
+# bodies), read once per i-tile pass; i-tile sizes of the launch shapes
+TILE_BYTES_PER_BODY = 6704 / 128
+
+
 def read_traffic():
     """DRAM bytes per launch of the pair kernel from the committed ncu summary."""
     p = ROOT / "profiles" / "regf_ds_kernel_plummer65536.txt"
@@ -776,13 +794,21 @@ def main():
     # every block's pair kernel: duration, pairs/s and the bound that applies
     # (small blocks read each j tile once: 52 B per body from L2/HBM, and are
     # latency-bound; large ones are FP32-bound)
+    # roofline of each block: min(FP32 peak / 60 flops, HBM bandwidth / j bytes per
+    # pair), the j tiles read once per i-tile (at most 128 i per tile pass)
     per_block = {}
+    fp32_gp = fp32_peak_tflops(gpu_info()[1], clk.get("sm_max_mhz") or 2070.0) * 1e12 / \
+        FLOPS_PER_PAIR / 1e9
     for q, ni in enumerate(BLOCKS):
         bm = float(np.mean(kt[:, q]))
         gp = ni * N / (bm * 1e-3) / 1e9
+        hbm_gp = hbm_gbs() / (TILE_BYTES_PER_BODY / min(ni, 128))
+        bound_gp = min(fp32_gp, hbm_gp)
         per_block[str(ni)] = {"kernel_ms": bm, "gpairs_s": gp,
-                              "frac_fp32_nominal": gp * 1e9 * FLOPS_PER_PAIR / 1e12 /
-                              fp32_peak_tflops(gpu_info()[1], clk.get("sm_max_mhz") or 2070.0),
+                              "frac_fp32_nominal": gp / fp32_gp,
+                              "roofline_gpairs_s": bound_gp,
+                              "roofline": "fp32" if fp32_gp <= hbm_gp else "hbm",
+                              "frac_of_roofline": gp / bound_gp,
                               "bound": "fp32" if ni >= 1024 else "latency (j set read once)"}
     pairs_big = 65536 * N
     achieved_tflops = pairs_big * FLOPS_PER_PAIR / (k_ms * 1e-3) / 1e12
@@ -905,7 +931,12 @@ def main():
                                   "shape"},
         "fp64": {"value": fp64_value, "unit": "Gpairs/s",
                  "kernel_ms_ni65536": float(np.mean(fp64_big)),
-                 "speedup_split_over_fp64_kernel": float(np.mean(fp64_big)) / k_ms},
+                 "speedup_split_over_fp64_kernel": float(np.mean(fp64_big)) / k_ms,
+                 "achieved_tflops_60_flops_per_pair":
+                     pairs_big * FLOPS_PER_PAIR / (float(np.mean(fp64_big)) * 1e-3) / 1e12,
+                 "fp64_peak_tflops": fp64_peak_tflops(n_sm, peak_mhz),
+                 "frac_fp64_peak": pairs_big * FLOPS_PER_PAIR /
+                     (float(np.mean(fp64_big)) * 1e-3) / 1e12 / fp64_peak_tflops(n_sm, peak_mhz)},
         "rel_err_vs_fp64_kernel": errs,
         "pair_kernel_per_block": per_block,
         "launch_plan_per_block": {str(ni): {"variant": v, "splits": sp_}
