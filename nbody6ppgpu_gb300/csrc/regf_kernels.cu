@@ -38,6 +38,17 @@
 #define GPUNB_FOLD_TILES 1
 #endif
 
+// The warp vote on the neighbour candidates of a pair group right after r^2,
+// before the rsqrt and Newton step (the accepted neighbours then drop out
+// through a zero mass, with r^2 set to 1 so that 1/r stays finite), so that
+// the inverse distances and the sums of the group's lane pairs follow the
+// branch in one block; else after the whole geometry (they drop out through a
+// zero 1/r).  Measured on GB300 (Plummer 65536): 4.522 -> 4.499 ms at
+// ni = 65536, 1.258 -> 1.253 ms at ni = 16384, identical errors and lists.
+#ifndef GPUNB_VOTE_EARLY
+#define GPUNB_VOTE_EARLY 1
+#endif
+
 namespace gpunb {
 
 // ---------------------------------------------------------------------------
@@ -359,6 +370,8 @@ struct TileCtx {
   float H, R;
 };
 
+__device__ __forceinline__ void pair_inv(PairGeo &g);
+
 template <bool REL>
 __device__ __forceinline__ void pair_geo(const IState &I, const TileCtx &C, const JPair &p,
                                          PairGeo &g) {
@@ -379,6 +392,10 @@ __device__ __forceinline__ void pair_geo(const IState &I, const TileCtx &C, cons
   g.mn = p.v[F_MN];
   g.r2 = fma2(g.dz, g.dz, fma2(g.dy, g.dy, mul2(g.dx, g.dx)));
   g.rv = fma2(g.dz, g.dvz, fma2(g.dy, g.dvy, mul2(g.dx, g.dvx)));
+  if (!GPUNB_VOTE_EARLY) pair_inv(g);
+}
+
+__device__ __forceinline__ void pair_inv(PairGeo &g) {
   // rsqrt estimate + one Newton step, scaled: z = y0 (x y0^2 - 3) = -2/r,
   // evaluated in residual form: e = x y0^2 - 1 is small, so its rounding is
   // negligible, and z = y0 e - 2 y0 takes a single rounding in the last FMA.
@@ -406,12 +423,22 @@ __device__ __forceinline__ void pair_candidates(const IState &I, const TileCtx &
   if (g.r2.x < H && decide_pair<MFLAG>(I, is, js, jg0, g.dx.x, g.dy.x, g.dz.x, g.dvx.x, g.dvy.x,
                                        g.dvz.x, g.r2.x, g.mn.x, C.R)) {
     rec.buf[rec.n++ * rec.stride] = jg0;
-    g.z.x = 0.f;
+    if (GPUNB_VOTE_EARLY) {
+      g.mn.x = 0.f;
+      g.r2.x = 1.f;
+    } else {
+      g.z.x = 0.f;
+    }
   }
   if (g.r2.y < H && decide_pair<MFLAG>(I, is, js, jg0 + 1, g.dx.y, g.dy.y, g.dz.y, g.dvx.y,
                                        g.dvy.y, g.dvz.y, g.r2.y, g.mn.y, C.R)) {
     rec.buf[rec.n++ * rec.stride] = jg0 + 1;
-    g.z.y = 0.f;
+    if (GPUNB_VOTE_EARLY) {
+      g.mn.y = 0.f;
+      g.r2.y = 1.f;
+    } else {
+      g.z.y = 0.f;
+    }
   }
 }
 
@@ -443,6 +470,10 @@ __device__ __forceinline__ void pair4(const IState &I, const TileCtx &C, const J
     pair_candidates<MFLAG>(I, C, g0, jg0, js, is, rec);
     pair_candidates<MFLAG>(I, C, g1, jg0 + 2, js, is, rec);
   }
+  if (GPUNB_VOTE_EARLY) {
+    pair_inv(g0);
+    pair_inv(g1);
+  }
   pair_acc(g0, q);
   pair_acc(g1, q);
 }
@@ -464,7 +495,10 @@ __device__ __forceinline__ void pair8(const IState &I, const TileCtx &C, const J
     for (int u = 0; u < 4; ++u) pair_candidates<MFLAG>(I, C, g[u], jg0 + 2 * u, js, is, rec);
   }
 #pragma unroll
-  for (int u = 0; u < 4; ++u) pair_acc(g[u], q);
+  for (int u = 0; u < 4; ++u) {
+    if (GPUNB_VOTE_EARLY) pair_inv(g[u]);
+    pair_acc(g[u], q);
+  }
 }
 
 // One warp's share [jbeg, jbeg + JW) of a tile against one i: the fields the
