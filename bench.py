@@ -370,7 +370,7 @@ KING_NNBMAX = 1024
 
 
 def king1m_leg(lib, dev, stream, n_sm: int, peak_mhz: float, steps: int = 2, warmup: int = 2):
-    """The spec configuration as a full regular step: King W0 = 6,
+    """The King 2^20 configuration as a full regular step: King W0 = 6,
     N = 2^20, Kroupa masses with 10% binaries as c.m. bodies, RS for a mean of
     100 neighbours, nbmax 1024; one step = send + regf for each block
     ni in {1024, 16384, 262144, N} (1.39e12 pairs).
