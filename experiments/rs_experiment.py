@@ -200,6 +200,8 @@ def main():
     ap.add_argument("--ticks-harvest", type=int, default=48)
     ap.add_argument("--harvest-every", type=int, default=1,
                     help="config 5: label only the King bodies i %% k == 0")
+    ap.add_argument("--eval-seed", type=int, default=41,
+                    help="config 5: seed of the King model the policies are evaluated on")
     ap.add_argument("--model", default="king", choices=["king", "plummer"])
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--ticks", type=int, default=64)
@@ -227,7 +229,8 @@ def main():
         print(json.dumps(config5(a.ticks_harvest, a.ticks, n_king=a.n, nnbopt=a.nnbopt,
                                  nnbmax=a.nnbmax, levels=a.levels, epochs=a.epochs, q=a.q,
                                  band=tuple(a.band), guard=a.guard,
-                                 harvest_every=a.harvest_every)), flush=True)
+                                 harvest_every=a.harvest_every, eval_seed=a.eval_seed)),
+              flush=True)
         return
     print(json.dumps(run(a.model, a.n, a.ticks, a.nnbopt, a.nnbmax, a.levels, epochs=a.epochs,
                          q=a.q, rounds=a.rounds, band=tuple(a.band), guard=a.guard,
