@@ -496,13 +496,16 @@ def king1m_leg(lib, dev, stream, n_sm: int, peak_mhz: float, steps: int = 2, war
                 nb.send(k.m, k.x, k.v)
                 outs[ni] = nb.regf(*hin[ni], KING_NNBMAX + 1, KING_NNBMAX, out=outs.get(ni))
 
+        # the first steps capture the graphs and touch the caller's host arrays
+        # for the first time (4.3 GB of LISTGP rows at ni = N): warm up fully
         lib.gpunb_set_graphs(1)
-        for _ in range(max(1, warmup - 1)):
+        for _ in range(max(2, warmup)):
             host_step()
+        e2e_steps = max(3, steps)
         t = time.perf_counter()
-        for _ in range(steps):
+        for _ in range(e2e_steps):
             host_step()
-        e2e_s = (time.perf_counter() - t) / steps
+        e2e_s = (time.perf_counter() - t) / e2e_steps
         lib.gpunb_set_graphs(0)
     lib.gpunb_set_autotune(autotune_prev)
     h2d = sum(56 * n + 64 * ni for ni in KING_BLOCKS)
@@ -518,6 +521,7 @@ def king1m_leg(lib, dev, stream, n_sm: int, peak_mhz: float, steps: int = 2, war
         "value": pairs / (step_ms * 1e-3) / 1e9, "unit": "Gpairs/s", "step_ms": step_ms,
         "steps": steps, "warmup": warmup, "clocks": clk,
         "e2e": {"value": pairs / e2e_s / 1e9, "unit": "Gpairs/s", "step_s": e2e_s,
+                "steps": e2e_steps, "warmup": max(2, warmup),
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "blocks": blocks,
         "roofline": {"bound": "fp32", "kernel": "regf_ds_kernel (ni = N block)",
