@@ -677,6 +677,17 @@ __device__ __forceinline__ void merge_itile(const RegfOut &out, int S, int slot0
   }
 }
 
+// Slot within the i-tile of (warp along i, i index of the thread, lane):
+// contiguous runs of 32 per warp, or with GPUNB_WARP_INTERLEAVE the tile's
+// slots dealt round-robin over its warps (each warp then spans the tile).
+#ifndef GPUNB_WARP_INTERLEAVE
+#define GPUNB_WARP_INTERLEAVE 0
+#endif
+template <int IPT, int WI>
+__device__ __forceinline__ int itile_slot(int wi, int k, int lane) {
+  return GPUNB_WARP_INTERLEAVE ? (k * 32 + lane) * WI + wi : wi * 32 * IPT + k * 32 + lane;
+}
+
 template <int IPT, int WI, int WJ, int JV, bool MFLAG, int MINB>
 __global__ void __launch_bounds__(32 * WI * WJ, MINB)
     regf_ds_kernel(const JSet js, const ISet is, const RegfOut out, const RegfWork w) {
@@ -756,7 +767,7 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
       rec[k].buf = nbuf + k * NT + tid;
       rec[k].stride = IPT * NT;
       rec[k].n = 0;
-      const int slot = slot0 + wi * 32 * IPT + k * 32 + lane;
+      const int slot = slot0 + itile_slot<IPT, WI>(wi, k, lane);
       load_istate(I[k], is.rec, slot, slot < slot_end);
 #pragma unroll
       for (int c = 0; c < NQ; ++c) {
@@ -873,7 +884,7 @@ __global__ void __launch_bounds__(32 * WI * WJ, MINB)
 #pragma unroll
       for (int k = 0; k < IPT; ++k) {
         if (I[k].i < 0) continue;
-        const int col = pcol0 + wi * 32 * IPT + k * 32 + lane;
+        const int col = pcol0 + itile_slot<IPT, WI>(wi, k, lane);
 #pragma unroll
         for (int c = 0; c < NQ; ++c) {
           const float2 v = make_float2(ffs[((0 * NQ + c) * IPT + k) * NT + tid],
