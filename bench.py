@@ -200,19 +200,28 @@ def cpu_side_checks(c, irr_check=None, pot_result=None):
     from oracle import oracle as O
     out = {}
     if irr_check is not None:
-        x, v, f, fdot, m, t0, lists, ti, act = irr_check["state"]
-        a, j, nid = irr_check["gpu"]
-        O.irr_fp64(x, v, f, fdot, m, t0, lists, ti, act)
+        st = irr_check["state"]
+        act = st[-1]
+        lists = st[6]
+        O.irr_fp64(*st)
         t = time.perf_counter()
-        oa, oj, on = O.irr_fp64(x, v, f, fdot, m, t0, lists, ti, act)
+        oa, oj, on = O.irr_fp64(*st)
         dt = time.perf_counter() - t
         ok = np.linalg.norm(oa, axis=1) > 0
+        a, j, nid = irr_check["gpu"]["fp64"]
         ea = np.linalg.norm(a[ok] - oa[ok], axis=1) / np.linalg.norm(oa[ok], axis=1)
+        sa, sj = O.irr_abs_sums(*st)
+        a, j, nid_s = irr_check["gpu"]["split"]
+        ones = np.ones(len(act))
+        pe = O.parity_errors(a[ok], j[ok], ones[ok], oa[ok], oj[ok], ones[ok], sa[ok], sj[ok])
+        pe.pop("pot")
         out["irregular"] = {"kind": "FP64 oracle (oracle/irr_fp64.c)", "cores": O.num_threads(),
                             "ni": int(len(act)),
                             "gpairs_s": int(lists[act, 0].sum()) / dt / 1e9,
-                            "gpu_max_rel_err_vs_fp64_oracle": float(ea.max()),
-                            "gpu_nnbid_identical": bool(np.array_equal(nid, on))}
+                            "gpu_fp64_max_rel_err_vs_fp64_oracle": float(ea.max()),
+                            "gpu_fp64_nnbid_identical": bool(np.array_equal(nid, on)),
+                            "gpu_split_parity_vs_fp64_oracle": pe,
+                            "gpu_split_nnbid_differing": int(np.sum(nid_s != on))}
     if pot_result is not None:
         n = c.n
         t = time.perf_counter()
@@ -554,12 +563,20 @@ def king_cpu_block(k, h2, act):
                                       f"{k.n} (FP32 restatement of src/Main/reg.avx.cpp)"}
 
 
-def irregular_leg(c, h2, lists_src):
+def irregular_leg(c, h2, lists_src, dev=None):
     """Irregular (neighbour) force through the irr_simd_* ABI (the drop-in
     for src/Main/irr.avx.cpp): the bench's Plummer N = 65536 with the
     neighbour lists of its ni = 65536 regular block (the particle itself
     removed), predictor state from that block's regular force, blocks of
-    1024, 16384 and 65536 particles at a common time.  Unit: listed pairs."""
+    1024, 16384 and 65536 particles at a common time, in split precision
+    (the default) and in FP64.  Host-ABI calls are timed on the wall clock;
+    the device-resident form (irr_firr_device) with CUDA events on its
+    stream.  Unit: listed pairs."""
+    import ctypes as C
+
+    import torch
+
+    from nbody6ppgpu_gb300.gpunb import load
     from nbody6ppgpu_gb300.irr import IrrSimd
     n = c.n
     lmax = lists_src.shape[1]
@@ -575,22 +592,29 @@ def irregular_leg(c, h2, lists_src):
     fdot = rng.normal(0.0, 0.5, (n, 3))
     ti = 1.0
     t0 = ti - rng.uniform(0.0, 2e-3, n)
-    out = {"workload": "Plummer N=65536 (the bench cluster), lists of its regular block, "
-                       "host ABI (irr_simd_firr_vec_)", "blocks": {}}
+    blocks = {ni: rng.permutation(n)[:ni] for ni in (1024, 16384, n)}
+    out = {"workload": "Plummer N=65536 (the bench cluster), lists of its regular block",
+           "precision": "fp64 (the default) and split FP32 (irr_set_precision(0): "
+                        "double-single positions after an FP64 prediction)",
+           "host_abi": {"split": {}, "fp64": {}}, "device": {"split": {}, "fp64": {}}}
     with IrrSimd(n, lmax) as irr:
         irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
         irr.set_lists(lists)
-        for ni in (1024, 16384, n):
-            act = rng.permutation(n)[:ni]
-            pairs = int(lists[act, 0].sum())
-            irr.firr(ti, act)
-            best = 1e9
-            for _ in range(5):
-                t = time.perf_counter()
-                a, j, nid = irr.firr(ti, act)
-                best = min(best, time.perf_counter() - t)
-            out["blocks"][str(ni)] = {"pairs": pairs, "ms": best * 1e3,
-                                      "gpairs_s": pairs / best / 1e9}
+        for prec, key in ((0, "split"), (1, "fp64")):
+            irr.set_precision(prec)
+            for ni, act in blocks.items():
+                pairs = int(lists[act, 0].sum())
+                # the caller's result arrays persist between calls (as Fortran's)
+                res = (np.zeros((ni, 3)), np.zeros((ni, 3)), np.zeros(ni, dtype=np.int32))
+                irr.firr(ti, act, out=res)
+                best = 1e9
+                for _ in range(5):
+                    t = time.perf_counter()
+                    irr.firr(ti, act, out=res)
+                    best = min(best, time.perf_counter() - t)
+                out["host_abi"][key][str(ni)] = {"pairs": pairs, "ms": best * 1e3,
+                                                 "gpairs_s": pairs / best / 1e9}
+        irr.set_precision(1)
         # predict-and-send from the stored state vs gpunb_send_ of host arrays
         from nbody6ppgpu_gb300.gpunb import GpuNb
         from nbody6ppgpu_gb300.irr import send_predicted
@@ -605,13 +629,56 @@ def irregular_leg(c, h2, lists_src):
                 ts.append(time.perf_counter() - t)
         out["predict_send_ms"] = 1e3 * min(tp[1:])
         out["send_host_arrays_ms"] = 1e3 * min(ts[1:])
-    # a block of 16384 for the CPU-baseline leg (timing and FP64 check)
-    act = rng.permutation(n)[:16384]
+    # the device-resident form, kernels timed with CUDA events on their stream
+    dev = dev or torch.device("cuda", 0)
+    rec = np.zeros((n, 16))
+    rec[:, 0:3] = c.x; rec[:, 3] = c.m; rec[:, 4:7] = c.v; rec[:, 7] = t0
+    rec[:, 8:11] = f; rec[:, 12:15] = fdot
+    R = torch.tensor(rec, device=dev)
+    L = torch.tensor(lists, device=dev)
+    lib = load()
+    fn = lib.irr_firr_device
+    fn.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_int, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    st = torch.cuda.Stream(dev)
+    for prec, key in ((0, "split"), (1, "fp64")):
+        lib.irr_set_precision(prec)
+        for ni, act in blocks.items():
+            A = torch.tensor(act.astype(np.int32), device=dev)
+            acc = torch.empty(ni, 3, dtype=torch.float64, device=dev)
+            jrk = torch.empty_like(acc)
+            nid = torch.empty(ni, dtype=torch.int32, device=dev)
+            args = (n, R.data_ptr(), lmax, L.data_ptr(), ti, ni, A.data_ptr(), acc.data_ptr(),
+                    jrk.data_ptr(), nid.data_ptr(), st.cuda_stream)
+            torch.cuda.synchronize()
+            for _ in range(3):
+                assert fn(*args) == 0
+            reps = 20
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(st):
+                e0.record(st)
+                for _ in range(reps):
+                    fn(*args)
+                e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            pairs = int(lists[act, 0].sum())
+            out["device"][key][str(ni)] = {"ms": ms, "gpairs_s": pairs / ms / 1e6}
+    lib.irr_set_precision(1)
+    s16, f16 = out["device"]["split"][str(n)], out["device"]["fp64"][str(n)]
+    out["device"]["split_over_fp64_ni65536"] = f16["ms"] / s16["ms"]
+    # a block of 16384 for the CPU-baseline leg (timing and the FP64 checks)
+    act = blocks[16384]
+    res = {}
     with IrrSimd(n, lmax) as irr:
         irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
         irr.set_lists(lists)
-        a, j, nid = irr.firr(ti, act)
-    check = {"state": (c.x, c.v, f, fdot, c.m, t0, lists, ti, act), "gpu": (a, j, nid)}
+        for prec, key in ((0, "split"), (1, "fp64")):
+            irr.set_precision(prec)
+            res[key] = irr.firr(ti, act)
+        irr.set_precision(1)
+    check = {"state": (c.x, c.v, f, fdot, c.m, t0, lists, ti, act), "gpu": res}
     return out, check
 
 

@@ -18,10 +18,17 @@
  * and returns the force and its derivative from the neighbours,
  *     acc += m dx / r^3,  jrk += m / r^3 (dv - 3 (dx.dv) / r^2 dx),
  * and nnbid = the Fortran index of the nearest listed neighbour (0 for an
- * empty list).  Computed in FP64 on the GPU (the reference: FP32 on the CPU).
+ * empty list).  Precision (irr_set_precision): FP64 throughout by default,
+ * or the reference's own scheme -- double-single positions, FP32 velocities,
+ * masses and force arithmetic (irr.avx.cpp:58-176) -- after an FP64
+ * prediction, with the nearest neighbour taken on the FP32 r^2: the
+ * accuracy class of the reference's library (force and derivative within
+ * 2e-6 of FP64 at the 99th percentile, within 5e-6 of max(|Q|, S/8) per
+ * particle, S the sum of the terms' magnitudes).
  * Deliberate differences: no 600-entry list cap (lmax up to 2^16 per row);
  * a listed body at zero distance (the particle itself) adds nothing instead
- * of a NaN; invalid addresses or ids are reported as GPUNB_E_ARG.
+ * of a NaN (in split precision: any body closer than 1e-19); invalid
+ * addresses or ids are reported as GPUNB_E_ARG.
  *
  * set_jp / set_list are safe to call concurrently for different particles
  * (the Fortran callers run them inside OpenMP loops); they only update host
@@ -51,12 +58,21 @@ void irr_simd_firr_vec_(double *ti, int *ni, int addr[], double acc[][3], double
  * the mode in effect, -1 without a device. */
 int irr_set_host_path(int mode);
 
+/* Arithmetic of the force: 1 (default) = FP64, 0 = split FP32 as above
+ * (the prediction is FP64 in both).  Also set at irr_simd_open_ from the
+ * environment variable GPUNB_IRR_PRECISION.  Applies to the next force call,
+ * host or device-resident form.  Returns the mode in effect. */
+int irr_set_precision(int mode);
+
 /* Device-resident form: state and lists already in device memory, 0-based
  * indices, work queued on `stream` (NULL: the library's stream).
  *   rec: n records of 16 doubles {x0[3], m, v0[3], t0, a2[3], 0, j6[3], 0}
  *   lists: n rows of lmax ints, [0] = count, then 0-based ids
  *   addr[ni]: 0-based particles; outputs acc[ni][3], jrk[ni][3], nnbid[ni]
- *   (nnbid is 1-based like the host form, 0 for an empty list). */
+ *   (nnbid is 1-based like the host form, 0 for an empty list).
+ * Blocks of at least n/32 particles predict the whole set first into a
+ * buffer the library keeps for this form (allocated on first use): calls of
+ * this form that overlap on the GPU must be serialised on one stream. */
 int irr_firr_device(int n, const double *rec, int lmax, const int *lists, double ti, int ni,
                     const int *addr, double *acc, double *jrk, int *nnbid, void *stream);
 

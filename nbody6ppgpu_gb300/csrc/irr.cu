@@ -9,7 +9,9 @@
 // the particle to a dirty list (lock-free, so the OpenMP callers stay
 // parallel); the next force call uploads only the changed records and rows,
 // then one warp per active particle predicts the particle and its listed
-// neighbours to the block time and sums the force, all in FP64.  On systems
+// neighbours to the block time (FP64) and sums the force in FP64 (the
+// default) or in split FP32 (the reference's own precision scheme, about 30
+// times faster on GB300).  On systems
 // where the device reads pageable memory coherently (Grace + GB300 over
 // NVLink-C2C) the kernels read the mirrors, the address list and write the
 // results in host memory directly; elsewhere they go through pinned staging.
@@ -27,9 +29,11 @@
 
 #include <cuda_runtime.h>
 
+#include "common.cuh"
 #include "gpunb.h"
 #include "internal.h"
 #include "irr.h"
+#include "launch.h"
 
 namespace gpunb {
 namespace irr {
@@ -37,6 +41,9 @@ namespace irr {
 // particle record: 16 doubles {x0[3], m, v0[3], t0, a2[3], 0, j6[3], 0}
 constexpr int REC = 16;
 constexpr int IRR_WARPS = 8;   // warps per block; one active particle per warp
+// per-call status on the device: the error word (int, offset 0) and the
+// listed pairs of the call (unsigned long long, offset 8)
+constexpr size_t kStatusBytes = 16;
 
 // ---------------------------------------------------------------------------
 // device
@@ -94,31 +101,50 @@ __device__ __forceinline__ void state(const double *__restrict__ rec,
   }
 }
 
-template <bool PRE>
+// Lanes per active particle G: 8 (four particles per warp) for blocks that
+// fill the GPU, 32 for smaller ones.  An irregular list holds ~50-150
+// bodies, so with G = 8 each lane takes 6-20 of them and the cross-lane sum
+// is 3 shuffle levels shared by the warp's four particles instead of 5 per
+// particle (on GB300 the FP64 adds of a per-particle 5-level butterfly cost
+// as much as the pair arithmetic); a small block has too few warps to hide
+// the latency of 6-20 dependent gathers per lane, and takes G = 32.  The lane
+// count sets the summation order, so a particle's last bits can differ
+// between a block below and a block above IRR_G_MIN_NI particles; for the
+// same call the results are always the same.
+constexpr int IRR_G = 8;
+constexpr int IRR_G_MIN_NI = 4 * 152 * IRR_WARPS;   // about 4 blocks per SM of GB300
+constexpr int IRR_U = 4;   // listings per lane in flight (split kernel)
+
+template <bool PRE, int G>
 __global__ void __launch_bounds__(32 * IRR_WARPS)
     irr_firr_kernel(int n, const double *__restrict__ rec, const double *__restrict__ pred,
                     int lmax, const int *__restrict__ lists, double ti, int ni,
                     const int *__restrict__ addr, int base, double *__restrict__ acc,
-                    double *__restrict__ jrk, int *__restrict__ nnbid, int *__restrict__ err) {
-  const int lane = threadIdx.x & 31;
+                    double *__restrict__ jrk, int *__restrict__ nnbid, int *__restrict__ err,
+                    unsigned long long *__restrict__ inter) {
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-  for (int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); k < ni; k += nwarps) {
-    const int i = addr[k] - base;
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  // every lane runs every iteration (the shuffles below need all 32)
+  for (int k0 = warp * (32 / G); k0 < ni; k0 += nwarps * (32 / G)) {
+    const int k = k0 + lane / G;
     double ax = 0, ay = 0, az = 0, jx = 0, jy = 0, jz = 0;
     double best = INFINITY;
     int bj = INT_MAX;
-    if (i < 0 || i >= n) {
-      if (lane == 0) flag(err, GPUNB_E_ARG);
-    } else {
+    const int i = k < ni ? addr[k] - base : 0;
+    if (k < ni && (i < 0 || i >= n)) {
+      if (sub == 0) flag(err, GPUNB_E_ARG);
+    } else if (k < ni) {
       double xi[3], vi[3], mi;
       state<PRE>(rec, pred, i, ti, xi, vi, mi);
       const int *row = lists + (size_t)i * lmax;
       int nnb = row[0];
       if (nnb < 0 || nnb > lmax - 1) {
-        if (lane == 0) flag(err, GPUNB_E_ARG);
+        if (sub == 0) flag(err, GPUNB_E_ARG);
         nnb = 0;
       }
-      for (int q = lane; q < nnb; q += 32) {
+      if (inter && sub == 0 && nnb > 0) atomicAdd(inter, (unsigned long long)nnb);
+      for (int q = sub; q < nnb; q += G) {
         const int j = row[1 + q];
         if (j < 0 || j >= n) {
           flag(err, GPUNB_E_ARG);
@@ -147,8 +173,8 @@ __global__ void __launch_bounds__(32 * IRR_WARPS)
         }
       }
     }
-    // fixed butterfly: the same order on every call (deterministic)
-    for (int o = 16; o > 0; o >>= 1) {
+    // fixed butterfly within the particle's lanes (deterministic)
+    for (int o = G / 2; o > 0; o >>= 1) {
       ax += __shfl_xor_sync(0xffffffffu, ax, o);
       ay += __shfl_xor_sync(0xffffffffu, ay, o);
       az += __shfl_xor_sync(0xffffffffu, az, o);
@@ -162,13 +188,197 @@ __global__ void __launch_bounds__(32 * IRR_WARPS)
         bj = oj;
       }
     }
-    if (lane == 0) {
+    if (sub == 0 && k < ni) {
       acc[3 * (size_t)k] = ax;
       acc[3 * (size_t)k + 1] = ay;
       acc[3 * (size_t)k + 2] = az;
       jrk[3 * (size_t)k] = jx;
       jrk[3 * (size_t)k + 1] = jy;
       jrk[3 * (size_t)k + 2] = jz;
+      nnbid[k] = (bj == INT_MAX) ? 0 : bj + 1;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Split precision (irr_set_precision(0)): the reference's own scheme for this force
+// (irr.avx.cpp:58-176: positions as FP32 hi + lo pairs, FP32 velocities and
+// force arithmetic), laid out for the GPU.  The prediction stays FP64 -- one
+// Taylor step per particle (whole-set blocks) or per listing (small blocks),
+// ~24 FP64 operations -- and its result is split into a double-single
+// position, an FP32 mass and velocity: 3 float4 = 48 bytes per particle,
+// which always span exactly two 32-byte sectors when gathered.  The pair
+// arithmetic runs on the FP32 pipe, which GB300 has 64 times more of than
+// FP64: double-single coordinate difference, rsqrt estimate with one Newton
+// step in residual form, 1/r^3 and the jerk term in FP32.  Each lane sums at
+// most IRR_U pairs in FP32 before it folds them into float-float lane sums, and
+// a particle's 8 lanes are combined in float-float in a fixed butterfly, so
+// the result is deterministic and the summation adds no error worth stating
+// (FP64 adds would cost as much as the pair arithmetic).  What remains is
+// the FP32 rounding of each pair term (a few units of 2^-24): an irregular
+// force is a sum of a few dominant terms, so unlike the regular force's
+// thousands these errors do not average out, and where the terms cancel the
+// relative error of the sum grows with the cancellation.  A C emulation of
+// the arithmetic against FP64 (Plummer N = 16384, lists of ~100) shows that
+// exact arithmetic after the FP32 inputs would still leave 1.1e-6 of
+// max(|Q_i|, S_i / 8) in the derivative: only double-single differences and
+// velocities with float-float arithmetic throughout would reach the regular
+// force's 1e-6 bound, so that accuracy is the FP64 mode's.
+constexpr int PRED32 = 3;   // float4 per particle
+
+__device__ __forceinline__ void split_state(const double x[3], const double v[3], double m,
+                                            float4 s[PRED32]) {
+  float h[3], l[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) ds_split(x[c], h[c], l[c]);
+  s[0] = make_float4(h[0], h[1], h[2], (float)m);
+  s[1] = make_float4(l[0], l[1], l[2], 0.f);
+  s[2] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+}
+
+__global__ void irr_pred32_kernel(int n, const double *__restrict__ rec, double ti,
+                                  float4 *__restrict__ pred) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[3], v[3], m;
+  predict(rec + (size_t)i * REC, ti, x, v, m);
+  float4 s[PRED32];
+  split_state(x, v, m, s);
+#pragma unroll
+  for (int u = 0; u < PRED32; ++u) pred[(size_t)i * PRED32 + u] = s[u];
+}
+
+template <bool PRE>
+__device__ __forceinline__ void state32(const double *__restrict__ rec,
+                                        const float4 *__restrict__ pred, int i, double ti,
+                                        float4 s[PRED32]) {
+  if (PRE) {
+#pragma unroll
+    for (int u = 0; u < PRED32; ++u) s[u] = __ldg(pred + (size_t)i * PRED32 + u);
+  } else {
+    double x[3], v[3], m;
+    predict(rec + (size_t)i * REC, ti, x, v, m);
+    split_state(x, v, m, s);
+  }
+}
+
+// Same contract as irr_firr_kernel.  Bodies closer than 1e-19 (r^2 below the
+// smallest normal float), the particle itself included, add nothing; the
+// nearest neighbour is chosen on the FP32 r^2 (ties to the smaller id).
+template <bool PRE, int G>
+__global__ void __launch_bounds__(32 * IRR_WARPS)
+    irr_firr32_kernel(int n, const double *__restrict__ rec, const float4 *__restrict__ pred,
+                      int lmax, const int *__restrict__ lists, double ti, int ni,
+                      const int *__restrict__ addr, int base, double *__restrict__ acc,
+                      double *__restrict__ jrk, int *__restrict__ nnbid, int *__restrict__ err,
+                      unsigned long long *__restrict__ inter) {
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  for (int k0 = warp * (32 / G); k0 < ni; k0 += nwarps * (32 / G)) {
+    const int k = k0 + lane / G;
+    float hi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, lo[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float best = INFINITY;
+    int bj = INT_MAX;
+    const int i = k < ni ? addr[k] - base : 0;
+    if (k < ni && (i < 0 || i >= n)) {
+      if (sub == 0) flag(err, GPUNB_E_ARG);
+    } else if (k < ni) {
+      float4 si[PRED32];
+      state32<PRE>(rec, pred, i, ti, si);
+      const int *row = lists + (size_t)i * lmax;
+      int nnb = row[0];
+      if (nnb < 0 || nnb > lmax - 1) {
+        if (sub == 0) flag(err, GPUNB_E_ARG);
+        nnb = 0;
+      }
+      if (inter && sub == 0 && nnb > 0) atomicAdd(inter, (unsigned long long)nnb);
+      // IRR_U listings per lane in flight: their ids, then their states, are
+      // loaded before any is used, so the gathers' latencies overlap
+      for (int q0 = sub; q0 < nnb; q0 += IRR_U * G) {
+        int jv[IRR_U];
+#pragma unroll
+        for (int u = 0; u < IRR_U; ++u) {
+          const int q = q0 + u * G;
+          jv[u] = q < nnb ? row[1 + q] : -1;
+          if (q < nnb && (jv[u] < 0 || jv[u] >= n)) {
+            flag(err, GPUNB_E_ARG);
+            jv[u] = -1;
+          }
+        }
+        float4 sj[IRR_U][PRED32];
+#pragma unroll
+        for (int u = 0; u < IRR_U; ++u) {
+          if (jv[u] >= 0) {
+            state32<PRE>(rec, pred, jv[u], ti, sj[u]);
+          } else {
+#pragma unroll
+            for (int w = 0; w < PRED32; ++w) sj[u][w] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+        float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // at most IRR_U pairs in FP32
+#pragma unroll
+        for (int u = 0; u < IRR_U; ++u) {
+          if (jv[u] < 0) continue;
+          const int j = jv[u];
+          // double-single difference: (hi_j - hi_i) + (lo_j - lo_i)
+          const float dx =
+              __fadd_rn(__fsub_rn(sj[u][0].x, si[0].x), __fsub_rn(sj[u][1].x, si[1].x));
+          const float dy =
+              __fadd_rn(__fsub_rn(sj[u][0].y, si[0].y), __fsub_rn(sj[u][1].y, si[1].y));
+          const float dz =
+              __fadd_rn(__fsub_rn(sj[u][0].z, si[0].z), __fsub_rn(sj[u][1].z, si[1].z));
+          const float dvx = __fsub_rn(sj[u][2].x, si[2].x);
+          const float dvy = __fsub_rn(sj[u][2].y, si[2].y);
+          const float dvz = __fsub_rn(sj[u][2].z, si[2].z);
+          const float r2 = fmaf(dz, dz, fmaf(dy, dy, __fmul_rn(dx, dx)));
+          if (r2 < best || (r2 == best && j < bj)) {
+            best = r2;
+            bj = j;
+          }
+          if (r2 >= 0x1p-126f) {
+            // rsqrt estimate, one Newton step in residual form:
+            // e = r2 y0^2 - 1, 1/r = y0 - y0 e / 2 (one rounding in the last FMA)
+            const float y0 = rsqrt_est(r2);
+            const float e = fmaf(__fmul_rn(r2, y0), y0, -1.0f);
+            const float rinv = fmaf(__fmul_rn(-0.5f, y0), e, y0);
+            const float rinv2 = __fmul_rn(rinv, rinv);
+            const float mr3 = __fmul_rn(__fmul_rn(sj[u][0].w, rinv), rinv2);
+            const float rv = fmaf(dz, dvz, fmaf(dy, dvy, __fmul_rn(dx, dvx)));
+            const float al = __fmul_rn(-3.0f * rv, rinv2);
+            f[0] = fmaf(mr3, dx, f[0]);
+            f[1] = fmaf(mr3, dy, f[1]);
+            f[2] = fmaf(mr3, dz, f[2]);
+            f[3] = fmaf(mr3, fmaf(al, dx, dvx), f[3]);
+            f[4] = fmaf(mr3, fmaf(al, dy, dvy), f[4]);
+            f[5] = fmaf(mr3, fmaf(al, dz, dvz), f[5]);
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) ff_accum(hi[c], lo[c], f[c]);
+      }
+    }
+    // fixed float-float butterfly within the particle's lanes (deterministic)
+    for (int o = G / 2; o > 0; o >>= 1) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const float oh = __shfl_xor_sync(0xffffffffu, hi[c], o);
+        const float ol = __shfl_xor_sync(0xffffffffu, lo[c], o);
+        ff_add(hi[c], lo[c], oh, ol);
+      }
+      const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+      if (ob < best || (ob == best && oj < bj)) {
+        best = ob;
+        bj = oj;
+      }
+    }
+    if (sub == 0 && k < ni) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        acc[3 * (size_t)k + c] = (double)hi[c] + (double)lo[c];
+        jrk[3 * (size_t)k + c] = (double)hi[3 + c] + (double)lo[3 + c];
+      }
       nnbid[k] = (bj == INT_MAX) ? 0 : bj + 1;
     }
   }
@@ -270,6 +480,7 @@ struct State {
   bool open = false;
   int nmax = 0, lmax = 0, rank = 0;
   int direct = 0;                // device reads/writes host memory coherently
+  int precision = 1;             // 1 = FP64 (default), 0 = split FP32
   cudaStream_t st = nullptr;
   std::vector<double> rec_h;     // host mirror of the records
   std::vector<int> list_h;       // host mirror of the rows (0-based ids)
@@ -279,7 +490,8 @@ struct State {
   unsigned epoch = 0;
   std::vector<int> uniq;
   DevBuf rec_d, list_d, addr_d, out_d, nid_d, idx_d, stage_d, off_d, err_d, pm_d, px_d, pv_d;
-  DevBuf pred_d;   // predicted states of all particles (large blocks)
+  DevBuf pred_d;   // predicted states of all particles (large blocks; 64 B each)
+  DevBuf pred_dev_d;   // the same for the device-resident form
   PinBuf stage_h, idx_h, off_h, err_h;
   double time_grav = 0.0;
   unsigned long long num_inter = 0, num_fcall = 0, num_steps = 0;
@@ -315,7 +527,7 @@ static double wtime() {
 
 static void release_all() {
   for (DevBuf *b : {&S.rec_d, &S.list_d, &S.addr_d, &S.out_d, &S.nid_d, &S.idx_d, &S.stage_d,
-                    &S.off_d, &S.err_d, &S.pm_d, &S.px_d, &S.pv_d, &S.pred_d})
+                    &S.off_d, &S.err_d, &S.pm_d, &S.px_d, &S.pv_d, &S.pred_d, &S.pred_dev_d})
     b->release();
   for (PinBuf *b : {&S.stage_h, &S.idx_h, &S.off_h, &S.err_h}) b->release();
   S.rec_h.clear();
@@ -440,21 +652,55 @@ static bool upload() {
   return true;
 }
 
-// pred: scratch of n * PRED doubles.  Blocks of at least n/32 particles
-// predict every particle once first (with ~100 neighbours each, the lists
-// then name every particle several times); smaller ones predict per listing.
-static int launch_firr(int n, const double *rec, double *pred, int lmax, const int *lists,
-                       double ti, int ni, const int *addr, int base, double *acc, double *jrk,
-                       int *nnbid, int *err, cudaStream_t st) {
+// pred: scratch of n * PRED doubles (64 bytes per particle, which also holds
+// the 48-byte split states).  Blocks of at least n/32 particles predict every
+// particle once first (with ~100 neighbours each, the lists then name every
+// particle several times); smaller ones predict per listing.  prec: 0 = split
+// FP32, 1 = FP64.
+static int launch_firr(int n, const double *rec, double *pred, int prec, int lmax,
+                       const int *lists, double ti, int ni, const int *addr, int base,
+                       double *acc, double *jrk, int *nnbid, int *err,
+                       unsigned long long *inter, cudaStream_t st) {
   if (ni <= 0) return GPUNB_OK;
-  const long long blocks = std::min<long long>((ni + IRR_WARPS - 1) / IRR_WARPS, 1ll << 20);
-  if (pred && 32ll * ni >= n) {
-    irr_pred_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, rec, ti, pred);
-    irr_firr_kernel<true><<<(unsigned)blocks, 32 * IRR_WARPS, 0, st>>>(
-        n, rec, pred, lmax, lists, ti, ni, addr, base, acc, jrk, nnbid, err);
+  const bool wide = ni < IRR_G_MIN_NI;   // 32 lanes per particle
+  const int per_block = IRR_WARPS * (wide ? 1 : 32 / IRR_G);   // particles per block and pass
+  const unsigned blocks =
+      (unsigned)std::min<long long>((ni + per_block - 1) / per_block, 1ll << 20);
+  const unsigned th = 32 * IRR_WARPS;
+  const bool whole = pred && 32ll * ni >= n;
+  if (prec == 1) {
+    if (whole) irr_pred_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, rec, ti, pred);
+    const double *p = whole ? pred : nullptr;
+    if (whole && wide)
+      irr_firr_kernel<true, 32><<<blocks, th, 0, st>>>(n, rec, p, lmax, lists, ti, ni, addr,
+                                                        base, acc, jrk, nnbid, err, inter);
+    else if (whole)
+      irr_firr_kernel<true, IRR_G><<<blocks, th, 0, st>>>(n, rec, p, lmax, lists, ti, ni, addr,
+                                                           base, acc, jrk, nnbid, err, inter);
+    else if (wide)
+      irr_firr_kernel<false, 32><<<blocks, th, 0, st>>>(n, rec, p, lmax, lists, ti, ni, addr,
+                                                         base, acc, jrk, nnbid, err, inter);
+    else
+      irr_firr_kernel<false, IRR_G><<<blocks, th, 0, st>>>(n, rec, p, lmax, lists, ti, ni, addr,
+                                                            base, acc, jrk, nnbid, err, inter);
   } else {
-    irr_firr_kernel<false><<<(unsigned)blocks, 32 * IRR_WARPS, 0, st>>>(
-        n, rec, nullptr, lmax, lists, ti, ni, addr, base, acc, jrk, nnbid, err);
+    float4 *p32 = whole ? reinterpret_cast<float4 *>(pred) : nullptr;
+    if (whole) irr_pred32_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, rec, ti, p32);
+    if (whole && wide)
+      irr_firr32_kernel<true, 32><<<blocks, th, 0, st>>>(n, rec, p32, lmax, lists, ti, ni, addr,
+                                                          base, acc, jrk, nnbid, err, inter);
+    else if (whole)
+      irr_firr32_kernel<true, IRR_G><<<blocks, th, 0, st>>>(n, rec, p32, lmax, lists, ti, ni,
+                                                             addr, base, acc, jrk, nnbid, err,
+                                                             inter);
+    else if (wide)
+      irr_firr32_kernel<false, 32><<<blocks, th, 0, st>>>(n, rec, p32, lmax, lists, ti, ni,
+                                                           addr, base, acc, jrk, nnbid, err,
+                                                           inter);
+    else
+      irr_firr32_kernel<false, IRR_G><<<blocks, th, 0, st>>>(n, rec, p32, lmax, lists, ti, ni,
+                                                              addr, base, acc, jrk, nnbid, err,
+                                                              inter);
   }
   return cudaGetLastError() == cudaSuccess ? GPUNB_OK : GPUNB_E_CUDA;
 }
@@ -488,6 +734,7 @@ static void open_lib(int nmax, int lmax, int rank) {
   }
   S.direct = (pageable && host_tables) ? 1 : 0;
   if (const char *p = getenv("GPUNB_HOST_DIRECT")) S.direct &= (atoi(p) != 0);
+  if (const char *p = getenv("GPUNB_IRR_PRECISION")) S.precision = atoi(p) == 0 ? 0 : 1;
   const size_t n = (size_t)std::max(nmax, 1);
   S.nmax = nmax;
   S.lmax = lmax;
@@ -501,8 +748,8 @@ static void open_lib(int nmax, int lmax, int rank) {
   S.seen.assign(n, 0u);
   S.epoch = 0;
   if (!S.rec_d.ensure(n * REC * sizeof(double)) ||
-      !S.list_d.ensure(n * (size_t)lmax * sizeof(int)) || !S.err_d.ensure(sizeof(int)) ||
-      !S.err_h.ensure(sizeof(int))) {
+      !S.list_d.ensure(n * (size_t)lmax * sizeof(int)) || !S.err_d.ensure(kStatusBytes) ||
+      !S.err_h.ensure(kStatusBytes)) {
     failf(GPUNB_E_ALLOC, "irr_simd_open_: device allocation for nmax = %d, lmax = %d failed",
           nmax, lmax);
     release_all();
@@ -597,7 +844,8 @@ static void firr_vec(double ti, int ni, const int *addr, double (*acc)[3], doubl
   const double t0 = wtime();
   cudaStream_t st = S.st;
   if (!upload()) return;
-  IRR_CUDA(cudaMemsetAsync(S.err_d.p, 0, sizeof(int), st), );
+  IRR_CUDA(cudaMemsetAsync(S.err_d.p, 0, kStatusBytes, st), );
+  unsigned long long *inter_d = (unsigned long long *)((char *)S.err_d.p + 8);
   double *pred = nullptr;
   if (32ll * ni >= S.nmax) {
     if (!S.pred_d.ensure((size_t)S.nmax * PRED * sizeof(double))) {
@@ -606,45 +854,54 @@ static void firr_vec(double ti, int ni, const int *addr, double (*acc)[3], doubl
     }
     pred = S.pred_d.as<double>();
   }
+  if (!S.addr_d.ensure((size_t)ni * sizeof(int)) ||
+      !S.out_d.ensure((size_t)ni * 6 * sizeof(double)) ||
+      !S.nid_d.ensure((size_t)ni * sizeof(int))) {
+    failf(GPUNB_E_ALLOC, "irr: output allocation failed");
+    return;
+  }
+  double *o = S.out_d.as<double>();
+  int *herr = S.err_h.as<int>();
   if (S.direct) {
-    // address list read, results written in the caller's arrays
-    if (launch_firr(S.nmax, S.rec_d.as<double>(), pred, S.lmax, S.list_d.as<int>(), ti, ni,
-                    addr, 1, &acc[0][0], &jrk[0][0], nnbid, S.err_d.as<int>(), st) != GPUNB_OK) {
-      failf(GPUNB_E_CUDA, "irr: force kernel launch failed");
-      return;
-    }
+    // the device reads the address list and writes the results in host
+    // memory itself, each with one coalesced copy kernel (the force kernel's
+    // scattered per-particle stores would cross the host link one by one)
+    HostCopyJobs in;
+    in.count = 1;
+    in.j[0] = HostCopyJob{addr, S.addr_d.p, ni, 4};
+    IRR_CUDA(launch_host_copy(in, st), );
   } else {
-    if (!S.addr_d.ensure((size_t)ni * sizeof(int)) ||
-        !S.out_d.ensure((size_t)ni * 6 * sizeof(double)) ||
-        !S.nid_d.ensure((size_t)ni * sizeof(int))) {
-      failf(GPUNB_E_ALLOC, "irr: output allocation failed");
-      return;
-    }
     IRR_CUDA(cudaMemcpyAsync(S.addr_d.p, addr, (size_t)ni * sizeof(int), cudaMemcpyHostToDevice,
                              st), );
-    double *o = S.out_d.as<double>();
-    if (launch_firr(S.nmax, S.rec_d.as<double>(), pred, S.lmax, S.list_d.as<int>(), ti, ni,
-                    S.addr_d.as<int>(), 1, o, o + 3 * (size_t)ni, S.nid_d.as<int>(),
-                    S.err_d.as<int>(), st) != GPUNB_OK) {
-      failf(GPUNB_E_CUDA, "irr: force kernel launch failed");
-      return;
-    }
+  }
+  if (launch_firr(S.nmax, S.rec_d.as<double>(), pred, S.precision, S.lmax, S.list_d.as<int>(),
+                  ti, ni, S.addr_d.as<int>(), 1, o, o + 3 * (size_t)ni, S.nid_d.as<int>(),
+                  S.err_d.as<int>(), inter_d, st) != GPUNB_OK) {
+    failf(GPUNB_E_CUDA, "irr: force kernel launch failed");
+    return;
+  }
+  // results, the error word and the call's listed pairs (for
+  // irr_simd_profile_)
+  if (S.direct) {
+    HostCopyJobs out;
+    out.count = 4;
+    out.j[0] = HostCopyJob{o, &acc[0][0], 3ll * ni, 8};
+    out.j[1] = HostCopyJob{o + 3 * (size_t)ni, &jrk[0][0], 3ll * ni, 8};
+    out.j[2] = HostCopyJob{S.nid_d.p, nnbid, ni, 4};
+    out.j[3] = HostCopyJob{S.err_d.p, herr, (long long)(kStatusBytes / 8), 8};
+    IRR_CUDA(launch_host_copy(out, st), );
+  } else {
     IRR_CUDA(cudaMemcpyAsync(&acc[0][0], o, (size_t)ni * 3 * sizeof(double),
                              cudaMemcpyDeviceToHost, st), );
     IRR_CUDA(cudaMemcpyAsync(&jrk[0][0], o + 3 * (size_t)ni, (size_t)ni * 3 * sizeof(double),
                              cudaMemcpyDeviceToHost, st), );
     IRR_CUDA(cudaMemcpyAsync(nnbid, S.nid_d.p, (size_t)ni * sizeof(int), cudaMemcpyDeviceToHost,
                              st), );
+    IRR_CUDA(cudaMemcpyAsync(herr, S.err_d.p, kStatusBytes, cudaMemcpyDeviceToHost, st), );
   }
-  int *herr = S.err_h.as<int>();
-  IRR_CUDA(cudaMemcpyAsync(herr, S.err_d.p, sizeof(int), cudaMemcpyDeviceToHost, st), );
   IRR_CUDA(cudaStreamSynchronize(st), );
   if (*herr) failf(*herr, "irr_simd_firr_vec_: an address or a listed id is out of range");
-  unsigned long long inter = 0;
-  for (int k = 0; k < ni; ++k) {
-    const int a = addr[k] - 1;
-    if (a >= 0 && a < S.nmax) inter += (unsigned long long)S.list_h[(size_t)a * S.lmax];
-  }
+  const unsigned long long inter = *(const unsigned long long *)((const char *)S.err_h.p + 8);
   S.num_inter += inter;
   S.num_fcall++;
   S.num_steps += (unsigned long long)ni;
@@ -746,8 +1003,21 @@ int irr_set_host_path(int mode) {
 int irr_firr_device(int n, const double *rec, int lmax, const int *lists, double ti, int ni,
                     const int *addr, double *acc, double *jrk, int *nnbid, void *stream) {
   if (n < 0 || lmax < 1 || ni < 0) return GPUNB_E_ARG;
+  std::lock_guard<std::mutex> lk(S.mu);
   cudaStream_t st = stream ? (cudaStream_t)stream : S.st;
-  return launch_firr(n, rec, nullptr, lmax, lists, ti, ni, addr, 0, acc, jrk, nnbid, nullptr, st);
+  // whole-set prediction into the library's buffer where it pays (as the
+  // host form); without the buffer, per-listing prediction (the same bits)
+  double *pred = nullptr;
+  if (32ll * ni >= n && n > 0 && S.pred_dev_d.ensure((size_t)n * PRED * sizeof(double)))
+    pred = S.pred_dev_d.as<double>();
+  return launch_firr(n, rec, pred, S.precision, lmax, lists, ti, ni, addr, 0, acc, jrk, nnbid,
+                     nullptr, nullptr, st);
+}
+
+int irr_set_precision(int mode) {
+  std::lock_guard<std::mutex> lk(S.mu);
+  S.precision = mode == 0 ? 0 : 1;
+  return S.precision;
 }
 
 }  // extern "C"

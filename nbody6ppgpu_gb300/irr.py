@@ -35,6 +35,7 @@ def _bind(lib):
         ("irr_simd_set_list_", [_I, _I], None),
         ("irr_simd_firr_vec_", [_D, _I, _I, _D, _D, _I], None),
         ("irr_set_host_path", [C.c_int], C.c_int),
+        ("irr_set_precision", [C.c_int], C.c_int),
     ]:
         f = getattr(lib, name)
         f.argtypes = args
@@ -44,9 +45,11 @@ def _bind(lib):
 class IrrSimd:
     """One open irregular-force library (the process-wide state of the C ABI)."""
 
-    def __init__(self, nmax: int, lmax: int, rank: int = 0):
+    def __init__(self, nmax: int, lmax: int, rank: int = 0, precision: int | None = None):
         self.lib = load()
         _bind(self.lib)
+        if precision is not None:
+            self.lib.irr_set_precision(int(precision))
         self.nmax, self.lmax = nmax, lmax
         self.lib.irr_simd_open_(C.byref(C.c_int(nmax)), C.byref(C.c_int(lmax)),
                                 C.byref(C.c_int(rank)))
@@ -64,6 +67,10 @@ class IrrSimd:
 
     def set_host_path(self, direct: bool) -> int:
         return self.lib.irr_set_host_path(1 if direct else 0)
+
+    def set_precision(self, mode: int) -> int:
+        """irr_set_precision: 1 = FP64 (the default), 0 = split FP32."""
+        return self.lib.irr_set_precision(int(mode))
 
     def set_jp(self, x0, v0, f, fdot, m, t0, idx=None) -> None:
         """irr_simd_set_jp_ for the particles idx (0-based; default all):
@@ -106,14 +113,25 @@ class IrrSimd:
             fn(C.byref(a), buf.ctypes.data_as(_I))
         _check(self.lib)
 
-    def firr(self, ti: float, active) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    def firr(self, ti: float, active, out=None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         """Irregular force, its derivative and the nearest neighbour (1-based,
-        0 for an empty list) of the 0-based particles `active` at time ti."""
+        0 for an empty list) of the 0-based particles `active` at time ti.
+        out: optional (acc [>=ni, 3] float64, jrk [>=ni, 3] float64, nnbid
+        [>=ni] int32) C-contiguous arrays to write into, kept between calls as
+        a Fortran caller keeps its arrays."""
         addr = np.ascontiguousarray(np.asarray(active) + 1, dtype=np.int32)
         ni = addr.shape[0]
-        acc = np.zeros((max(ni, 1), 3))
-        jrk = np.zeros((max(ni, 1), 3))
-        nid = np.zeros(max(ni, 1), dtype=np.int32)
+        if out is None:
+            acc = np.zeros((max(ni, 1), 3))
+            jrk = np.zeros((max(ni, 1), 3))
+            nid = np.zeros(max(ni, 1), dtype=np.int32)
+        else:
+            acc, jrk, nid = out
+            if not (acc.dtype == np.float64 and jrk.dtype == np.float64 and nid.dtype == np.int32
+                    and acc.flags.c_contiguous and jrk.flags.c_contiguous
+                    and nid.flags.c_contiguous and acc.shape[1:] == (3,)
+                    and jrk.shape[1:] == (3,) and min(len(acc), len(jrk), len(nid)) >= ni):
+                raise ValueError("out must be C-contiguous float64 [ni,3] x2 and int32 [ni]")
         self.lib.irr_simd_firr_vec_(C.byref(C.c_double(ti)), C.byref(C.c_int(ni)),
                                     addr.ctypes.data_as(_I), _dp(acc), _dp(jrk),
                                     nid.ctypes.data_as(_I))

@@ -9,6 +9,7 @@ module, as the checker or the timed CPU baseline; the product never imports it.
     RefAVX          the reference's own reg.avx.cpp / pot.avx.cpp compiled from
                     its sources into oracle/_ref (x86_64 hosts only)
     irr_fp64(...)   FP64 irregular force of src/Main/irr.avx.cpp (irr_fp64.c)
+    irr_abs_sums()  its per-particle sums of pair-term magnitudes (parity bound)
     RefIrrAVX       the reference's own irr.avx.cpp compiled into oracle/_ref
 """
 from __future__ import annotations
@@ -251,6 +252,45 @@ def irr_fp64(x0, v0, a2, j6, m, t0, lists, ti, addr):
                           lists.shape[1], lists.ctypes.data_as(_I), float(ti), ni,
                           addr.ctypes.data_as(_I), _dp(acc), _dp(jrk), nid.ctypes.data_as(_I))
     return acc, jrk, nid
+
+
+def irr_abs_sums(x0, v0, a2, j6, m, t0, lists, ti, addr):
+    """Sums of the magnitudes of the pair terms of the irregular force and
+    of its derivative, S_i = sum_j |q_ij|, for the particles addr (the same
+    prediction and terms as irr_fp64; listed bodies at zero distance add
+    nothing).  With them, parity_errors gives the cancellation-aware bound
+    of the split-precision irregular force.  FP64 numpy, rows processed in
+    chunks."""
+    m = np.asarray(m, dtype=np.float64)
+    n = m.shape[0]
+    x0, v0, a2, j6 = (np.asarray(a, dtype=np.float64).reshape(n, 3) for a in (x0, v0, a2, j6))
+    dt = (float(ti) - np.asarray(t0, dtype=np.float64))[:, None]
+    x = x0 + dt * (v0 + dt * (a2 + dt * j6))            # irr.avx.cpp:162-176
+    v = v0 + 2.0 * dt * (a2 + 1.5 * dt * j6)
+    lists = np.asarray(lists)
+    addr = np.asarray(addr, dtype=np.int64)
+    accabs = np.zeros(addr.shape[0])
+    jrkabs = np.zeros(addr.shape[0])
+    lmax = lists.shape[1]
+    for s in range(0, addr.shape[0], 1024):
+        a = addr[s:s + 1024]
+        cnt = np.maximum(lists[a, 0], 0)
+        w = int(min(max(int(cnt.max()) if cnt.size else 0, 1), lmax - 1))
+        k = np.arange(1, w + 1)[None, :]
+        valid = k <= cnt[:, None]
+        j = np.where(valid, lists[a, 1:w + 1], 0)
+        dx = x[j] - x[a][:, None, :]
+        dv = v[j] - v[a][:, None, :]
+        r2 = np.einsum("ijk,ijk->ij", dx, dx)
+        use = valid & (r2 > 0.0)
+        r2s = np.where(use, r2, 1.0)
+        rinv = 1.0 / np.sqrt(r2s)
+        mr3 = np.where(use, m[j] * rinv ** 3, 0.0)
+        al = -3.0 * np.einsum("ijk,ijk->ij", dx, dv) * rinv ** 2
+        accabs[s:s + 1024] = (mr3 * np.sqrt(r2s)).sum(axis=1)
+        jt = mr3[:, :, None] * (dv + al[:, :, None] * dx)
+        jrkabs[s:s + 1024] = np.linalg.norm(jt, axis=2).sum(axis=1)
+    return accabs, jrkabs
 
 
 class RefIrrAVX:

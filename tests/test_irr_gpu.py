@@ -1,9 +1,11 @@
 """GPU irregular force (include/irr.h, drop-in for src/Main/irr.avx.cpp)
-through its Fortran-style C ABI, against the FP64 oracle and the golden
-vectors of the reference's own irr.avx.cpp.
+through its Fortran-style C ABI in its FP64 mode (irr_set_precision(1)),
+against the FP64 oracle and the golden vectors of the reference's own
+irr.avx.cpp.  The split-precision default is tested in
+test_irr_split_gpu.py.
 
-Tolerances: the GPU computes in FP64, so against the FP64 oracle the force
-and its derivative agree to 1e-10 relative (the two differ only in fused
+Tolerances: in FP64 mode, against the FP64 oracle the force and its
+derivative agree to 1e-10 relative (the two differ only in fused
 multiply-adds) and the nearest neighbours are identical; against the
 reference's FP32 library they agree within its own error (2e-6 at the 99th
 percentile, 2e-5 maximum)."""
@@ -23,7 +25,7 @@ REF_P99, REF_MAX = 2e-6, 2e-5
 def _irr(g):
     from nbody6ppgpu_gb300.irr import IrrSimd
     n, lmax = len(g["m"]), g["lists"].shape[1]
-    irr = IrrSimd(n, lmax)
+    irr = IrrSimd(n, lmax, precision=1)
     irr.set_jp(g["x0"], g["v0"], g["f"], g["fdot"], g["m"], g["t0"])
     irr.set_lists(g["lists"])
     return irr
@@ -152,6 +154,7 @@ def test_device_resident_entry_point():
     J = torch.empty_like(A)
     NID = torch.empty(ni, dtype=torch.int32, device=dev)
     lib = load()
+    lib.irr_set_precision(1)
     fn = lib.irr_firr_device
     fn.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_int, C.c_void_p,
                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]

@@ -58,3 +58,28 @@ def test_reference_library_if_built():
     finally:
         r.close()
     assert np.array_equal(a, g["ref_acc"]) and np.array_equal(nid, g["ref_nnbid"])
+
+
+def test_abs_sums_bound_the_force_and_match_a_plain_loop():
+    """oracle.irr_abs_sums (the S_i of the split-precision parity bound): at
+    least |Q_i| for every particle, and equal to a plain per-pair loop."""
+    g = load_golden("irr_plummer2048")
+    args = (g["x0"], g["v0"], g["f"], g["fdot"], g["m"], g["t0"], g["lists"], float(g["ti"]),
+            g["active"])
+    a, j, _ = O.irr_fp64(*args)
+    sa, sj = O.irr_abs_sums(*args)
+    assert np.all(np.linalg.norm(a, axis=1) <= sa * (1 + 1e-12))
+    assert np.all(np.linalg.norm(j, axis=1) <= sj * (1 + 1e-12))
+    dt = (float(g["ti"]) - g["t0"])[:, None]
+    x = g["x0"] + dt * (g["v0"] + dt * (g["f"] + dt * g["fdot"]))
+    v = g["v0"] + 2.0 * dt * (g["f"] + 1.5 * dt * g["fdot"])
+    for k in range(0, len(g["active"]), 97):
+        i = int(g["active"][k])
+        ta = tj = 0.0
+        for jj in g["lists"][i, 1:1 + g["lists"][i, 0]]:
+            dx, dv = x[jj] - x[i], v[jj] - v[i]
+            r2 = float(dx @ dx)
+            if r2 > 0.0:
+                ta += g["m"][jj] / r2
+                tj += np.linalg.norm(g["m"][jj] / r2 ** 1.5 * (dv - 3.0 * (dx @ dv) / r2 * dx))
+        assert abs(sa[k] - ta) <= 1e-12 * ta and abs(sj[k] - tj) <= 1e-12 * tj
