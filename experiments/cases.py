@@ -7,6 +7,12 @@ Sends the j-set once and calls gpunb_regf_ `reps` times on the same active
 set (the first call warms the library up; a profiler is pointed at a later
 one).  Prints the per-call kernel time from the library's CUDA events and
 the mean neighbour count.
+
+    python -m experiments.cases --irr 0 --n 65536 --ni 65536 --reps 4
+
+adds, after the regular block, `reps` irregular-force calls (irr_simd_*,
+precision 0 = split FP32, 1 = FP64) of `ni` particles with the neighbour
+lists of a full regular block (self removed).
 """
 from __future__ import annotations
 
@@ -24,6 +30,7 @@ def main():
     ap.add_argument("--reps", type=int, default=4)
     ap.add_argument("--nnbmax", type=int, default=512)
     ap.add_argument("--target", type=float, default=100.0)
+    ap.add_argument("--irr", type=int, default=-1, help="irregular force precision (0, 1)")
     a = ap.parse_args()
     if a.model == "king":
         c = ics.king(a.n, seed=4, nb_target=a.target)
@@ -39,6 +46,42 @@ def main():
         times = nb.kernel_times()
     print(f"{a.model} N={c.n} ni={a.ni}: kernel ms per call {[round(t, 4) for t in times]}, "
           f"mean count {r.list[:, 0].mean():.1f}")
+    if a.irr >= 0:
+        irregular(c, h2, a)
+
+
+def irregular(c, h2, a):
+    import time
+
+    import numpy as np
+
+    from nbody6ppgpu_gb300.irr import IrrSimd
+    lmax = a.nnbmax + 1
+    with GpuNb(c.n) as nb:
+        nb.send(c.m, c.x, c.v)
+        r = nb.regf(h2, c.dtr, c.x, c.v, lmax, a.nnbmax)
+    lists = np.zeros_like(r.list)
+    for i in range(c.n):
+        ids = r.list[i, 1:1 + max(int(r.list[i, 0]), 0)]
+        ids = ids[ids != i]
+        lists[i, 0] = len(ids)
+        lists[i, 1:1 + len(ids)] = ids
+    rng = np.random.default_rng(7)
+    f = rng.normal(0.0, 0.5, (c.n, 3))
+    fdot = rng.normal(0.0, 0.5, (c.n, 3))
+    t0 = 1.0 - rng.uniform(0.0, 2e-3, c.n)
+    act = rng.permutation(c.n)[:a.ni]
+    out = (np.zeros((a.ni, 3)), np.zeros((a.ni, 3)), np.zeros(a.ni, dtype=np.int32))
+    with IrrSimd(c.n, lmax, precision=a.irr) as irr:
+        irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
+        irr.set_lists(lists)
+        ms = []
+        for _ in range(a.reps):
+            t = time.perf_counter()
+            irr.firr(1.0, act, out=out)
+            ms.append(1e3 * (time.perf_counter() - t))
+    print(f"irregular precision {a.irr} ni={a.ni}: {int(lists[act, 0].sum())} pairs, "
+          f"host-ABI ms per call {[round(t, 3) for t in ms]}")
 
 
 if __name__ == "__main__":

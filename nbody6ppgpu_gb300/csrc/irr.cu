@@ -114,6 +114,9 @@ __device__ __forceinline__ void state(const double *__restrict__ rec,
 constexpr int IRR_G = 8;
 constexpr int IRR_G_MIN_NI = 4 * 152 * IRR_WARPS;   // about 4 blocks per SM of GB300
 constexpr int IRR_U = 4;   // listings per lane in flight (split kernel)
+// split kernel: ~100 registers a thread, so blocks of 4 warps (5 per SM)
+// keep more warps resident than blocks of 8 (2 per SM)
+constexpr int IRR32_WARPS = 4;
 
 template <bool PRE, int G>
 __global__ void __launch_bounds__(32 * IRR_WARPS)
@@ -266,7 +269,7 @@ __device__ __forceinline__ void state32(const double *__restrict__ rec,
 // smallest normal float), the particle itself included, add nothing; the
 // nearest neighbour is chosen on the FP32 r^2 (ties to the smaller id).
 template <bool PRE, int G>
-__global__ void __launch_bounds__(32 * IRR_WARPS)
+__global__ void __launch_bounds__(32 * IRR32_WARPS)
     irr_firr32_kernel(int n, const double *__restrict__ rec, const float4 *__restrict__ pred,
                       int lmax, const int *__restrict__ lists, double ti, int ni,
                       const int *__restrict__ addr, int base, double *__restrict__ acc,
@@ -295,13 +298,23 @@ __global__ void __launch_bounds__(32 * IRR_WARPS)
       if (inter && sub == 0 && nnb > 0) atomicAdd(inter, (unsigned long long)nnb);
       // IRR_U listings per lane in flight: their ids, then their states, are
       // loaded before any is used, so the gathers' latencies overlap
+      // ids of the lane's next IRR_U listings; loaded one chunk ahead, so the
+      // row read of chunk c + 1 is in flight while chunk c computes
+      int jn[IRR_U];
+      auto load_ids = [&](int q0) {
+#pragma unroll
+        for (int u = 0; u < IRR_U; ++u) {
+          const int q = q0 + u * G;
+          jn[u] = q < nnb ? __ldg(row + 1 + q) : -1;
+        }
+      };
+      load_ids(sub);
       for (int q0 = sub; q0 < nnb; q0 += IRR_U * G) {
         int jv[IRR_U];
 #pragma unroll
         for (int u = 0; u < IRR_U; ++u) {
-          const int q = q0 + u * G;
-          jv[u] = q < nnb ? row[1 + q] : -1;
-          if (q < nnb && (jv[u] < 0 || jv[u] >= n)) {
+          jv[u] = jn[u];
+          if (q0 + u * G < nnb && (jv[u] < 0 || jv[u] >= n)) {
             flag(err, GPUNB_E_ARG);
             jv[u] = -1;
           }
@@ -316,6 +329,7 @@ __global__ void __launch_bounds__(32 * IRR_WARPS)
             for (int w = 0; w < PRED32; ++w) sj[u][w] = make_float4(0.f, 0.f, 0.f, 0.f);
           }
         }
+        load_ids(q0 + IRR_U * G);
         float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // at most IRR_U pairs in FP32
 #pragma unroll
         for (int u = 0; u < IRR_U; ++u) {
@@ -373,13 +387,20 @@ __global__ void __launch_bounds__(32 * IRR_WARPS)
         bj = oj;
       }
     }
-    if (sub == 0 && k < ni) {
+    // every lane of the particle now holds its sums: lane c < 6 converts and
+    // stores component c (one warp-wide conversion instead of six per
+    // particle on the FP64 pipe), lane 6 the nearest neighbour
+    if (k < ni) {
+      float h = hi[0], l = lo[0];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        acc[3 * (size_t)k + c] = (double)hi[c] + (double)lo[c];
-        jrk[3 * (size_t)k + c] = (double)hi[3 + c] + (double)lo[3 + c];
-      }
-      nnbid[k] = (bj == INT_MAX) ? 0 : bj + 1;
+      for (int c = 1; c < 6; ++c)
+        if (sub == c) {
+          h = hi[c];
+          l = lo[c];
+        }
+      if (sub < 3) acc[3 * (size_t)k + sub] = (double)h + (double)l;
+      else if (sub < 6) jrk[3 * (size_t)k + sub - 3] = (double)h + (double)l;
+      else if (sub == 6) nnbid[k] = (bj == INT_MAX) ? 0 : bj + 1;
     }
   }
 }
@@ -663,10 +684,11 @@ static int launch_firr(int n, const double *rec, double *pred, int prec, int lma
                        unsigned long long *inter, cudaStream_t st) {
   if (ni <= 0) return GPUNB_OK;
   const bool wide = ni < IRR_G_MIN_NI;   // 32 lanes per particle
-  const int per_block = IRR_WARPS * (wide ? 1 : 32 / IRR_G);   // particles per block and pass
+  const int warps = prec == 1 ? IRR_WARPS : IRR32_WARPS;
+  const int per_block = warps * (wide ? 1 : 32 / IRR_G);   // particles per block and pass
   const unsigned blocks =
       (unsigned)std::min<long long>((ni + per_block - 1) / per_block, 1ll << 20);
-  const unsigned th = 32 * IRR_WARPS;
+  const unsigned th = 32 * warps;
   const bool whole = pred && 32ll * ni >= n;
   if (prec == 1) {
     if (whole) irr_pred_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, rec, ti, pred);
