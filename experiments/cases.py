@@ -13,6 +13,12 @@ the mean neighbour count.
 adds, after the regular block, `reps` irregular-force calls (irr_simd_*,
 precision 0 = split FP32, 1 = FP64) of `ni` particles with the neighbour
 lists of a full regular block (self removed).
+
+    python -m experiments.cases --batched --reps 4
+
+runs instead `reps` steps (batched send + regf, graphs on) of the 256-cluster
+workload of the bench, a 256 MB fill between steps marking the step bounds
+in a launch list.
 """
 from __future__ import annotations
 
@@ -31,7 +37,11 @@ def main():
     ap.add_argument("--nnbmax", type=int, default=512)
     ap.add_argument("--target", type=float, default=100.0)
     ap.add_argument("--irr", type=int, default=-1, help="irregular force precision (0, 1)")
+    ap.add_argument("--batched", action="store_true", help="the 256-cluster batched step")
     a = ap.parse_args()
+    if a.batched:
+        batched(a)
+        return
     if a.model == "king":
         c = ics.king(a.n, seed=4, nb_target=a.target)
     else:
@@ -48,6 +58,38 @@ def main():
           f"mean count {r.list[:, 0].mean():.1f}")
     if a.irr >= 0:
         irregular(c, h2, a)
+
+
+def batched(a):
+    import time
+
+    import torch
+
+    from nbody6ppgpu_gb300 import workloads
+    from nbody6ppgpu_gb300.batch import DeviceBatch
+    from nbody6ppgpu_gb300.gpunb import load
+    lib = load()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    sets, active, h2, dtr, _ = workloads.clusters256()
+    nb = GpuNb(sum(len(s[0]) for s in sets))   # the library open, as the integrator has it
+    b = DeviceBatch(sets, active, 512, device=0, stream=stream)
+    b.set_radii(h2, dtr)
+    lib.gpunb_set_graphs(1)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ms = []
+    for _ in range(a.reps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        b.send()
+        b.regf()
+        torch.cuda.synchronize()
+        ms.append(1e3 * (time.perf_counter() - t))
+    print(f"batched 256 clusters: {b.total_ni} active, plan {b.last_plan()}, "
+          f"ms per step {[round(t, 3) for t in ms]}")
+    nb.close()
 
 
 def irregular(c, h2, a):

@@ -497,13 +497,16 @@ static int plan_splits(int variant, int ni, int ntile, bool mflag) {
   return (int)s;
 }
 
-// Shapes measured on GB300 (autotuner sweeps, N = 65536 Plummer and N = 2^20
-// King): below 512 i-particles one warp of 32 i with the j tile split over 8
-// warps (variant 2); up to 8191 4 warps x 32 i reading 4 j per warp vote
-// (variant 4, 5 blocks per SM); from 8192 on 8 j per vote (variant 6, 4
-// blocks per SM).
+// Shapes measured on GB300 (Plummer N = 65536, pair-kernel time of each
+// variant at its own split count): below 256 i-particles one warp of 32 i
+// with the j tile split over 8 warps (variant 2); from 256 on 4 warps x 32 i
+// reading 8 j per warp vote (variant 6, 4 blocks per SM), which beats the
+// 4-j vote at 5 blocks per SM (variant 4) by 3-5 % at every size from 512 to
+// 16384 (0.081 / 0.132 / 0.214 / 0.370 / 0.673 / 1.235 ms at ni = 512 ...
+// 16384 against 0.085 / 0.136 / 0.224 / 0.388 / 0.722 / 1.286) and variant 2
+// by 15 % at 256.
 static void heuristic_plan(int ni, int ntile, bool mflag, int &variant, int &splits) {
-  variant = ni < 512 ? 2 : (ni < 8192 ? 4 : 6);
+  variant = ni < 256 ? 2 : 6;
   splits = plan_splits(variant, ni, ntile, mflag);
 }
 

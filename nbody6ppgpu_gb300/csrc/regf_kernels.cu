@@ -1428,12 +1428,23 @@ static regf_fn regf_kernel_ptr(int v, bool mflag) {
 #undef GPUNB_RK
 }
 
+// Dynamic shared memory above 48 KB needs the kernel's opt-in attribute,
+// both to launch and for the occupancy calculator: queried without it, the
+// calculator reports no resident block at all.
+static cudaError_t allow_smem(regf_fn fn, size_t smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 int regf_ds_blocks_per_sm(int v, bool mflag) {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, regf_kernel_ptr(v, mflag),
-                                                    kVariants[v].threads(),
-                                                    regf_ds_smem(v)) != cudaSuccess)
+  regf_fn fn = regf_kernel_ptr(v, mflag);
+  if (allow_smem(fn, regf_ds_smem(v)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kVariants[v].threads(),
+                                                    regf_ds_smem(v)) != cudaSuccess) {
+    cudaGetLastError();
     return 1;
+  }
   return n > 0 ? n : 1;
 }
 
@@ -1450,8 +1461,8 @@ cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int
   const VariantDesc d = kVariants[v];
   regf_fn fn = regf_kernel_ptr(v, mflag);
   const size_t smem = regf_ds_smem(v);
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  {
+    const cudaError_t e = allow_smem(fn, smem);
     if (e != cudaSuccess) return e;
   }
   // the item counter, and with the merge in the kernel the per-i-tile counts

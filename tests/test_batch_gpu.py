@@ -132,3 +132,53 @@ def test_batch_autotune_picks_a_shape_on_the_batch_and_keeps_it(batch_case, tmp_
                                                  NNBMAX + 1, NNBMAX, with_abs=True)
         assert np.array_equal(np.asarray(r1.nnb[c]), lst[:, 0]), c
         check_split(r1.acc[c], r1.jrk[c], r1.pot[c], acc, jrk, pot, aa, ja, ok=lst[:, 0] >= 0)
+
+
+_PLAN_CHILD = r"""
+import sys
+sys.path.insert(0, {root!r})
+sys.path.insert(0, {tests!r})
+import numpy as np
+from nbody6ppgpu_gb300 import ics
+from nbody6ppgpu_gb300.batch import DeviceBatch
+from nbody6ppgpu_gb300.gpunb import GpuNb
+from test_batch_gpu import SPECS, NNBMAX
+sets, act, h2s, dtrs = [], [], [], []
+for n, seed, tgt, k in SPECS:
+    c = ics.plummer(n, seed=seed, masses="kroupa", nb_target=tgt)
+    a = ics.active_set(n, k, seed=seed)
+    sets.append((c.m, c.x, c.v)); act.append(a); h2s.append(c.h2()[a]); dtrs.append(c.dtr[a])
+with GpuNb(1 << 16) as nb:
+    if {warm}:
+        c = ics.plummer(4096, seed=1, nb_target=50.0)
+        nb.send(c.m, c.x, c.v)
+        for v in range(nb.lib.gpunb_num_variants()):
+            nb.set_launch(v, 0)
+            nb.regf(c.h2(), c.dtr, c.x, c.v, 257, 256)
+        nb.set_launch(-1, 0)
+    b = DeviceBatch(sets, act, NNBMAX)
+    b.set_radii(h2s, dtrs)
+    b.send()
+    b.regf()
+    print("PLAN", *b.last_plan())
+"""
+
+
+def test_first_launch_plans_with_full_residency():
+    """A batch whose plan is made before any pair kernel has run in the
+    process (so before any kernel's shared-memory opt-in) gets the same work
+    items as one made after every kernel shape has run: the occupancy
+    behind the plan counts every resident block from the first call."""
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    plans = []
+    for warm in (False, True):
+        src = _PLAN_CHILD.format(root=str(root), tests=str(root / "tests"), warm=warm)
+        r = subprocess.run([sys.executable, "-c", src], capture_output=True, text=True,
+                           timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        line = [ln for ln in r.stdout.splitlines() if ln.startswith("PLAN")][-1]
+        plans.append(tuple(int(t) for t in line.split()[1:]))
+    assert plans[0] == plans[1], plans
