@@ -258,3 +258,42 @@ def test_profile_counts_the_listed_pairs(capfd):
     assert int(f[f.index("Ncall:") + 1]) == 2
     assert int(f[f.index("<NI>:") + 1]) == pairs
     assert abs(float(f[f.index("<NB>:") + 1]) - pairs / len(act)) < 1e-6 * pairs
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_long_lists_both_lane_layouts(precision):
+    """Lists of ~300 neighbours (many chunks per lane), a block large enough
+    for 8 lanes per particle and a small one with 32, both precisions,
+    against the FP64 oracle."""
+    from nbody6ppgpu_gb300 import ics
+    from nbody6ppgpu_gb300.gpunb import GpuNb
+    from nbody6ppgpu_gb300.irr import IrrSimd
+    c = ics.plummer(8192, seed=9, masses="kroupa", nb_target=300.0)
+    lmax = 1025
+    with GpuNb(c.n) as nb:
+        nb.send(c.m, c.x, c.v)
+        r = nb.regf(c.h2(), c.dtr, c.x, c.v, lmax, 1024)
+    lists = np.zeros((c.n, lmax), dtype=np.int32)
+    for i in range(c.n):
+        ids = r.list[i, 1:1 + max(int(r.list[i, 0]), 0)]
+        ids = ids[ids != i]
+        lists[i, 0] = len(ids)
+        lists[i, 1:1 + len(ids)] = ids
+    assert lists[:, 0].mean() > 200
+    rng = np.random.default_rng(10)
+    f = rng.normal(0.0, 0.5, (c.n, 3))
+    fdot = rng.normal(0.0, 0.5, (c.n, 3))
+    ti = 0.5
+    t0 = ti - rng.uniform(0.0, 1e-3, c.n)
+    st = (c.x, c.v, f, fdot, c.m, t0, lists, ti)
+    with IrrSimd(c.n, lmax, precision=precision) as irr:
+        irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
+        irr.set_lists(lists)
+        for act in (np.arange(c.n), rng.permutation(c.n)[:300]):
+            a, j, nid = irr.firr(ti, act)
+            if precision == 0:
+                _check_vs_oracle(a, j, nid, st, act)
+            else:
+                oa, oj, on = O.irr_fp64(*st, act)
+                assert np.max(rel_vec_err(a, oa)) < 1e-10 and np.max(rel_vec_err(j, oj)) < 1e-10
+                assert np.array_equal(nid, on)
