@@ -284,7 +284,7 @@ struct Engine {
   long long num_inter = 0;
   long long icall = 0, ini = 0, isend = 0;
   // potential
-  DevBuf praw, ptiles, ppart, pout;
+  DevBuf praw, ptiles, ppart, pout, pperm, piperm, pbbox;
   PinBuf hp;
 };
 
@@ -1153,15 +1153,20 @@ void gpupot_(int *irank, int *istart, int *ni, int *n, double m[], double x[][3]
   }
   if (k == 0) return;
   cudaStream_t st = g.stream;
-  const int ntile = (nn + POT_JT - 1) / POT_JT;
+  // the set in Morton order, packed into the regular force's tile layout
+  // (own permutation and box buffers: the sent j-set's stay as they are)
+  const int ntile = (nn + JT - 1) / JT;
   const int itile = pot_itile();
   const int gx = (k + itile - 1) / itile;
-  const long long want = 2ll * g.n_sm * pot_blocks_per_sm();
+  const long long want = 2ll * g.n_sm * pot_rel_blocks_per_sm();
   int S = (int)std::max(1ll, std::min<long long>((want + gx - 1) / gx, std::max(1, ntile / 2)));
   const int ni_pad = gx * itile;
+  const bool whole = is0 == 0 && k == nn;   // i in the j-set's own Morton order
   if (!g.praw.ensure((size_t)nn * 4 * sizeof(double)) || !g.hp.ensure((size_t)nn * 4 * sizeof(double)) ||
-      !g.ptiles.ensure((size_t)std::max(ntile, 1) * POT_TILE_FLOATS * sizeof(float)) ||
-      !g.ppart.ensure((size_t)S * ni_pad * sizeof(double)) ||
+      !g.ptiles.ensure((size_t)std::max(ntile, 1) * TILE_FLOATS * sizeof(float)) ||
+      !g.pperm.ensure((size_t)std::max(ntile, 1) * JT * sizeof(int)) ||
+      !g.piperm.ensure((size_t)k * sizeof(int)) || !g.pbbox.ensure_zero(BBOX_INTS * sizeof(int)) ||
+      !ensure_order_scratch(nn) || !g.ppart.ensure((size_t)S * ni_pad * sizeof(double)) ||
       !g.pout.ensure((size_t)k * sizeof(double) + sizeof(int)))
     return;
   double *h = g.hp.as<double>();
@@ -1170,11 +1175,27 @@ void gpupot_(int *irank, int *istart, int *ni, int *n, double m[], double x[][3]
   double *d = g.praw.as<double>();
   CUDA_OR(cudaMemsetAsync(g.err.p, 0, sizeof(int), st), );
   CUDA_OR(cudaMemcpyAsync(d, h, (size_t)nn * 4 * sizeof(double), cudaMemcpyHostToDevice, st), );
-  CUDA_OR(launch_pack_pot(d, d + nn, nn, g.ptiles.as<float>(), ntile, g.err.as<int>(), st), );
-  CUDA_OR(launch_pot(g.ptiles.as<float>(), ntile, d + nn, is0, k, gx, S, g.ppart.as<double>(),
-                     ni_pad, g.err.as<int>(), st), );
+  int *perm = g.pperm.as<int>();
+  CUDA_OR(launch_bbox(d + nn, nn, g.pbbox.as<int>(), st), );
+  CUDA_OR(launch_order(d + nn, nn, g.pbbox.as<int>(), g.okeys.as<unsigned long long>(),
+                       g.okeys_alt.as<unsigned long long>(), g.ovals_alt.as<int>(), perm,
+                       g.otemp.p, g.otemp.bytes, st), );
+  if (ntile * JT > nn)
+    CUDA_OR(cudaMemsetAsync(perm + nn, 0xff, (size_t)(ntile * JT - nn) * sizeof(int), st), );
+  CUDA_OR(launch_pack_jtiles(d, d + nn, nullptr, nn, perm, g.ptiles.as<float>(), ntile,
+                             g.err.as<int>(), st), );
+  const int *iorder = perm;
+  if (!whole) {
+    CUDA_OR(launch_order(d + nn + 3 * (size_t)is0, k, g.pbbox.as<int>(),
+                         g.okeys.as<unsigned long long>(), g.okeys_alt.as<unsigned long long>(),
+                         g.ovals_alt.as<int>(), g.piperm.as<int>(), g.otemp.p, g.otemp.bytes,
+                         st), );
+    iorder = g.piperm.as<int>();
+  }
+  CUDA_OR(launch_pot_rel(g.ptiles.as<float>(), ntile, d + nn, iorder, is0, k, gx, S,
+                         g.ppart.as<double>(), ni_pad, g.err.as<int>(), st), );
   CUDA_OR(launch_pot_merge(g.ppart.as<double>(), S, k, ni_pad, g.err.as<int>(),
-                           g.pout.as<double>(), st), );
+                           g.pout.as<double>(), st, iorder), );
   // results land in the staging buffer (reused: m/x no longer needed)
   CUDA_OR(cudaMemcpyAsync(h, g.pout.p, (size_t)k * sizeof(double), cudaMemcpyDeviceToHost, st), );
   int herr = 0;

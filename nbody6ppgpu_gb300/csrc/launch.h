@@ -103,6 +103,12 @@ cudaError_t launch_pot(const float *tiles, int ntile, const double *x, int istar
 int pot_blocks_per_sm();
 // err (may be null): the call's device error word; nonzero -> every pot[i] = NaN
 cudaError_t launch_pot_merge(const double *part, int S, int ni, int ni_pad, const int *err,
-                             double *pot, cudaStream_t st);
+                             double *pot, cudaStream_t st, const int *iorder = nullptr);
+// potential on the regular force's Morton-ordered tiles (pack_jtiles with
+// v = null); slot s of the i-range is the i-particle istart0 + iorder[s]
+int pot_rel_blocks_per_sm();
+cudaError_t launch_pot_rel(const float *tiles, int ntile, const double *x, const int *iorder,
+                           int istart0, int ni, int gx, int S, double *part, int ni_pad, int *err,
+                           cudaStream_t st);
 
 }  // namespace gpunb

@@ -19,18 +19,6 @@
 #include <cfloat>
 #include <climits>
 
-// A tile is "near" an i-particle, and its pairs take the double-single
-// coordinate path, when |O - x_i|^2 < GPUNB_NEAR_K2 R^2.  With K = 2 every
-// pair of a far tile is at least R away, so the tile-relative rounding
-// (2^-22 (R + |dx|) per axis) stays within 2^-21 |dx|.  Measured against the
-// FP64 kernel (Plummer 65536 and King 2^20, ni = 16384): force and jerk
-// errors equal to the all-double-single kernel's to two digits, while
-// K = 0 (every tile relative) doubled the jerk's 99th percentile; the pair
-// kernel gains 7% (N = 65536) to 13% (N = 2^20) over K = infinity.
-#ifndef GPUNB_NEAR_K2
-#define GPUNB_NEAR_K2 4.0f
-#endif
-
 // The FP32 chunk sums of the pair loop are folded into the float-float
 // accumulators every GPUNB_FOLD_TILES tiles (64 terms per f32x2 half per
 // tile).
@@ -85,6 +73,7 @@ __device__ __forceinline__ void block_maxf(float (&a)[NV], float (*s)[NV]) {
 // formed in FP32 from the rounded values and widened by 2^-18 with upward
 // rounding: the FP32 evaluation of |v|, |x - O| and sqrt(m) is within 2^-21
 // of the exact value, so the stored maxima stay upper bounds.
+// v may be null (the potential's tiles): velocity fields and maxima are 0.
 __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restrict__ m,
                                                          const double *__restrict__ x,
                                                          const double *__restrict__ v, int nj,
@@ -102,7 +91,7 @@ __global__ void __launch_bounds__(JT) pack_jtiles_kernel(const double *__restric
     for (int c = 0; c < 3; ++c) {
       xj[c] = x[3 * j + c];
       xf[c] = (float)xj[c];
-      vf[c] = (float)v[3 * j + c];
+      vf[c] = v ? (float)v[3 * j + c] : 0.f;
     }
     mf = (float)m[j];
     if (isnan(xf[0]) || isnan(xf[1]) || isnan(xf[2]) || isnan(vf[0]) || isnan(vf[1]) ||

@@ -310,6 +310,42 @@ def test_gpupot_coincident_and_large(lib):
     assert np.isfinite(p[10]) and np.isfinite(p[11])
 
 
+def test_gpupot_morton_tiles(lib, plummer64k):
+    """gpupot_ runs on Morton-ordered tiles with tile-relative coordinates for
+    far tiles: the whole set, a sub-range (its own order), a clump of bodies
+    at one point (a tile of radius 0), against the FP64 oracle; and a call
+    between gpunb_send_ and gpunb_regf_ leaves the regular force unchanged,
+    bit for bit."""
+    c = plummer64k
+    p = gpupot(c.m, c.x)
+    samp = np.arange(0, c.n, 211)
+    o = np.array([O.pot_fp64(c.m, c.x, int(i) + 1, 1)[0] for i in samp])
+    assert (np.abs(p[samp] - o) / o).max() < 1e-6
+    istart, ni = 12345, 20000
+    q = gpupot(c.m, c.x, istart=istart, ni=ni)
+    ref = p[istart - 1:istart - 1 + ni]
+    assert (np.abs(q - ref) / ref).max() < 1e-6
+    qs = np.arange(0, ni, 97)
+    o = np.array([O.pot_fp64(c.m, c.x, istart + int(k), 1)[0] for k in qs])
+    assert (np.abs(q[qs] - o) / o).max() < 1e-6
+    # 300 bodies at one point: they see each other at r = 0 (skipped)
+    m, x = c.m[:4096].copy(), c.x[:4096].copy()
+    x[:300] = x[300]
+    r = gpupot(m, x)
+    idx = np.r_[0:5, 295:305, 4000:4096:7]
+    o = np.array([O.pot_fp64(m, x, int(i) + 1, 1)[0] for i in idx])
+    assert np.all(np.isfinite(r)) and (np.abs(r[idx] - o) / o).max() < 1e-6
+    act = ics.active_set(c.n, 1024, seed=5)
+    h2 = c.h2()
+    with GpuNb(c.n) as nb:
+        nb.send(c.m, c.x, c.v)
+        r1 = nb.regf(h2[act], c.dtr[act], c.x[act], c.v[act], 513, 512)
+        gpupot(c.m[::2], c.x[::2])
+        r2 = nb.regf(h2[act], c.dtr[act], c.x[act], c.v[act], 513, 512)
+    for a, b in ((r1.acc, r2.acc), (r1.jrk, r2.jrk), (r1.pot, r2.pot), (r1.list, r2.list)):
+        assert np.array_equal(a, b)
+
+
 def test_host_paths_identical(lib, plummer64k):
     """Direct host arrays (device writes the rows) and pinned staging give the
     same bytes, including overflow rows and blocks above the host-scatter
