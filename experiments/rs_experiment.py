@@ -134,7 +134,7 @@ def run(model="king", n=16384, ticks=64, nnbopt=100, nnbmax=200, levels=6, epoch
     return out
 
 
-def config5(ticks_harvest=48, ticks_eval=48, n_king=1 << 20, n_plummer=65536, nnbopt=100,
+def pooled_king(ticks_harvest=48, ticks_eval=48, n_king=1 << 20, n_plummer=65536, nnbopt=100,
             nnbmax=200, levels=6, epochs=25, q=0.1, band=PRED_BAND, eval_seed=41,
             max_pairs=2_000_000, guard="max", harvest_every=1):
     """The learned-radius configuration: training pairs harvested with the
@@ -169,7 +169,7 @@ def config5(ticks_harvest=48, ticks_eval=48, n_king=1 << 20, n_plummer=65536, nn
     losses = mlp.train(X, Y, epochs=epochs)
     t_train = time.perf_counter() - t0
     c = make("king", n_king, eval_seed, nnbopt, q)
-    out = {"config": "config 5: King W0=6 evaluation model, pairs from Plummer/Kroupa and King",
+    out = {"config": "King W0=6 evaluation model, pairs pooled from Plummer/Kroupa and King runs",
            "n_eval": n_king, "q": q, "ticks_harvest": ticks_harvest, "ticks_eval": ticks_eval,
            "band": band, "guard": guard, "nnbopt": nnbopt, "nnbmax": nnbmax, "levels": levels,
            "harvest_every_king": harvest_every, "harvest_sources": sources, "train_pairs": int(len(X)),
@@ -194,14 +194,14 @@ def config5(ticks_harvest=48, ticks_eval=48, n_king=1 << 20, n_plummer=65536, nn
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config5", action="store_true",
-                    help="the config-5 protocol (pairs from Plummer and King runs, evaluation "
-                         "on a King model of --n bodies)")
+    ap.add_argument("--pooled-king", action="store_true",
+                    help="pairs pooled from a Plummer run of 65536 bodies and a King run of "
+                         "--n bodies, evaluation on a further King model of --n bodies")
     ap.add_argument("--ticks-harvest", type=int, default=48)
     ap.add_argument("--harvest-every", type=int, default=1,
-                    help="config 5: label only the King bodies i %% k == 0")
+                    help="--pooled-king: label only the King bodies i %% k == 0")
     ap.add_argument("--eval-seed", type=int, default=41,
-                    help="config 5: seed of the King model the policies are evaluated on")
+                    help="--pooled-king: seed of the King model the policies are evaluated on")
     ap.add_argument("--model", default="king", choices=["king", "plummer"])
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--ticks", type=int, default=64)
@@ -225,8 +225,8 @@ def main():
                     help="with --diag: save a sample of the per-row diagnostics to "
                          "<prefix>_<leg>.npy (label, y, motion, static, target, accepted)")
     a = ap.parse_args()
-    if a.config5:
-        print(json.dumps(config5(a.ticks_harvest, a.ticks, n_king=a.n, nnbopt=a.nnbopt,
+    if a.pooled_king:
+        print(json.dumps(pooled_king(a.ticks_harvest, a.ticks, n_king=a.n, nnbopt=a.nnbopt,
                                  nnbmax=a.nnbmax, levels=a.levels, epochs=a.epochs, q=a.q,
                                  band=tuple(a.band), guard=a.guard,
                                  harvest_every=a.harvest_every, eval_seed=a.eval_seed)),
