@@ -346,6 +346,31 @@ def test_gpupot_morton_tiles(lib, plummer64k):
         assert np.array_equal(a, b)
 
 
+def test_profile_counters(lib, capfd):
+    """gpunb_profile_ prints the reference's line (gpunb.velocity.cu:882-902):
+    sends and regular calls since the last profile, <Ni> = active particles
+    per send, a positive rate; then resets, so a second call prints nothing."""
+    c = ics.plummer(4096, seed=8, nb_target=50.0)
+    h2 = c.h2()
+    with GpuNb(c.n) as nb:
+        nb.profile()
+        capfd.readouterr()
+        nb.send(c.m, c.x, c.v)
+        nb.send(c.m, c.x, c.v)
+        for k in (100, 200, 300):
+            nb.regf(h2[:k], c.dtr[:k], c.x[:k], c.v[:k], 129, 128)
+        nb.profile()
+        err = capfd.readouterr().err
+        nb.profile()
+        again = capfd.readouterr().err
+    line = [ln for ln in err.splitlines() if "Reg.F" in ln][-1]
+    f = line.replace("(s)", "").split()
+    assert int(f[f.index("Nsend") + 1]) == 2 and int(f[f.index("Ngrav") + 1]) == 3
+    assert int(f[f.index("<Ni>") + 1]) == 300
+    assert float(f[f.index("Perf.(Gflops)") + 1]) > 0
+    assert "Reg.F" not in again
+
+
 def test_host_paths_identical(lib, plummer64k):
     """Direct host arrays (device writes the rows) and pinned staging give the
     same bytes, including overflow rows and blocks above the host-scatter
