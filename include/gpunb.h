@@ -88,8 +88,9 @@ void gpunb_set_abort_on_error(int flag);    /* 1 (default): print + abort() */
  * 1 = plain FP64. */
 void gpunb_set_precision(int mode);
 
-/* Force a launch shape (variant index, j-splits); -1/0 restores the
- * autotuned or heuristic choice.  gpunb_num_variants() lists the shapes. */
+/* Force a launch shape (variant index, j-splits; for the batched entry
+ * points, work items per resident block instead of j-splits); -1/0 restores
+ * the autotuned or heuristic choice.  gpunb_num_variants() lists the shapes. */
 void gpunb_set_launch(int variant, int splits);
 int gpunb_num_variants(void);
 int gpunb_variant_info(int variant, int *ipt, int *warps_i, int *warps_j);
