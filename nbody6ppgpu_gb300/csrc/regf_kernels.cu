@@ -972,14 +972,11 @@ __global__ void __launch_bounds__(128) regf_fp64_kernel(const JSet js, const ISe
         record_neighbour(out, i, jb + jj);
         continue;
       }
-      // 1/r from the FP32 estimate and two Newton steps in FP64 (relative
-      // error below 2^-80 before rounding: FP64-exact to a few ulp) instead of
-      // an FP64 division and square root, which cost about as many FP64
-      // instructions as the rest of the pair on a part whose FP64 pipe runs
-      // at 1/64 of the FP32 rate
-      double y = (double)rsqrt_est((float)r2);
-      y = fma(0.5 * y, fma(-r2 * y, y, 1.0), y);
-      y = fma(0.5 * y, fma(-r2 * y, y, 1.0), y);
+      // 1/r with the FP64 reciprocal square root (rsqrt), not an FP64
+      // division and square root, which cost about as many FP64 instructions
+      // as the rest of the pair on a part whose FP64 pipe runs at 1/64 of the
+      // FP32 rate
+      const double y = rsqrt(r2);
       const double dr2i = y * y;
       const double mr = sm[jj] * y;              // m/r
       const double dr3i = mr * dr2i;             // m/r^3
