@@ -335,6 +335,12 @@ def test_gpupot_morton_tiles(lib, plummer64k):
     idx = np.r_[0:5, 295:305, 4000:4096:7]
     o = np.array([O.pot_fp64(m, x, int(i) + 1, 1)[0] for i in idx])
     assert np.all(np.isfinite(r)) and (np.abs(r[idx] - o) / o).max() < 1e-6
+    # tiny and ragged sets: one body (nothing at r > 0), two, one tile plus one
+    assert gpupot(c.m[:1], c.x[:1])[0] == 0.0
+    for k in (2, 129):
+        r = gpupot(c.m[:k], c.x[:k])
+        o = O.pot_fp64(c.m[:k], c.x[:k], 1, k)
+        assert (np.abs(r - o) / o).max() < 1e-6
     act = ics.active_set(c.n, 1024, seed=5)
     h2 = c.h2()
     with GpuNb(c.n) as nb:
