@@ -104,6 +104,27 @@ def test_config2_block_sizes(lib, plummer64k, ni):
     check_forces(sub, acc, jrk, pot, aa, ja)
 
 
+@pytest.mark.parametrize("ni", [1024, 16384])
+def test_config2_mass_weighted_criterion(lib, plummer64k, ni):
+    """The mass-weighted neighbour criterion (m_flag: r^2 < m_j h2 with
+    h2 = RS^2 / <m>, util_gpu.F:48) on the Plummer N = 65536 Kroupa cluster:
+    512 sampled rows of the block against the FP64 oracle, lists identical,
+    the named bound."""
+    c = plummer64k
+    act = ics.active_set(c.n, ni, seed=ni + 7)
+    h2m = c.h2() / c.m.mean()
+    with GpuNb(c.n) as nb:
+        nb.send(c.m, c.x, c.v)
+        res = nb.regf(h2m[act], c.dtr[act], c.x[act], c.v[act], 513, 512, m_flag=1)
+    samp = np.arange(ni) if ni <= 1024 else np.linspace(0, ni - 1, 512).astype(int)
+    a = act[samp]
+    acc, jrk, pot, lst, aa, ja = O.regf_fp64(c.m, c.x, c.v, h2m[a], c.dtr[a], c.x[a], c.v[a],
+                                             513, 512, m_flag=1, with_abs=True)
+    sub = type(res)(acc=res.acc[samp], jrk=res.jrk[samp], pot=res.pot[samp], list=res.list[samp])
+    assert rows_equal(sub.list, lst) == []
+    check_forces(sub, acc, jrk, pot, aa, ja)
+
+
 def test_autotune_on_the_callers_block_is_cached_saved_and_loaded(lib, plummer64k, tmp_path):
     """gpunb_set_autotune(1): the first call of an (N, ni) bucket times every
     launch shape on that call's own block and keeps the fastest.  The tuned
