@@ -211,6 +211,9 @@ def cpu_side_checks(c, irr_check=None, pot_result=None):
         a, j, nid = irr_check["gpu"]["fp64"]
         ea = np.linalg.norm(a[ok] - oa[ok], axis=1) / np.linalg.norm(oa[ok], axis=1)
         sa, sj = O.irr_abs_sums(*st)
+        a, j, nid_d = irr_check["gpu"]["double_float"]
+        ed = max(float((np.linalg.norm(a[ok] - oa[ok], axis=1) / np.linalg.norm(oa[ok], axis=1)).max()),
+                 float((np.linalg.norm(j[ok] - oj[ok], axis=1) / np.linalg.norm(oj[ok], axis=1)).max()))
         a, j, nid_s = irr_check["gpu"]["split"]
         ones = np.ones(len(act))
         pe = O.parity_errors(a[ok], j[ok], ones[ok], oa[ok], oj[ok], ones[ok], sa[ok], sj[ok])
@@ -220,6 +223,8 @@ def cpu_side_checks(c, irr_check=None, pot_result=None):
                             "gpairs_s": int(lists[act, 0].sum()) / dt / 1e9,
                             "gpu_fp64_max_rel_err_vs_fp64_oracle": float(ea.max()),
                             "gpu_fp64_nnbid_identical": bool(np.array_equal(nid, on)),
+                            "gpu_double_float_max_rel_err_vs_fp64_oracle": ed,
+                            "gpu_double_float_nnbid_identical": bool(np.array_equal(nid_d, on)),
                             "gpu_split_parity_vs_fp64_oracle": pe,
                             "gpu_split_nnbid_differing": int(np.sum(nid_s != on))}
     if pot_result is not None:
@@ -594,13 +599,15 @@ def irregular_leg(c, h2, lists_src, dev=None):
     t0 = ti - rng.uniform(0.0, 2e-3, n)
     blocks = {ni: rng.permutation(n)[:ni] for ni in (1024, 16384, n)}
     out = {"workload": "Plummer N=65536 (the bench cluster), lists of its regular block",
-           "precision": "fp64 (the default) and split FP32 (irr_set_precision(0): "
-                        "double-single positions after an FP64 prediction)",
-           "host_abi": {"split": {}, "fp64": {}}, "device": {"split": {}, "fp64": {}}}
+           "precision": "double-float on the FP32 pipe (the default), fp64 "
+                        "(irr_set_precision(1)) and split FP32 (irr_set_precision(0): "
+                        "double-single positions); an FP64 prediction in every mode",
+           "host_abi": {"double_float": {}, "split": {}, "fp64": {}},
+           "device": {"double_float": {}, "split": {}, "fp64": {}}}
     with IrrSimd(n, lmax) as irr:
         irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
         irr.set_lists(lists)
-        for prec, key in ((0, "split"), (1, "fp64")):
+        for prec, key in ((2, "double_float"), (0, "split"), (1, "fp64")):
             irr.set_precision(prec)
             for ni, act in blocks.items():
                 pairs = int(lists[act, 0].sum())
@@ -614,7 +621,7 @@ def irregular_leg(c, h2, lists_src, dev=None):
                     best = min(best, time.perf_counter() - t)
                 out["host_abi"][key][str(ni)] = {"pairs": pairs, "ms": best * 1e3,
                                                  "gpairs_s": pairs / best / 1e9}
-        irr.set_precision(1)
+        irr.set_precision(2)
         # predict-and-send from the stored state vs gpunb_send_ of host arrays
         from nbody6ppgpu_gb300.gpunb import GpuNb
         from nbody6ppgpu_gb300.irr import send_predicted
@@ -642,7 +649,7 @@ def irregular_leg(c, h2, lists_src, dev=None):
                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     fn.restype = C.c_int
     st = torch.cuda.Stream(dev)
-    for prec, key in ((0, "split"), (1, "fp64")):
+    for prec, key in ((2, "double_float"), (0, "split"), (1, "fp64")):
         lib.irr_set_precision(prec)
         for ni, act in blocks.items():
             A = torch.tensor(act.astype(np.int32), device=dev)
@@ -665,19 +672,21 @@ def irregular_leg(c, h2, lists_src, dev=None):
             ms = e0.elapsed_time(e1) / reps
             pairs = int(lists[act, 0].sum())
             out["device"][key][str(ni)] = {"ms": ms, "gpairs_s": pairs / ms / 1e6}
-    lib.irr_set_precision(1)
+    lib.irr_set_precision(2)
     s16, f16 = out["device"]["split"][str(n)], out["device"]["fp64"][str(n)]
+    d16 = out["device"]["double_float"][str(n)]
     out["device"]["split_over_fp64_ni65536"] = f16["ms"] / s16["ms"]
+    out["device"]["double_float_over_fp64_ni65536"] = f16["ms"] / d16["ms"]
     # a block of 16384 for the CPU-baseline leg (timing and the FP64 checks)
     act = blocks[16384]
     res = {}
     with IrrSimd(n, lmax) as irr:
         irr.set_jp(c.x, c.v, f, fdot, c.m, t0)
         irr.set_lists(lists)
-        for prec, key in ((0, "split"), (1, "fp64")):
+        for prec, key in ((2, "double_float"), (0, "split"), (1, "fp64")):
             irr.set_precision(prec)
             res[key] = irr.firr(ti, act)
-        irr.set_precision(1)
+        irr.set_precision(2)
     check = {"state": (c.x, c.v, f, fdot, c.m, t0, lists, ti, act), "gpu": res}
     return out, check
 

@@ -18,17 +18,19 @@
  * and returns the force and its derivative from the neighbours,
  *     acc += m dx / r^3,  jrk += m / r^3 (dv - 3 (dx.dv) / r^2 dx),
  * and nnbid = the Fortran index of the nearest listed neighbour (0 for an
- * empty list).  Precision (irr_set_precision): FP64 throughout by default,
- * or the reference's own scheme -- double-single positions, FP32 velocities,
- * masses and force arithmetic (irr.avx.cpp:58-176) -- after an FP64
- * prediction, with the nearest neighbour taken on the FP32 r^2: the
- * accuracy class of the reference's library (force and derivative within
- * 2e-6 of FP64 at the 99th percentile, within 5e-6 of max(|Q|, S/8) per
- * particle, S the sum of the terms' magnitudes).
+ * empty list).  Precision (irr_set_precision), the prediction in FP64 in
+ * every mode: by default double-float arithmetic (hi + lo pairs of floats,
+ * error-free transforms) on the FP32 pipe, within ~1e-11 of FP64; FP64
+ * throughout; or the reference's own scheme -- double-single positions, FP32
+ * velocities, masses and force arithmetic (irr.avx.cpp:58-176), the nearest
+ * neighbour taken on the FP32 r^2: the accuracy class of the reference's
+ * library (force and derivative within 2e-6 of FP64 at the 99th percentile,
+ * within 5e-6 of max(|Q|, S/8) per particle, S the sum of the terms'
+ * magnitudes).
  * Deliberate differences: no 600-entry list cap (lmax up to 2^16 per row);
  * a listed body at zero distance (the particle itself) adds nothing instead
- * of a NaN (in split precision: any body closer than 1e-19); invalid
- * addresses or ids are reported as GPUNB_E_ARG.
+ * of a NaN (in the double-float and split modes: any body closer than
+ * 1e-19); invalid addresses or ids are reported as GPUNB_E_ARG.
  *
  * set_jp / set_list are safe to call concurrently for different particles
  * (the Fortran callers run them inside OpenMP loops); they only update host
@@ -58,10 +60,10 @@ void irr_simd_firr_vec_(double *ti, int *ni, int addr[], double acc[][3], double
  * the mode in effect, -1 without a device. */
 int irr_set_host_path(int mode);
 
-/* Arithmetic of the force: 1 (default) = FP64, 0 = split FP32 as above
- * (the prediction is FP64 in both).  Also set at irr_simd_open_ from the
- * environment variable GPUNB_IRR_PRECISION.  Applies to the next force call,
- * host or device-resident form.  Returns the mode in effect. */
+/* Arithmetic of the force: 2 (default) = double-float, 1 = FP64, 0 = split
+ * FP32, as above.  Also set at irr_simd_open_ from the environment variable
+ * GPUNB_IRR_PRECISION.  Applies to the next force call, host or
+ * device-resident form.  Returns the mode in effect. */
 int irr_set_precision(int mode);
 
 /* Device-resident form: state and lists already in device memory, 0-based

@@ -8,10 +8,11 @@
 // AVX on the host cores.  Here the same calls update host mirrors and append
 // the particle to a dirty list (lock-free, so the OpenMP callers stay
 // parallel); the next force call uploads only the changed records and rows,
-// then one warp per active particle predicts the particle and its listed
-// neighbours to the block time (FP64) and sums the force in FP64 (the
-// default) or in split FP32 (the reference's own precision scheme, about 30
-// times faster on GB300).  On systems
+// then 8 or 32 lanes per active particle predict the particle and its listed
+// neighbours to the block time (FP64) and sum the force in double-float
+// arithmetic on the FP32 pipe (the default: within ~1e-11 of FP64, 4x faster
+// than FP64 on GB300), in FP64, or in split FP32 (the reference's own
+// precision scheme, 7.6x faster than FP64).  On systems
 // where the device reads pageable memory coherently (Grace + GB300 over
 // NVLink-C2C) the kernels read the mirrors, the address list and write the
 // results in host memory directly; elsewhere they go through pinned staging.
@@ -405,6 +406,219 @@ __global__ void __launch_bounds__(32 * IRR32_WARPS)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float precision (irr_set_precision(2), the default): FP64-class results from the
+// FP32 pipe.  Every quantity is an unevaluated sum hi + lo of two floats
+// (about 48 significant bits) and every operation an error-free transform
+// (Knuth's TwoSum, the FMA product error) followed by renormalisation, the
+// classic double-single arithmetic of Dekker (1971), so that a pair costs
+// ~300 FP32 operations instead of ~40 FP64 ones: on GB300, whose FP64 pipe
+// runs at 1/64 of the FP32 rate, that is several times faster, at a relative
+// error near 1e-13 per term.  Positions, velocities and masses are the
+// double-single split of the FP64 prediction (4 float4 = 64 bytes per
+// particle, two sectors when gathered); 1/r is the hardware estimate refined
+// by one Newton step carried in double-float (error ~2^-45).
+struct dfl {
+  float h, l;
+};
+__device__ __forceinline__ dfl df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ dfl df_fast(float a, float b) {   // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+  const dfl s = df_two_sum(a.h, b.h);
+  return df_fast(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return df_fast(p, e);
+}
+__device__ __forceinline__ dfl df_mulf(dfl a, float b) {
+  const float p = __fmul_rn(a.h, b);
+  return df_fast(p, fmaf(a.l, b, fmaf(a.h, b, -p)));
+}
+__device__ __forceinline__ dfl df_sqr(dfl a) {
+  const float p = __fmul_rn(a.h, a.h);
+  return df_fast(p, fmaf(__fmul_rn(2.0f, a.h), a.l, fmaf(a.h, a.h, -p)));
+}
+// difference of two double-single values b - a
+__device__ __forceinline__ dfl df_diff(float bh, float bl, float ah, float al) {
+  const dfl s = df_two_sum(bh, -ah);
+  return df_fast(s.h, __fadd_rn(s.l, __fsub_rn(bl, al)));
+}
+
+constexpr int PREDDF = 4;   // float4 per particle
+constexpr int IRRDF_U = 2;  // listings per lane in flight
+
+__device__ __forceinline__ void split_state_df(const double x[3], const double v[3], double m,
+                                               float4 s[PREDDF]) {
+  float xh[3], xl[3], vh[3], vl[3], mh, ml;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    ds_split(x[c], xh[c], xl[c]);
+    ds_split(v[c], vh[c], vl[c]);
+  }
+  ds_split(m, mh, ml);
+  s[0] = make_float4(xh[0], xh[1], xh[2], mh);
+  s[1] = make_float4(xl[0], xl[1], xl[2], ml);
+  s[2] = make_float4(vh[0], vh[1], vh[2], 0.f);
+  s[3] = make_float4(vl[0], vl[1], vl[2], 0.f);
+}
+
+__global__ void irr_preddf_kernel(int n, const double *__restrict__ rec, double ti,
+                                  float4 *__restrict__ pred) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[3], v[3], m;
+  predict(rec + (size_t)i * REC, ti, x, v, m);
+  float4 s[PREDDF];
+  split_state_df(x, v, m, s);
+#pragma unroll
+  for (int u = 0; u < PREDDF; ++u) pred[(size_t)i * PREDDF + u] = s[u];
+}
+
+template <bool PRE>
+__device__ __forceinline__ void statedf(const double *__restrict__ rec,
+                                        const float4 *__restrict__ pred, int i, double ti,
+                                        float4 s[PREDDF]) {
+  if (PRE) {
+#pragma unroll
+    for (int u = 0; u < PREDDF; ++u) s[u] = __ldg(pred + (size_t)i * PREDDF + u);
+  } else {
+    double x[3], v[3], m;
+    predict(rec + (size_t)i * REC, ti, x, v, m);
+    split_state_df(x, v, m, s);
+  }
+}
+
+// Same contract as irr_firr_kernel.  Bodies closer than 1e-19 (r^2 below the
+// smallest normal float), the particle itself included, add nothing; the
+// nearest neighbour is chosen on the double-float r^2 (ties to the smaller
+// id).
+template <bool PRE, int G>
+__global__ void __launch_bounds__(32 * IRR32_WARPS)
+    irr_firrdf_kernel(int n, const double *__restrict__ rec, const float4 *__restrict__ pred,
+                      int lmax, const int *__restrict__ lists, double ti, int ni,
+                      const int *__restrict__ addr, int base, double *__restrict__ acc,
+                      double *__restrict__ jrk, int *__restrict__ nnbid, int *__restrict__ err,
+                      unsigned long long *__restrict__ inter) {
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  for (int k0 = warp * (32 / G); k0 < ni; k0 += nwarps * (32 / G)) {
+    const int k = k0 + lane / G;
+    dfl sum[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sum[c] = {0.f, 0.f};
+    dfl best = {INFINITY, 0.f};
+    int bj = INT_MAX;
+    const int i = k < ni ? addr[k] - base : 0;
+    if (k < ni && (i < 0 || i >= n)) {
+      if (sub == 0) flag(err, GPUNB_E_ARG);
+    } else if (k < ni) {
+      float4 si[PREDDF];
+      statedf<PRE>(rec, pred, i, ti, si);
+      const int *row = lists + (size_t)i * lmax;
+      int nnb = row[0];
+      if (nnb < 0 || nnb > lmax - 1) {
+        if (sub == 0) flag(err, GPUNB_E_ARG);
+        nnb = 0;
+      }
+      if (inter && sub == 0 && nnb > 0) atomicAdd(inter, (unsigned long long)nnb);
+      for (int q0 = sub; q0 < nnb; q0 += IRRDF_U * G) {
+        int jv[IRRDF_U];
+#pragma unroll
+        for (int u = 0; u < IRRDF_U; ++u) {
+          const int q = q0 + u * G;
+          jv[u] = q < nnb ? __ldg(row + 1 + q) : -1;
+          if (q < nnb && (jv[u] < 0 || jv[u] >= n)) {
+            flag(err, GPUNB_E_ARG);
+            jv[u] = -1;
+          }
+        }
+        float4 sj[IRRDF_U][PREDDF];
+#pragma unroll
+        for (int u = 0; u < IRRDF_U; ++u) {
+          if (jv[u] >= 0) {
+            statedf<PRE>(rec, pred, jv[u], ti, sj[u]);
+          } else {
+#pragma unroll
+            for (int w = 0; w < PREDDF; ++w) sj[u][w] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < IRRDF_U; ++u) {
+          if (jv[u] < 0) continue;
+          const int j = jv[u];
+          const dfl dx = df_diff(sj[u][0].x, sj[u][1].x, si[0].x, si[1].x);
+          const dfl dy = df_diff(sj[u][0].y, sj[u][1].y, si[0].y, si[1].y);
+          const dfl dz = df_diff(sj[u][0].z, sj[u][1].z, si[0].z, si[1].z);
+          const dfl r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+          if (r2.h < best.h || (r2.h == best.h && (r2.l < best.l || (r2.l == best.l && j < bj)))) {
+            best = r2;
+            bj = j;
+          }
+          if (r2.h < 0x1p-126f) continue;
+          const dfl dvx = df_diff(sj[u][2].x, sj[u][3].x, si[2].x, si[3].x);
+          const dfl dvy = df_diff(sj[u][2].y, sj[u][3].y, si[2].y, si[3].y);
+          const dfl dvz = df_diff(sj[u][2].z, sj[u][3].z, si[2].z, si[3].z);
+          // 1/r: estimate y0, then y0 (1 + (1 - r2 y0^2) / 2) with r2 y0^2 in double-float
+          const float y0 = rsqrt_est(r2.h);
+          const float q = __fmul_rn(y0, y0);
+          const dfl t = df_mul(r2, {q, fmaf(y0, y0, -q)});
+          const float e = __fsub_rn(__fsub_rn(1.0f, t.h), t.l);
+          const dfl rinv = df_fast(y0, __fmul_rn(__fmul_rn(0.5f, y0), e));
+          const dfl rinv2 = df_sqr(rinv);
+          const dfl mr3 = df_mul(df_mul({sj[u][0].w, sj[u][1].w}, rinv), rinv2);
+          const dfl rv = df_add(df_add(df_mul(dx, dvx), df_mul(dy, dvy)), df_mul(dz, dvz));
+          const dfl al = df_mulf(df_mul(rv, rinv2), -3.0f);
+          sum[0] = df_add(sum[0], df_mul(mr3, dx));
+          sum[1] = df_add(sum[1], df_mul(mr3, dy));
+          sum[2] = df_add(sum[2], df_mul(mr3, dz));
+          sum[3] = df_add(sum[3], df_mul(mr3, df_add(dvx, df_mul(al, dx))));
+          sum[4] = df_add(sum[4], df_mul(mr3, df_add(dvy, df_mul(al, dy))));
+          sum[5] = df_add(sum[5], df_mul(mr3, df_add(dvz, df_mul(al, dz))));
+        }
+      }
+    }
+    // fixed double-float butterfly within the particle's lanes (deterministic)
+    for (int o = G / 2; o > 0; o >>= 1) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const dfl other = {__shfl_xor_sync(0xffffffffu, sum[c].h, o),
+                           __shfl_xor_sync(0xffffffffu, sum[c].l, o)};
+        sum[c] = df_add(sum[c], other);
+      }
+      const float obh = __shfl_xor_sync(0xffffffffu, best.h, o);
+      const float obl = __shfl_xor_sync(0xffffffffu, best.l, o);
+      const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+      if (obh < best.h || (obh == best.h && (obl < best.l || (obl == best.l && oj < bj)))) {
+        best = {obh, obl};
+        bj = oj;
+      }
+    }
+    // lane c < 6 converts and stores component c, lane 6 the nearest neighbour
+    if (k < ni) {
+      dfl v = sum[0];
+#pragma unroll
+      for (int c = 1; c < 6; ++c)
+        if (sub == c) v = sum[c];
+      if (sub < 3) acc[3 * (size_t)k + sub] = (double)v.h + (double)v.l;
+      else if (sub < 6) jrk[3 * (size_t)k + sub - 3] = (double)v.h + (double)v.l;
+      else if (sub == 6) nnbid[k] = (bj == INT_MAX) ? 0 : bj + 1;
+    }
+  }
+}
+
 // changed records: rec[idx[r]] = src record r (thread per double)
 __global__ void irr_put_rec_kernel(int k, const int *__restrict__ idx,
                                    const double *__restrict__ src, int src_by_index,
@@ -501,7 +715,7 @@ struct State {
   bool open = false;
   int nmax = 0, lmax = 0, rank = 0;
   int direct = 0;                // device reads/writes host memory coherently
-  int precision = 1;             // 1 = FP64 (default), 0 = split FP32
+  int precision = 2;             // 2 = double-float (default), 1 = FP64, 0 = split FP32
   cudaStream_t st = nullptr;
   std::vector<double> rec_h;     // host mirror of the records
   std::vector<int> list_h;       // host mirror of the rows (0-based ids)
@@ -674,7 +888,7 @@ static bool upload() {
 }
 
 // pred: scratch of n * PRED doubles (64 bytes per particle, which also holds
-// the 48-byte split states).  Blocks of at least n/32 particles predict every
+// the 48-byte split and 64-byte double-float states).  Blocks of at least n/32 particles predict every
 // particle once first (with ~100 neighbours each, the lists then name every
 // particle several times); smaller ones predict per listing.  prec: 0 = split
 // FP32, 1 = FP64.
@@ -705,6 +919,24 @@ static int launch_firr(int n, const double *rec, double *pred, int prec, int lma
     else
       irr_firr_kernel<false, IRR_G><<<blocks, th, 0, st>>>(n, rec, p, lmax, lists, ti, ni, addr,
                                                             base, acc, jrk, nnbid, err, inter);
+  } else if (prec == 2) {
+    float4 *pdf = whole ? reinterpret_cast<float4 *>(pred) : nullptr;
+    if (whole) irr_preddf_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, rec, ti, pdf);
+    if (whole && wide)
+      irr_firrdf_kernel<true, 32><<<blocks, th, 0, st>>>(n, rec, pdf, lmax, lists, ti, ni, addr,
+                                                          base, acc, jrk, nnbid, err, inter);
+    else if (whole)
+      irr_firrdf_kernel<true, IRR_G><<<blocks, th, 0, st>>>(n, rec, pdf, lmax, lists, ti, ni,
+                                                             addr, base, acc, jrk, nnbid, err,
+                                                             inter);
+    else if (wide)
+      irr_firrdf_kernel<false, 32><<<blocks, th, 0, st>>>(n, rec, pdf, lmax, lists, ti, ni,
+                                                           addr, base, acc, jrk, nnbid, err,
+                                                           inter);
+    else
+      irr_firrdf_kernel<false, IRR_G><<<blocks, th, 0, st>>>(n, rec, pdf, lmax, lists, ti, ni,
+                                                              addr, base, acc, jrk, nnbid, err,
+                                                              inter);
   } else {
     float4 *p32 = whole ? reinterpret_cast<float4 *>(pred) : nullptr;
     if (whole) irr_pred32_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, rec, ti, p32);
@@ -756,7 +988,10 @@ static void open_lib(int nmax, int lmax, int rank) {
   }
   S.direct = (pageable && host_tables) ? 1 : 0;
   if (const char *p = getenv("GPUNB_HOST_DIRECT")) S.direct &= (atoi(p) != 0);
-  if (const char *p = getenv("GPUNB_IRR_PRECISION")) S.precision = atoi(p) == 0 ? 0 : 1;
+  if (const char *p = getenv("GPUNB_IRR_PRECISION")) {
+    const int v = atoi(p);
+    S.precision = (v == 0 || v == 1) ? v : 2;
+  }
   const size_t n = (size_t)std::max(nmax, 1);
   S.nmax = nmax;
   S.lmax = lmax;
@@ -1038,7 +1273,7 @@ int irr_firr_device(int n, const double *rec, int lmax, const int *lists, double
 
 int irr_set_precision(int mode) {
   std::lock_guard<std::mutex> lk(S.mu);
-  S.precision = mode == 0 ? 0 : 1;
+  S.precision = (mode == 0 || mode == 1) ? mode : 2;
   return S.precision;
 }
 

@@ -69,7 +69,7 @@ class IrrSimd:
         return self.lib.irr_set_host_path(1 if direct else 0)
 
     def set_precision(self, mode: int) -> int:
-        """irr_set_precision: 1 = FP64 (the default), 0 = split FP32."""
+        """irr_set_precision: 2 = double-float (the default), 1 = FP64, 0 = split FP32."""
         return self.lib.irr_set_precision(int(mode))
 
     def set_jp(self, x0, v0, f, fdot, m, t0, idx=None) -> None:
