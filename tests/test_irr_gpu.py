@@ -1,8 +1,8 @@
 """GPU irregular force (include/irr.h, drop-in for src/Main/irr.avx.cpp)
 through its Fortran-style C ABI in its FP64 mode (irr_set_precision(1)),
 against the FP64 oracle and the golden vectors of the reference's own
-irr.avx.cpp.  The split-precision default is tested in
-test_irr_split_gpu.py.
+irr.avx.cpp.  The double-float default is tested in test_irr_df_gpu.py,
+the split-FP32 mode in test_irr_split_gpu.py.
 
 Tolerances: in FP64 mode, against the FP64 oracle the force and its
 derivative agree to 1e-10 relative (the two differ only in fused
