@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(32 * IRR_WARPS)
 // exact arithmetic after the FP32 inputs would still leave 1.1e-6 of
 // max(|Q_i|, S_i / 8) in the derivative: only double-single differences and
 // velocities with float-float arithmetic throughout would reach the regular
-// force's 1e-6 bound, so that accuracy is the FP64 mode's.
+// force's 1e-6 bound: that is the double-float mode below.
 constexpr int PRED32 = 3;   // float4 per particle
 
 __device__ __forceinline__ void split_state(const double x[3], const double v[3], double m,

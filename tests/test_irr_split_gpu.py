@@ -10,8 +10,8 @@ relative at the 99th percentile, and per particle within IRR_BOUND = 5e-6 of
 max(|Q_i|, S_i / 8), S_i the sum of the pair terms' magnitudes
 (oracle.irr_abs_sums).  The regular force's bound is 1e-6: an irregular
 force sums a few dominant terms whose FP32 roundings do not average out the
-way a regular force's thousands do; that accuracy is the FP64 mode's (the
-default).  Against the golden vectors of the reference's library: within
+way a regular force's thousands do; that accuracy is the double-float (the
+default) and FP64 modes'.  Against the golden vectors of the reference's library: within
 its error.  The nearest neighbour is the FP64
 oracle's, except where the two nearest listed bodies lie within 1e-6 of each
 other in r^2 (the choice is made on the FP32 r^2)."""
