@@ -30,7 +30,12 @@
  * Deliberate differences: no 600-entry list cap (lmax up to 2^16 per row);
  * a listed body at zero distance (the particle itself) adds nothing instead
  * of a NaN (in the double-float and split modes: any body closer than
- * 1e-19); invalid addresses or ids are reported as GPUNB_E_ARG.
+ * 1e-19); invalid addresses or ids are reported as GPUNB_E_ARG.  The
+ * double-float and split modes hold each term m/r^3 (dv - ...) in the FP32
+ * exponent range, below ~3e38: enough for every unregularised pair of an
+ * N-body run in its own units (with m ~ 1/N and r >= 1e-10, m/r^3 < 1e30),
+ * while pairs closer still, which the integrator regularises, need the FP64
+ * mode.
  *
  * set_jp / set_list are safe to call concurrently for different particles
  * (the Fortran callers run them inside OpenMP loops); they only update host
