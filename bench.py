@@ -12,6 +12,7 @@ per second, in Gpairs/s.
   e2e    the same step through the C ABI with host arrays (gpunb_send_,
          gpunb_regf_), host<->device copies included, wall clock;
   fp64   the plain FP64 kernel on the same step (the metric's "vs FP64").
+  double_float  the same step in double-float arithmetic on the FP32 pipe.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -926,6 +927,21 @@ def main():
                          "jrk_p99": float(np.percentile(ej, 99)), "jrk_max": float(ej.max()),
                          "pot_max": float(ep.max())}
     fp64_big = np.asarray(fp64_kt).reshape(-1, len(BLOCKS))[:, BLOCKS.index(65536)]
+    # the same step in double-float arithmetic (gpunb_set_precision(2)), against the FP64 kernel
+    res_fp64 = {ni: (blk[ni]["acc"].cpu().numpy().copy(), blk[ni]["jrk"].cpu().numpy().copy(),
+                     blk[ni]["pot"].cpu().numpy().copy()) for ni in (1024, 16384)}
+    df_ms, df_kt = timed_steps(1, "double_float")
+    df_value = ws * pairs_per_step / (float(np.mean(df_ms)) * 1e-3) / 1e9
+    df_big = np.asarray(df_kt).reshape(-1, len(BLOCKS))[:, BLOCKS.index(65536)]
+    df_errs = {}
+    for ni in (1024, 16384):
+        a64, j64, p64 = res_fp64[ni]
+        a = blk[ni]["acc"].cpu().numpy(); j = blk[ni]["jrk"].cpu().numpy()
+        p = blk[ni]["pot"].cpu().numpy()
+        df_errs[str(ni)] = {
+            "acc_max": float((np.linalg.norm(a - a64, axis=1) / np.linalg.norm(a64, axis=1)).max()),
+            "jrk_max": float((np.linalg.norm(j - j64, axis=1) / np.linalg.norm(j64, axis=1)).max()),
+            "pot_max": float((np.abs(p - p64) / np.abs(p64)).max())}
 
     # ---- end to end through the C ABI with host arrays --------------------
     nb.set_precision("split")
@@ -1018,6 +1034,12 @@ def main():
                  "frac_fp64_peak": pairs_big * FLOPS_PER_PAIR /
                      (float(np.mean(fp64_big)) * 1e-3) / 1e12 / fp64_peak_tflops(n_sm, peak_mhz)},
         "rel_err_vs_fp64_kernel": errs,
+        "double_float": {"value": df_value, "unit": "Gpairs/s",
+                         "kernel_ms_ni65536": float(np.mean(df_big)),
+                         "speedup_over_fp64_kernel": float(np.mean(fp64_big)) / float(np.mean(df_big)),
+                         "max_rel_err_vs_fp64_kernel": df_errs,
+                         "note": "gpunb_set_precision(2): every pair in double-float arithmetic "
+                                 "on the FP32 pipe"},
         "pair_kernel_per_block": per_block,
         "launch_plan_per_block": {str(ni): {"variant": v, "splits": sp_}
                                   for ni, (v, sp_) in plan_split.items()},

@@ -85,7 +85,10 @@ void gpunb_set_abort_on_error(int flag);    /* 1 (default): print + abort() */
 
 /* Pair kernel selection: 0 = split precision (FP32 arithmetic on double-single
  * positions, float-float merges and FP64 neighbour re-tests; default),
- * 1 = plain FP64. */
+ * 1 = plain FP64, 2 = double-float (every pair in hi + lo pairs of floats on
+ * the FP32 pipe: FP64-class results, within ~1e-11 of FP64, several times
+ * faster than FP64 on GB300; lists identical to FP64).  The batched entry
+ * points always use the split kernel. */
 void gpunb_set_precision(int mode);
 
 /* Force a launch shape (variant index, j-splits; for the batched entry

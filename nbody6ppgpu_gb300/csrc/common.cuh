@@ -66,6 +66,51 @@ __device__ __forceinline__ void ff_add(float &hi, float &lo, float bhi, float bl
 }
 
 // ---------------------------------------------------------------------------
+// Double-float arithmetic: a value is the unevaluated sum hi + lo of two
+// floats (about 48 significant bits); each operation is an error-free
+// transform (Knuth's TwoSum, the FMA product error) followed by
+// renormalisation -- the double-single arithmetic of Dekker (1971).  On a
+// part whose FP64 pipe runs at 1/64 of the FP32 rate it gives FP64-class
+// results several times faster than FP64 itself.
+struct dfl {
+  float h, l;
+};
+__device__ __forceinline__ dfl df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ dfl df_fast(float a, float b) {   // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+  const dfl s = df_two_sum(a.h, b.h);
+  return df_fast(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return df_fast(p, e);
+}
+__device__ __forceinline__ dfl df_mulf(dfl a, float b) {
+  const float p = __fmul_rn(a.h, b);
+  return df_fast(p, fmaf(a.l, b, fmaf(a.h, b, -p)));
+}
+__device__ __forceinline__ dfl df_sqr(dfl a) {
+  const float p = __fmul_rn(a.h, a.h);
+  return df_fast(p, fmaf(__fmul_rn(2.0f, a.h), a.l, fmaf(a.h, a.h, -p)));
+}
+// difference of two double-single values b - a
+__device__ __forceinline__ dfl df_diff(float bh, float bl, float ah, float al) {
+  const dfl s = df_two_sum(bh, -ah);
+  return df_fast(s.h, __fadd_rn(s.l, __fsub_rn(bl, al)));
+}
+
+// ---------------------------------------------------------------------------
 // Bulk-async global->shared copies completing on an mbarrier (TMA engine).
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);

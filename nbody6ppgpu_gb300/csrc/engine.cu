@@ -548,7 +548,7 @@ static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, in
   const int ni = is.ni;
   RegfOut out;
   int gx;
-  if (g.precision == 1) {
+  if (g.precision != 0) {
     gx = (ni + FP64_THREADS - 1) / FP64_THREADS;
     out.ni_pad = gx * FP64_THREADS;
   } else {
@@ -595,6 +595,8 @@ static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, in
   if (timed || pooled) CUDA_OR(cudaEventRecord(e0, st), GPUNB_E_CUDA);
   if (g.precision == 1) {
     CUDA_OR(launch_regf_fp64(mflag, gx, S, js, is, out, st), GPUNB_E_CUDA);
+  } else if (g.precision == 2) {
+    CUDA_OR(launch_regf_df(mflag, gx, S, js, is, out, st), GPUNB_E_CUDA);
   } else {
     const long long items = (long long)gx * S;
     const long long resident = (long long)g.n_sm * regf_ds_blocks_per_sm(variant, mflag);
@@ -603,7 +605,7 @@ static int run_pair_pass(const ISet &is, int nnbmax, bool mflag, int variant, in
             GPUNB_E_CUDA);
   }
   if (timed || pooled) CUDA_OR(cudaEventRecord(e1, st), GPUNB_E_CUDA);
-  g.last_variant = g.precision == 1 ? -1 : variant;
+  g.last_variant = g.precision != 0 ? -1 : variant;
   g.last_splits = S;
   g.last_gx = gx;
   return GPUNB_OK;
@@ -626,7 +628,7 @@ static int finish_lists(int ni, int nnbmax, int S, int ni_pad, const int *perm, 
 
 static void choose_plan(int ni, bool mflag, int &variant, int &S) {
   const JSet js = jset();
-  if (g.precision == 1) {
+  if (g.precision != 0) {
     int gx;
     fp64_plan(ni, js.ntile64, gx, S);
     variant = -1;
@@ -768,7 +770,7 @@ static void regf_host_direct(int ni, const double *h2, const double *dtr, const 
     o.dense = g.dense.as<int>();
     int rc = run_pair_pass(is, nnbmax, mflag, variant, S, s, false, &o);
     if (rc != GPUNB_OK) return rc;
-    const int itile = g.precision == 1 ? FP64_THREADS : regf_variant(variant).itile();
+    const int itile = g.precision != 0 ? FP64_THREADS : regf_variant(variant).itile();
     const int ni_pad = ((ni + itile - 1) / itile) * itile;
     rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, 0, s, g.last_fused);
     if (rc != GPUNB_OK) return rc;
@@ -882,7 +884,7 @@ static void regf_host(int ni, const double *h2, const double *dtr, const double 
   o.btot = g.btot.as<int>();
   o.dense = g.dense.as<int>();
   if (run_pair_pass(is, nnbmax, mflag, variant, S, st, false, &o) != GPUNB_OK) return;
-  const int ni_pad = g.precision == 1
+  const int ni_pad = g.precision != 0
                          ? ((ni + FP64_THREADS - 1) / FP64_THREADS) * FP64_THREADS
                          : ((ni + regf_variant(variant).itile() - 1) / regf_variant(variant).itile()) *
                                regf_variant(variant).itile();
@@ -1218,7 +1220,7 @@ void gpunb_clear_error(void) {
 }
 void gpunb_set_abort_on_error(int flag) { g_abort_on_error = flag; }
 
-void gpunb_set_precision(int mode) { g.precision = mode == 1 ? 1 : 0; }
+void gpunb_set_precision(int mode) { g.precision = (mode == 1 || mode == 2) ? mode : 0; }
 
 void gpunb_set_launch(int variant, int splits) {
   g.force_variant = variant;
@@ -1469,7 +1471,7 @@ int gpunb_regf_device(int ni, const double *h2, const double *dtr, const double 
     o.rowlen = g.rowlen.as<int>(); o.off = list_off; o.btot = g.btot.as<int>(); o.dense = list;
     int rc = run_pair_pass(is, nnbmax, mflag, variant, S, s, false, &o);
     if (rc != GPUNB_OK) return rc;
-    const int itile = g.precision == 1 ? FP64_THREADS : regf_variant(variant).itile();
+    const int itile = g.precision != 0 ? FP64_THREADS : regf_variant(variant).itile();
     const int ni_pad = ((ni + itile - 1) / itile) * itile;
     rc = finish_lists(ni, nnbmax, S, ni_pad, is.perm, o, list_cap, s, g.last_fused);
     if (rc != GPUNB_OK) return rc;

@@ -411,51 +411,13 @@ __global__ void __launch_bounds__(32 * IRR32_WARPS)
 // FP32 pipe.  Every quantity is an unevaluated sum hi + lo of two floats
 // (about 48 significant bits) and every operation an error-free transform
 // (Knuth's TwoSum, the FMA product error) followed by renormalisation, the
-// classic double-single arithmetic of Dekker (1971), so that a pair costs
-// ~300 FP32 operations instead of ~40 FP64 ones: on GB300, whose FP64 pipe
-// runs at 1/64 of the FP32 rate, that is several times faster, at a relative
-// error near 1e-13 per term.  Positions, velocities and masses are the
+// classic double-single arithmetic of Dekker (1971; df_* in common.cuh), so
+// that a pair costs ~530 instructions on the FP32 pipe instead of ~40 on the
+// FP64 pipe: on GB300, whose FP64 pipe runs at 1/64 of the FP32 rate, 4.2x
+// faster, at a relative error near 1e-13 per term.  Positions, velocities and masses are the
 // double-single split of the FP64 prediction (4 float4 = 64 bytes per
 // particle, two sectors when gathered); 1/r is the hardware estimate refined
 // by one Newton step carried in double-float (error ~2^-45).
-struct dfl {
-  float h, l;
-};
-__device__ __forceinline__ dfl df_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return {s, e};
-}
-__device__ __forceinline__ dfl df_fast(float a, float b) {   // |a| >= |b| or a == 0
-  const float s = __fadd_rn(a, b);
-  return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
-  const dfl s = df_two_sum(a.h, b.h);
-  return df_fast(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
-}
-__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
-  const float p = __fmul_rn(a.h, b.h);
-  float e = fmaf(a.h, b.h, -p);
-  e = fmaf(a.h, b.l, e);
-  e = fmaf(a.l, b.h, e);
-  return df_fast(p, e);
-}
-__device__ __forceinline__ dfl df_mulf(dfl a, float b) {
-  const float p = __fmul_rn(a.h, b);
-  return df_fast(p, fmaf(a.l, b, fmaf(a.h, b, -p)));
-}
-__device__ __forceinline__ dfl df_sqr(dfl a) {
-  const float p = __fmul_rn(a.h, a.h);
-  return df_fast(p, fmaf(__fmul_rn(2.0f, a.h), a.l, fmaf(a.h, a.h, -p)));
-}
-// difference of two double-single values b - a
-__device__ __forceinline__ dfl df_diff(float bh, float bl, float ah, float al) {
-  const dfl s = df_two_sum(bh, -ah);
-  return df_fast(s.h, __fadd_rn(s.l, __fsub_rn(bl, al)));
-}
-
 constexpr int PREDDF = 4;   // float4 per particle
 constexpr int IRRDF_U = 2;  // listings per lane in flight
 

@@ -32,6 +32,9 @@ cudaError_t launch_regf_ds(int v, bool mflag, int n_itiles, int S, int grid, int
                            int n_items = 0);
 cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const ISet &is,
                              const RegfOut &out, cudaStream_t st);
+// the same call shape in double-float arithmetic (gpunb_set_precision(2))
+cudaError_t launch_regf_df(bool mflag, int gx, int S, const JSet &js, const ISet &is,
+                             const RegfOut &out, cudaStream_t st);
 constexpr int FP64_THREADS = 128;
 // ff: the partials are float-float pairs (split kernel), else doubles (FP64 kernel)
 cudaError_t launch_regf_merge(const double *part, bool ff, int S, int ni, int ni_pad,

@@ -997,6 +997,115 @@ __global__ void __launch_bounds__(128) regf_fp64_kernel(const JSet js, const ISe
   }
 }
 
+// Double-float pair kernel (gpunb_set_precision(2)): the FP64 kernel's
+// structure and semantics with every pair computed in double-float
+// arithmetic on the FP32 pipe (df_* in common.cuh): FP64-class results --
+// force, jerk and potential within ~1e-11 of FP64 -- several times faster
+// than FP64 on GB300.  The j tile is split into double-single positions,
+// velocities and masses once per tile in shared memory; the neighbour
+// decision compares the double-float min(r^2, r_p^2) with the criterion and
+// re-takes it in the oracle's FP64 expression order (nb_test_fp64) whenever
+// the two lie within 2^-40 of each other, so that the lists are the FP64
+// oracle's exactly.
+template <bool MFLAG>
+__global__ void __launch_bounds__(128) regf_df_kernel(const JSet js, const ISet is,
+                                                      const RegfOut out) {
+  constexpr int NT = 128;
+  __shared__ float sxh[JT64 * 3], sxl[JT64 * 3], svh[JT64 * 3], svl[JT64 * 3];
+  __shared__ float smh[JT64], sml[JT64];
+  const int tid = threadIdx.x;
+  const int i = blockIdx.x * NT + tid;
+  const bool valid = i < is.ni;
+  const int ns = gridDim.y, sy = blockIdx.y;
+  const int t0 = (int)(((long long)js.ntile64 * sy) / ns);
+  const int t1 = (int)(((long long)js.ntile64 * (sy + 1)) / ns);
+  float xh[3] = {0.f, 0.f, 0.f}, xl[3] = {0.f, 0.f, 0.f};
+  float vh[3] = {0.f, 0.f, 0.f}, vl[3] = {0.f, 0.f, 0.f};
+  dfl h2 = {-1.f, 0.f}, dtr = {0.f, 0.f};
+  if (valid) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      ds_split(is.x[3 * i + c], xh[c], xl[c]);
+      ds_split(is.v[3 * i + c], vh[c], vl[c]);
+    }
+    const double h2d = is.h2[i], dtrd = is.dtr[i];
+    ds_split(h2d, h2.h, h2.l);
+    ds_split(dtrd, dtr.h, dtr.l);
+    if (sy == 0 && (isnan(is.x[3 * i]) || isnan(is.x[3 * i + 1]) || isnan(is.x[3 * i + 2]) ||
+                    isnan(is.v[3 * i]) || isnan(is.v[3 * i + 1]) || isnan(is.v[3 * i + 2]) ||
+                    isnan(h2d) || isnan(dtrd)))
+      raise_error(out.err, GPUNB_E_NAN);
+  }
+  dfl q[NQ];
+#pragma unroll
+  for (int c = 0; c < NQ; ++c) q[c] = {0.f, 0.f};
+  for (int t = t0; t < t1; ++t) {
+    const int jb = t * JT64;
+    const int n = min(JT64, js.nj - jb);
+    __syncthreads();
+    for (int u = tid; u < 3 * n; u += NT) {
+      ds_split(js.x64[3 * (size_t)jb + u], sxh[u], sxl[u]);
+      ds_split(js.v64[3 * (size_t)jb + u], svh[u], svl[u]);
+    }
+    for (int u = tid; u < n; u += NT) ds_split(js.m64[jb + u], smh[u], sml[u]);
+    __syncthreads();
+    if (!valid) continue;
+    for (int jj = 0; jj < n; ++jj) {
+      const dfl dx = df_diff(sxh[3 * jj], sxl[3 * jj], xh[0], xl[0]);
+      const dfl dy = df_diff(sxh[3 * jj + 1], sxl[3 * jj + 1], xh[1], xl[1]);
+      const dfl dz = df_diff(sxh[3 * jj + 2], sxl[3 * jj + 2], xh[2], xl[2]);
+      const dfl dvx = df_diff(svh[3 * jj], svl[3 * jj], vh[0], vl[0]);
+      const dfl dvy = df_diff(svh[3 * jj + 1], svl[3 * jj + 1], vh[1], vl[1]);
+      const dfl dvz = df_diff(svh[3 * jj + 2], svl[3 * jj + 2], vh[2], vl[2]);
+      const dfl r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+      const dfl px = df_add(dx, df_mul(dvx, dtr));
+      const dfl py = df_add(dy, df_mul(dvy, dtr));
+      const dfl pz = df_add(dz, df_mul(dvz, dtr));
+      const dfl r2p = df_add(df_add(df_sqr(px), df_sqr(py)), df_sqr(pz));
+      const bool pless = r2p.h < r2.h || (r2p.h == r2.h && r2p.l < r2.l);
+      const dfl r2min = pless ? r2p : r2;
+      const dfl m = {smh[jj], sml[jj]};
+      const dfl crit = MFLAG ? df_mul(m, h2) : h2;
+      const dfl diff = df_add(r2min, {-crit.h, -crit.l});
+      bool in;
+      if (fabsf(diff.h) <= 0x1p-40f * fabsf(crit.h))
+        in = nb_test_fp64(is, i, js, jb + jj, MFLAG);   // the oracle's own decision
+      else
+        in = diff.h < 0.f;
+      if (in) {
+        record_neighbour(out, i, jb + jj);
+        continue;
+      }
+      if (r2.h < 0x1p-126f) continue;   // a body closer than 1e-19 that is no neighbour
+      // 1/r: estimate y0, then y0 (1 + (1 - r2 y0^2) / 2) with r2 y0^2 in double-float
+      const float y0 = rsqrt_est(r2.h);
+      const float y2 = __fmul_rn(y0, y0);
+      const dfl tq = df_mul(r2, {y2, fmaf(y0, y0, -y2)});
+      const float e = __fsub_rn(__fsub_rn(1.0f, tq.h), tq.l);
+      const dfl rinv = df_fast(y0, __fmul_rn(__fmul_rn(0.5f, y0), e));
+      const dfl rinv2 = df_sqr(rinv);
+      const dfl mr = df_mul(m, rinv);                     // m/r
+      const dfl mr3 = df_mul(mr, rinv2);                  // m/r^3
+      const dfl rv = df_add(df_add(df_mul(dx, dvx), df_mul(dy, dvy)), df_mul(dz, dvz));
+      const dfl al = df_mulf(df_mul(rv, rinv2), -3.0f);  // -3 (r.v)/r^2
+      q[0] = df_add(q[0], df_mul(mr3, dx));
+      q[1] = df_add(q[1], df_mul(mr3, dy));
+      q[2] = df_add(q[2], df_mul(mr3, dz));
+      q[3] = df_add(q[3], df_mul(mr3, df_add(dvx, df_mul(al, dx))));
+      q[4] = df_add(q[4], df_mul(mr3, df_add(dvy, df_mul(al, dy))));
+      q[5] = df_add(q[5], df_mul(mr3, df_add(dvz, df_mul(al, dz))));
+      q[6] = df_add(q[6], mr);
+    }
+  }
+  if (valid) {
+    // the FP64 kernel's partial layout (4x acc and jrk, as the split kernel)
+    double *p = out.part + (size_t)sy * NQ * out.ni_pad + i;
+#pragma unroll
+    for (int c = 0; c < NQ; ++c)
+      p[c * out.ni_pad] = (c < 6 ? 4.0 : 1.0) * ((double)q[c].h + (double)q[c].l);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Merge of the S j-split partials, fixed order s = 0..S-1 (the
 // deterministic replacement of force_reduce_kernel + the host sum over GPUs,
@@ -1474,6 +1583,15 @@ cudaError_t launch_regf_fp64(bool mflag, int gx, int S, const JSet &js, const IS
     regf_fp64_kernel<true><<<dim3(gx, S), FP64_THREADS, 0, st>>>(js, is, out);
   else
     regf_fp64_kernel<false><<<dim3(gx, S), FP64_THREADS, 0, st>>>(js, is, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_regf_df(bool mflag, int gx, int S, const JSet &js, const ISet &is,
+                           const RegfOut &out, cudaStream_t st) {
+  if (mflag)
+    regf_df_kernel<true><<<dim3(gx, S), FP64_THREADS, 0, st>>>(js, is, out);
+  else
+    regf_df_kernel<false><<<dim3(gx, S), FP64_THREADS, 0, st>>>(js, is, out);
   return cudaGetLastError();
 }
 

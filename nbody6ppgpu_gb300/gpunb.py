@@ -176,7 +176,7 @@ class GpuNb:
 
     # -- configuration -----------------------------------------------------
     def set_precision(self, mode: str) -> None:
-        self.lib.gpunb_set_precision({"split": 0, "fp64": 1}[mode])
+        self.lib.gpunb_set_precision({"split": 0, "fp64": 1, "double_float": 2}[mode])
 
     def set_launch(self, variant: int = -1, splits: int = 0) -> None:
         self.lib.gpunb_set_launch(int(variant), int(splits))

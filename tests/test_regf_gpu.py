@@ -22,6 +22,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
+DF_TOL = 1e-10   # the double-float kernel against the FP64 oracle, every particle
 
 
 @pytest.fixture(scope="module")
@@ -48,7 +49,7 @@ def run_golden(g, precision="split", variant=-1, splits=0):
 
 @pytest.mark.parametrize("name", ["plummer2048_equal", "mflag_plummer512",
                                   "overflow_plummer512", "ragged_n37"])
-@pytest.mark.parametrize("precision", ["split", "fp64"])
+@pytest.mark.parametrize("precision", ["split", "fp64", "double_float"])
 def test_golden_cases(lib, name, precision):
     g = load_golden(name)
     res = run_golden(g, precision)
@@ -61,8 +62,13 @@ def test_golden_cases(lib, name, precision):
                      g["fp64_jrkabs"])
     else:
         ok = res.list[:, 0] >= 0
-        np.testing.assert_allclose(res.acc[ok], g["fp64_acc"][ok], rtol=FP64_TOL, atol=1e-14)
-        np.testing.assert_allclose(res.pot[ok], g["fp64_pot"][ok], rtol=FP64_TOL)
+        if precision == "fp64":
+            np.testing.assert_allclose(res.acc[ok], g["fp64_acc"][ok], rtol=FP64_TOL, atol=1e-14)
+            np.testing.assert_allclose(res.pot[ok], g["fp64_pot"][ok], rtol=FP64_TOL)
+        else:   # double-float: every particle's vectors and potential
+            assert rel_vec_err(res.acc[ok], g["fp64_acc"][ok]).max() < DF_TOL
+            assert rel_vec_err(res.jrk[ok], g["fp64_jrk"][ok]).max() < DF_TOL
+            np.testing.assert_allclose(res.pot[ok], g["fp64_pot"][ok], rtol=DF_TOL)
 
 
 def test_all_launch_shapes_agree_and_are_deterministic(lib):
@@ -216,6 +222,31 @@ def test_fp64_kernel_matches_oracle(lib, plummer64k):
     assert rows_equal(res.list, lst) == []
     assert rel_vec_err(res.acc, acc).max() < FP64_TOL
     assert rel_vec_err(res.jrk, jrk).max() < 1e-10
+
+
+@pytest.mark.parametrize("m_flag", [0, 1])
+def test_double_float_kernel_meets_fp64_accuracy_at_every_particle(lib, plummer64k, m_flag):
+    """gpunb_set_precision(2): force, jerk and potential of every sampled
+    particle (512 rows) of a 16384 block of the Plummer 65536 cluster within
+    1e-10 of the FP64 oracle in plain relative terms -- no cancellation
+    allowance -- and the lists identical (the golden cases run in this mode
+    too, test_golden_cases)."""
+    c = plummer64k
+    act = ics.active_set(c.n, 16384, seed=9)
+    h2 = c.h2() / (c.m.mean() if m_flag else 1.0)
+    samp = np.linspace(0, act.size - 1, 512).astype(int)
+    with GpuNb(c.n) as nb:
+        nb.set_precision("double_float")
+        nb.send(c.m, c.x, c.v)
+        res = nb.regf(h2[act], c.dtr[act], c.x[act], c.v[act], 513, 512, m_flag=m_flag)
+        nb.set_precision("split")
+    a = act[samp]
+    acc, jrk, pot, lst = O.regf_fp64(c.m, c.x, c.v, h2[a], c.dtr[a], c.x[a], c.v[a], 513, 512,
+                                     m_flag=m_flag)
+    assert rows_equal(res.list[samp], lst) == []
+    assert rel_vec_err(res.acc[samp], acc).max() < DF_TOL
+    assert rel_vec_err(res.jrk[samp], jrk).max() < DF_TOL
+    assert (np.abs(res.pot[samp] - pot) / pot).max() < DF_TOL
 
 
 def test_edge_cases(lib):
