@@ -88,7 +88,8 @@ void gpunb_set_abort_on_error(int flag);    /* 1 (default): print + abort() */
  * 1 = plain FP64, 2 = double-float (every pair in hi + lo pairs of floats on
  * the FP32 pipe: FP64-class results, within ~1e-11 of FP64, several times
  * faster than FP64 on GB300; lists identical to FP64).  The batched entry
- * points always use the split kernel. */
+ * points always use the split kernel.  gpunb_open_ resets the mode to the
+ * environment variable GPUNB_PRECISION (0 when unset). */
 void gpunb_set_precision(int mode);
 
 /* Force a launch shape (variant index, j-splits; for the batched entry

@@ -1017,8 +1017,13 @@ void gpunb_open_(int *nbmax, int *irank) {
       !g.hj.ensure(nmax * 7 * sizeof(double)))
     return;
   g.nj = 0;
-  // a new run starts from the default configuration
+  // a new run starts from the default configuration (GPUNB_PRECISION: the
+  // pair kernel, as gpunb_set_precision)
   g.precision = 0;
+  if (const char *p = getenv("GPUNB_PRECISION")) {
+    const int v = atoi(p);
+    g.precision = (v == 1 || v == 2) ? v : 0;
+  }
   g.force_variant = -1;
   g.force_splits = 0;
   g.timing = 0;
