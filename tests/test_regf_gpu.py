@@ -249,6 +249,51 @@ def test_double_float_kernel_meets_fp64_accuracy_at_every_particle(lib, plummer6
     assert (np.abs(res.pot[samp] - pot) / pot).max() < DF_TOL
 
 
+_PRECISION_CHILD = """
+import sys, hashlib
+sys.path[:0] = [{root!r}, {tests!r}]
+from conftest import load_golden
+from nbody6ppgpu_gb300.gpunb import GpuNb
+g = load_golden("plummer2048_equal")
+ii = g["ii"]
+for explicit in (None, {name!r}):
+    with GpuNb(len(g["m"])) as nb:
+        if explicit:
+            nb.set_precision(explicit)
+        nb.send(g["m"], g["x"], g["v"])
+        r = nb.regf(g["h2"], g["dtr"], g["x"][ii], g["v"][ii], int(g["lmax"]),
+                    int(g["nnbmax"]), int(g["m_flag"]))
+    print("DIGEST", hashlib.sha256(r.acc.tobytes() + r.jrk.tobytes() + r.pot.tobytes()
+                                   + r.list.tobytes()).hexdigest())
+"""
+
+
+def test_precision_from_the_environment_at_open(lib):
+    """gpunb_open_ takes the pair kernel from GPUNB_PRECISION: a process that
+    sets it to 1 (or 2) and never calls gpunb_set_precision gets the bits of
+    the FP64 (or double-float) kernel; unset or 0 gives the split kernel."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    seen = []
+    for mode, name in ((None, "split"), ("0", "split"), ("1", "fp64"), ("2", "double_float")):
+        env = dict(os.environ)
+        env.pop("GPUNB_PRECISION", None)
+        if mode is not None:
+            env["GPUNB_PRECISION"] = mode
+        src = _PRECISION_CHILD.format(root=str(root), tests=str(root / "tests"), name=name)
+        r = subprocess.run([sys.executable, "-c", src], capture_output=True, text=True,
+                           timeout=600, env=env)
+        assert r.returncode == 0, r.stderr[-2000:]
+        from_env, explicit = [ln.split()[1] for ln in r.stdout.splitlines()
+                              if ln.startswith("DIGEST")]
+        assert from_env == explicit, mode
+        seen.append(from_env)
+    assert seen[0] == seen[1] and len(set(seen)) == 3
+
+
 def test_edge_cases(lib):
     c = ics.plummer(300, seed=8, nb_target=10.0)
     with GpuNb(1000) as nb:
