@@ -1058,14 +1058,35 @@ __global__ void __launch_bounds__(128) regf_df_kernel(const JSet js, const ISet 
       const dfl dvy = df_diff(svh[3 * jj + 1], svl[3 * jj + 1], vh[1], vl[1]);
       const dfl dvz = df_diff(svh[3 * jj + 2], svl[3 * jj + 2], vh[2], vl[2]);
       const dfl r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
-      const dfl px = df_add(dx, df_mul(dvx, dtr));
-      const dfl py = df_add(dy, df_mul(dvy, dtr));
-      const dfl pz = df_add(dz, df_mul(dvz, dtr));
-      const dfl r2p = df_add(df_add(df_sqr(px), df_sqr(py)), df_sqr(pz));
-      const bool pless = r2p.h < r2.h || (r2p.h == r2.h && r2p.l < r2.l);
-      const dfl r2min = pless ? r2p : r2;
       const dfl m = {smh[jj], sml[jj]};
       const dfl crit = MFLAG ? df_mul(m, h2) : h2;
+      // r_p^2 in double-float only where it can decide: an FP32 lower bound
+      // first -- each predicted component from the heads, less 2^-21 of the
+      // magnitudes involved (the tails are at most 2^-24 of their heads and
+      // the FMA rounds once: several times the worst case); NaN or infinite
+      // inputs give a bound of 0.  Where the bound clears the criterion by
+      // 2^-16, r_p^2 is no smaller than the criterion, so min(r^2, r_p^2)
+      // decides exactly as r^2 alone does.
+      dfl r2min = r2;
+      {
+        const float qx = fmaf(dvx.h, dtr.h, dx.h), qy = fmaf(dvy.h, dtr.h, dy.h),
+                    qz = fmaf(dvz.h, dtr.h, dz.h);
+        const float dt = fabsf(dtr.h);
+        const float ax = fmaxf(fabsf(qx) - 0x1p-21f * (fabsf(qx) + fmaf(fabsf(dvx.h), dt,
+                                                                        fabsf(dx.h))), 0.f);
+        const float ay = fmaxf(fabsf(qy) - 0x1p-21f * (fabsf(qy) + fmaf(fabsf(dvy.h), dt,
+                                                                        fabsf(dy.h))), 0.f);
+        const float az = fmaxf(fabsf(qz) - 0x1p-21f * (fabsf(qz) + fmaf(fabsf(dvz.h), dt,
+                                                                        fabsf(dz.h))), 0.f);
+        const float lb = fmaf(ax, ax, fmaf(ay, ay, az * az));
+        if (!(lb >= fmaf(crit.h, 1.0f + 0x1p-16f, 0x1p-100f))) {
+          const dfl px = df_add(dx, df_mul(dvx, dtr));
+          const dfl py = df_add(dy, df_mul(dvy, dtr));
+          const dfl pz = df_add(dz, df_mul(dvz, dtr));
+          const dfl r2p = df_add(df_add(df_sqr(px), df_sqr(py)), df_sqr(pz));
+          if (r2p.h < r2.h || (r2p.h == r2.h && r2p.l < r2.l)) r2min = r2p;
+        }
+      }
       const dfl diff = df_add(r2min, {-crit.h, -crit.l});
       bool in;
       if (fabsf(diff.h) <= 0x1p-40f * fabsf(crit.h))
